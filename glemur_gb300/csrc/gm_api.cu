@@ -1,0 +1,576 @@
+// gm_api.cu -- the C-ABI of include/glemur.h over the relaxation kernels.
+//
+// A handle owns every device buffer of one relaxation (src/memory.cu:10-95
+// allocates the reference's), a stream, the device-resident controller state
+// and a CUDA graph of one attempted step (6 stage launches + the control
+// launch), so a run is graph replays with no host round trip per step; the
+// reference instead synchronises after every launch and copies maxDelta to the
+// host each step (src/main.cu:259-384, src/maths.cu:101-130).
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "glemur.h"
+#include "gm_internal.h"
+#include "gm_kernels.cuh"
+
+using gmk::DevState;
+using gmk::KP;
+using gmk::StageArgs;
+
+namespace {
+
+#define CUDA_TRY(x)                                                                        \
+    do {                                                                                   \
+        cudaError_t e_ = (x);                                                              \
+        if (e_ != cudaSuccess)                                                             \
+            return gm::fail(GM_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_));    \
+    } while (0)
+
+int check_params(const gm_params* p) {
+    if (!p) return gm::fail(GM_EPARAM, "null params");
+    if (p->precision != 32 && p->precision != 64) return gm::fail(GM_EPARAM, "precision must be 32 or 64");
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3) return gm::fail(GM_EPARAM, "nx, ny, nz must be >= 3");
+    if ((long long)p->nx * p->ny * p->nz > (1ll << 31)) return gm::fail(GM_EPARAM, "grid too large");
+    if (strncmp(p->jMethod, "Stokes ", 7) != 0)
+        return gm::fail(GM_EPARAM, "jMethod: only the Stokes current (the reference default) is implemented");
+    if (p->pressure && strncmp(p->pMethod, "Classic ", 8) != 0) return gm::fail(GM_EPARAM, "pMethod must be Classic");
+    if (p->inertia) return gm::fail(GM_EPARAM, "inertia = T is not implemented");
+    if (p->jxbAver) return gm::fail(GM_EPARAM, "jxbAver = T is not implemented");
+    if (p->initShearA != 0 || p->initShearB != 0)
+        return gm::fail(GM_EPARAM, "initial-distortion ghost corrections (initShearA/B != 0) are not implemented");
+    if (!(p->dx > 0 && p->dy > 0 && p->dz > 0)) return gm::fail(GM_EPARAM, "dx, dy, dz must be > 0 (call gm_params_derive)");
+    if (p->errMode != 0 && p->errMode != 1) return gm::fail(GM_EPARAM, "errMode must be 0 or 1");
+    return GM_OK;
+}
+
+struct ImplBase {
+    virtual ~ImplBase() {}
+    virtual int upload(const void* xb, const void* B0, double t, double dt) = 0;
+    virtual int stage(int n) = 0;
+    virtual int control() = 0;
+    virtual int steps_async(int n) = 0;
+    virtual int run(int nCycle, gm_state* out) = 0;
+    virtual int get_state(gm_state* out) = 0;
+    virtual int set_dt(double t, double dt, int timeIndex) = 0;
+    virtual int refresh(gm_reduction* r) = 0;
+    virtual int download(void* xb, void* B, void* J, void* D) = 0;
+    virtual int download_k(int m, void* k) = 0;
+    virtual int download_x(int which, void* xb) = 0;
+    virtual int step(gm_step_result* r) = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    int64_t launches = 0;
+    bool uploaded = false;
+};
+
+template <typename T>
+struct Impl : ImplBase {
+    gm_params gp;
+    KP<T> kp;
+    // device buffers
+    T* X[2] = {nullptr, nullptr};
+    T* XS[2] = {nullptr, nullptr};
+    T* K[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    T* B0 = nullptr;
+    T* outB = nullptr;
+    T* outJ = nullptr;
+    T* outD = nullptr;
+    T* stage_buf = nullptr;     // ghosted AoS staging for transfers
+    T* eps = nullptr;           // ex | ey | ez
+    DevState* st = nullptr;
+    double* log = nullptr;
+    double* part = nullptr;
+    double* red = nullptr;
+    DevState* h_st = nullptr;   // pinned
+    double* h_red = nullptr;    // pinned
+    int logCap = 0;
+    // launch shape
+    int TY = 8, TZ = 32;
+    dim3 grid, block;
+    size_t smem_stage = 0, smem_diag = 0;
+    int nparts = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    size_t NG = 0, N = 0, NP = 0;
+
+    ~Impl() override {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        void* ptrs[] = {X[0], X[1], XS[0], XS[1], K[0], K[1], K[2], K[3], K[4], B0, outB, outJ,
+                        outD, stage_buf, eps, st, log, part, red};
+        for (void* q : ptrs)
+            if (q) cudaFree(q);
+        if (h_st) cudaFreeHost(h_st);
+        if (h_red) cudaFreeHost(h_red);
+        if (own_stream) cudaStreamDestroy(own_stream);
+    }
+
+    int alloc(void** pp, size_t bytes) {
+        cudaError_t e = cudaMalloc(pp, bytes);
+        if (e != cudaSuccess) return gm::fail(GM_EALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        e = cudaMemsetAsync(*pp, 0, bytes, stream);
+        if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
+        return GM_OK;
+    }
+
+    int init(const gm_params* p) {
+        gp = *p;
+        CUDA_TRY(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+        stream = own_stream;
+        CUDA_TRY(gmk::prepare_kernels<T>());
+        const int nx = p->nx, ny = p->ny, nz = p->nz;
+        memset(&kp, 0, sizeof kp);
+        kp.nx = nx; kp.ny = ny; kp.nz = nz;
+        kp.px = ((nx + 4) + 7) / 8 * 8;
+        kp.py = ny + 4;
+        kp.pz = nz + 4;
+        kp.cs = ((long long)kp.px * kp.py * kp.pz + 63) / 64 * 64;
+        kp.N = (long long)nx * ny * nz;
+        kp.dx = (T)p->dx; kp.dy = (T)p->dy; kp.dz = (T)p->dz;
+        kp.dx1 = (T)p->dx1; kp.dy1 = (T)p->dy1; kp.dz1 = (T)p->dz1;
+        kp.Lx = (T)p->Lx; kp.Ly = (T)p->Ly; kp.Lz = (T)p->Lz;
+        kp.Ox = (T)p->Ox; kp.Oy = (T)p->Oy; kp.Oz = (T)p->Oz;
+        kp.xPeri = p->xPeri != 0; kp.yPeri = p->yPeri != 0; kp.zPeri = p->zPeri != 0;
+        kp.zUpdate = p->zUpdate != 0;
+        kp.errMode = p->errMode;
+        kp.refDt = p->errMode == 0;
+        kp.beta = (T)p->beta;
+        kp.p0Amp = (T)p->p0Amp;
+        kp.p0W2 = (T)(p->p0Width * p->p0Width);
+        kp.maxError = (double)(T)p->maxError;
+        kp.dtMin = (double)(T)p->dtMin;
+        kp.ar = p->ar; kp.az = p->az; kp.phi1 = p->phi1;
+        kp.wantXbAn = p->redErrXb_XbAn != 0;
+        // Cash-Karp tableau, src/rungeKutta.cu:10-25
+        static const double bd[7][6] = {
+            {0, 0, 0, 0, 0, 0},
+            {0.2, 0, 0, 0, 0, 0},
+            {3 / 40., 9 / 40., 0, 0, 0, 0},
+            {0.3, -0.9, 1.2, 0, 0, 0},
+            {-11 / 54., 2.5, -70 / 27., 35 / 27., 0, 0},
+            {1631 / 55296., 175 / 512., 575 / 13824., 44275 / 110592., 253 / 4096., 0},
+            {0, 0, 0, 0, 0, 0}};
+        static const double cd[6] = {37 / 378., 0, 250 / 621., 125 / 594., 0, 512 / 1771.};
+        static const double csd[6] = {2825 / 27648., 0, 18575 / 48384., 13525 / 55296., 277 / 14336., 0.25};
+        for (int n = 0; n < 6; n++)
+            for (int m = 0; m < 6; m++) kp.db[n][m] = (T)bd[n + 1][m] - (T)bd[n][m];
+        for (int m = 0; m < 6; m++) {
+            kp.c[m] = (T)cd[m];
+            kp.cst[m] = (T)csd[m];
+            kp.cmc[m] = (double)(T)cd[m] - (double)(T)csd[m];
+        }
+        NG = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+        N = (size_t)kp.N;
+        NP = (size_t)kp.cs * 3;
+        int rc;
+        for (int q = 0; q < 2; q++) {
+            if ((rc = alloc((void**)&X[q], NP * sizeof(T)))) return rc;
+            if ((rc = alloc((void**)&XS[q], NP * sizeof(T)))) return rc;
+        }
+        for (int m = 0; m < 5; m++)
+            if ((rc = alloc((void**)&K[m], 3 * N * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&B0, NP * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&outB, 3 * NG * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&outJ, 3 * N * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&outD, NG * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&stage_buf, 3 * NG * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&eps, (size_t)(nx + ny + nz) * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&st, sizeof(DevState)))) return rc;
+        logCap = 1 << 16;
+        if ((rc = alloc((void**)&log, (size_t)3 * logCap * sizeof(double)))) return rc;
+        CUDA_TRY(cudaMallocHost((void**)&h_st, sizeof(DevState)));
+        CUDA_TRY(cudaMallocHost((void**)&h_red, gmk::R_COUNT * sizeof(double)));
+        // epsilon profile factors, src/rungeKutta.cu:180-185 (evaluated in double)
+        {
+            std::vector<T> e((size_t)nx + ny + nz);
+            const int n3[3] = {nx, ny, nz};
+            size_t o = 0;
+            for (int a = 0; a < 3; a++)
+                for (int i = 0; i < n3[a]; i++) {
+                    const int n = n3[a];
+                    e[o++] = p->epsilonProf ? (T)(-(i - n / 2.) / n * (i + 1 - n / 2.) / n * 4 + 1) : (T)1;
+                }
+            CUDA_TRY(cudaMemcpyAsync(eps, e.data(), e.size() * sizeof(T), cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaStreamSynchronize(stream));
+        }
+        kp.ex = eps;
+        kp.ey = eps + nx;
+        kp.ez = eps + nx + ny;
+        // launch shape: 32 x TY column tiles, TZ planes per CTA; enough CTAs
+        // for two waves over the 152 SMs where the grid allows it
+        const int nbx = (nx + gmk::TX - 1) / gmk::TX;
+        auto nctas = [&](int ty, int tz) { return (long long)nbx * ((ny + ty - 1) / ty) * ((nz + tz - 1) / tz); };
+        TY = 8;
+        TZ = 32;
+        while (TZ > 4 && nctas(TY, TZ) < 2 * 152) TZ /= 2;
+        while (TY > 2 && nctas(TY, TZ) < 2 * 152) TY /= 2;
+        grid = dim3((unsigned)nbx, (unsigned)((ny + TY - 1) / TY), (unsigned)((nz + TZ - 1) / TZ));
+        block = dim3(gmk::TX, (unsigned)TY, 1);
+        smem_stage = gmk::stage_smem_bytes<T>(TY, gmk::MODE_STAGE, p->pressure);
+        smem_diag = gmk::stage_smem_bytes<T>(TY, gmk::MODE_DIAG, p->pressure);
+        nparts = (int)(grid.x * grid.y * grid.z);
+        if ((rc = alloc((void**)&part, (size_t)nparts * gmk::R_COUNT * sizeof(double)))) return rc;
+        if ((rc = alloc((void**)&red, gmk::R_COUNT * sizeof(double)))) return rc;
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    StageArgs<T> args(int n) {
+        StageArgs<T> a;
+        memset(&a, 0, sizeof a);
+        a.p = kp;
+        a.X[0] = X[0]; a.X[1] = X[1];
+        a.XS[0] = XS[0]; a.XS[1] = XS[1];
+        for (int m = 0; m < 5; m++) a.K[m] = K[m];
+        a.B0 = B0;
+        a.st = st;
+        a.log = log;
+        a.n = n;
+        a.TZ = TZ;
+        a.outB = outB; a.outJ = outJ; a.outD = outD;
+        a.part = part;
+        return a;
+    }
+
+    int upload(const void* xb, const void* b0, double t, double dt) override {
+        if (!xb || !b0) return gm::fail(GM_EPARAM, "gm_upload: null array");
+        const size_t bytes = 3 * NG * sizeof(T);
+        CUDA_TRY(cudaMemcpyAsync(stage_buf, b0, bytes, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(gmk::launch_unpack<T>(kp, stage_buf, B0, stream));
+        CUDA_TRY(cudaMemcpyAsync(outB, stage_buf, bytes, cudaMemcpyDeviceToDevice, stream));   // main.cu:195
+        CUDA_TRY(cudaMemcpyAsync(stage_buf, xb, bytes, cudaMemcpyHostToDevice, stream));
+        T* bufs[4] = {X[0], X[1], XS[0], XS[1]};
+        for (T* b : bufs) {
+            CUDA_TRY(gmk::launch_unpack<T>(kp, stage_buf, b, stream));
+            CUDA_TRY(gmk::launch_images<T>(kp, b, stream));
+        }
+        launches += 10;
+        DevState s;
+        memset(&s, 0, sizeof s);
+        s.t = gp.errMode == 0 ? (double)(T)t : t;
+        s.dt = gp.errMode == 0 ? (double)(T)dt : dt;
+        s.target = INT_MAX;
+        s.logCap = logCap;
+        s.done = !(s.dt > kp.dtMin);
+        *h_st = s;
+        CUDA_TRY(cudaMemcpyAsync(st, h_st, sizeof s, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        uploaded = true;
+        return GM_OK;
+    }
+
+    int stage(int n) override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_stage before gm_upload");
+        if (n < 0 || n > 5) return gm::fail(GM_EPARAM, "stage index must be 0..5");
+        StageArgs<T> a = args(n);
+        CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_STAGE, gp.pressure, grid, block, smem_stage, stream));
+        launches++;
+        return GM_OK;
+    }
+
+    int control() override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_control before gm_upload");
+        CUDA_TRY(gmk::launch_control<T>(kp, st, log, stream));
+        launches++;
+        return GM_OK;
+    }
+
+    int enqueue_step() {
+        int rc;
+        for (int n = 0; n < 6; n++)
+            if ((rc = stage(n))) return rc;
+        return control();
+    }
+
+    int steps_async(int nsteps) override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_steps_async before gm_upload");
+        if (nsteps <= 0) return GM_OK;
+        if (!gexec) {
+            // capture one attempted step on a private stream
+            cudaStream_t cs;
+            CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            cudaStream_t saved = stream;
+            int64_t saved_launches = launches;
+            stream = cs;
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            int rc = e == cudaSuccess ? enqueue_step() : GM_ECUDA;
+            cudaGraph_t g = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+            stream = saved;
+            launches = saved_launches;
+            cudaStreamDestroy(cs);
+            if (e != cudaSuccess || rc != GM_OK || e2 != cudaSuccess)
+                return gm::fail(GM_ECUDA, "capture of the step graph failed");
+            graph = g;
+            CUDA_TRY(cudaGraphInstantiate(&gexec, graph, 0));
+        }
+        for (int s = 0; s < nsteps; s++) {
+            CUDA_TRY(cudaGraphLaunch(gexec, stream));
+            launches += 7;
+        }
+        return GM_OK;
+    }
+
+    int read_state() {
+        CUDA_TRY(cudaMemcpyAsync(h_st, st, sizeof(DevState), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    void fill(gm_state* o) {
+        o->t = h_st->t;
+        o->dt = h_st->dt;
+        o->maxDelta = h_st->maxDelta;
+        o->timeIndex = h_st->timeIndex;
+        o->nAttempted = h_st->nAttempted;
+        o->nRejected = h_st->nRejected;
+        o->status = h_st->status;
+    }
+
+    int get_state(gm_state* out) override {
+        int rc = read_state();
+        if (rc) return rc;
+        if (out) fill(out);
+        return GM_OK;
+    }
+
+    int set_control(int target, bool reset_done) {
+        int rc = read_state();
+        if (rc) return rc;
+        h_st->target = target;
+        if (reset_done) {
+            h_st->done = !(h_st->dt > kp.dtMin) || (h_st->status & GM_ST_NAN) || h_st->timeIndex >= target;
+            if (!h_st->done) h_st->status &= ~(unsigned)GM_ST_DONE;
+        }
+        CUDA_TRY(cudaMemcpyAsync(st, h_st, sizeof(DevState), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    int set_dt(double t, double dt, int timeIndex) override {
+        int rc = read_state();
+        if (rc) return rc;
+        h_st->t = gp.errMode == 0 ? (double)(T)t : t;
+        h_st->dt = gp.errMode == 0 ? (double)(T)dt : dt;
+        h_st->timeIndex = timeIndex;
+        h_st->done = !(h_st->dt > kp.dtMin);
+        CUDA_TRY(cudaMemcpyAsync(st, h_st, sizeof(DevState), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    int run(int nCycle, gm_state* out) override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_run before gm_upload");
+        int rc = read_state();
+        if (rc) return rc;
+        const long long tgt = (long long)h_st->timeIndex + nCycle;
+        if ((rc = set_control(tgt > INT_MAX ? INT_MAX : (int)tgt, true))) return rc;
+        // graph replays in chunks; steps after the stop rule do no work
+        int chunk = 16;
+        while (!h_st->done) {
+            if ((rc = steps_async(chunk))) return rc;
+            if ((rc = read_state())) return rc;
+            if (chunk < 256) chunk *= 2;
+        }
+        if (out) fill(out);
+        if (h_st->status & GM_ST_NAN) return gm::fail(GM_ENAN, "NaN/Inf in a stage increment");
+        return GM_OK;
+    }
+
+    int refresh(gm_reduction* r) override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_refresh before gm_upload");
+        StageArgs<T> a = args(0);
+        CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_DIAG, gp.pressure, grid, block, smem_diag, stream));
+        CUDA_TRY(gmk::launch_finalize<T>(part, nparts, red, stream));
+        CUDA_TRY(gmk::launch_export_ghosts<T>(kp, outB, outD, stream));
+        launches += 2 + kp.xPeri + kp.yPeri + kp.zPeri;
+        CUDA_TRY(cudaMemcpyAsync(h_red, red, gmk::R_COUNT * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        if (r) {
+            const double* v = h_red;
+            r->B2 = v[gmk::R_SUM_B2W] * gp.dx * gp.dy * gp.dz;
+            r->residual = v[gmk::R_SUM_JB] > 0 ? v[gmk::R_SUM_CROSS] / v[gmk::R_SUM_JB] : 0.0;
+            r->residualPw = v[gmk::R_SUM_PW] / (double)N;
+            r->BMax = v[gmk::R_MAX_B];
+            r->JMax = v[gmk::R_MAX_J];
+            r->JxB_B2Max = v[gmk::R_MAX_JXBB2];
+            r->minDetJac = v[gmk::R_MIN_DET];
+            r->wedgeMin = v[gmk::R_MIN_WEDGE];
+            r->convex = v[gmk::R_MIN_CONVEX];
+            r->errB_1ez = sqrt(v[gmk::R_SUM_E1]) / sqrt((double)N);
+            r->errXb_XbAn = sqrt(v[gmk::R_SUM_E2]) / sqrt((double)N);
+        }
+        return GM_OK;
+    }
+
+    int download(void* xb, void* B, void* J, void* D) override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_download before gm_upload");
+        if (xb) {
+            int rc = read_state();
+            if (rc) return rc;
+            CUDA_TRY(gmk::launch_pack<T>(kp, X[h_st->cur], stage_buf, stream));
+            launches++;
+            CUDA_TRY(cudaMemcpyAsync(xb, stage_buf, 3 * NG * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        }
+        if (B) CUDA_TRY(cudaMemcpyAsync(B, outB, 3 * NG * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        if (J) CUDA_TRY(cudaMemcpyAsync(J, outJ, 3 * N * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        if (D) CUDA_TRY(cudaMemcpyAsync(D, outD, NG * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    int step(gm_step_result* r) override {
+        int rc = enqueue_step();
+        if (rc) return rc;
+        if ((rc = read_state())) return rc;
+        if (r) {
+            r->maxDelta = h_st->maxDelta;
+            r->t = h_st->t;
+            r->dt = h_st->dt;
+            r->accepted = h_st->lastAccepted;
+            r->timeIndex = h_st->timeIndex;
+            r->status = h_st->status;
+            r->pad = 0;
+        }
+        return GM_OK;
+    }
+
+    int download_k(int m, void* k) override {
+        if (m < 0 || m > 4 || !k) return gm::fail(GM_EPARAM, "gm_download_k: m must be 0..4");
+        CUDA_TRY(gmk::launch_pack_k<T>(kp, K[m], stage_buf, stream));
+        launches++;
+        CUDA_TRY(cudaMemcpyAsync(k, stage_buf, 3 * N * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    int download_x(int which, void* xb) override {
+        if (which < 0 || which > 6 || !xb) return gm::fail(GM_EPARAM, "gm_download_x: which must be 0..6");
+        int rc = read_state();
+        if (rc) return rc;
+        const int cur = h_st->cur;
+        T* src = which <= 4 ? XS[which & 1] : (which == 5 ? X[cur] : X[cur ^ 1]);
+        CUDA_TRY(gmk::launch_pack<T>(kp, src, stage_buf, stream));
+        launches++;
+        CUDA_TRY(cudaMemcpyAsync(xb, stage_buf, 3 * NG * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+};
+
+}  // namespace
+
+struct gm_handle {
+    std::unique_ptr<ImplBase> impl;
+    int precision;
+};
+
+extern "C" {
+
+int gm_create(const gm_params* p, gm_handle** out) {
+    if (!out) return gm::fail(GM_EPARAM, "gm_create: null output");
+    *out = nullptr;
+    int rc = check_params(p);
+    if (rc) return rc;
+    gm_handle* h = new gm_handle();
+    h->precision = p->precision;
+    if (p->precision == 32) {
+        auto* im = new Impl<float>();
+        h->impl.reset(im);
+        rc = im->init(p);
+    } else {
+        auto* im = new Impl<double>();
+        h->impl.reset(im);
+        rc = im->init(p);
+    }
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GM_OK;
+}
+
+int gm_destroy(gm_handle* h) {
+    if (!h) return GM_OK;
+    if (h->impl && h->impl->stream) cudaStreamSynchronize(h->impl->stream);
+    delete h;
+    return GM_OK;
+}
+
+int gm_set_stream(gm_handle* h, void* stream) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    h->impl->stream = stream ? (cudaStream_t)stream : h->impl->own_stream;
+    return GM_OK;
+}
+
+int gm_upload(gm_handle* h, const void* xb, const void* B0, double t, double dt) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->upload(xb, B0, t, dt);
+}
+
+int gm_stage(gm_handle* h, int n) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->stage(n);
+}
+
+int gm_control(gm_handle* h) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->control();
+}
+
+int gm_step(gm_handle* h, gm_step_result* r) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->step(r);
+}
+
+int gm_steps_async(gm_handle* h, int nSteps) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->steps_async(nSteps);
+}
+
+int gm_run(gm_handle* h, int nCycle, gm_state* out) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->run(nCycle, out);
+}
+
+int gm_get_state(gm_handle* h, gm_state* out) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->get_state(out);
+}
+
+int gm_set_dt(gm_handle* h, double t, double dt, int timeIndex) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->set_dt(t, dt, timeIndex);
+}
+
+int gm_refresh(gm_handle* h, gm_reduction* r) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->refresh(r);
+}
+
+int gm_download(gm_handle* h, void* xb, void* B, void* J, void* detJac) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->download(xb, B, J, detJac);
+}
+
+int gm_download_k(gm_handle* h, int m, void* k) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->download_k(m, k);
+}
+
+int gm_download_x(gm_handle* h, int which, void* xb) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->download_x(which, xb);
+}
+
+int64_t gm_launch_count(const gm_handle* h) { return h ? h->impl->launches : 0; }
+
+}  // extern "C"

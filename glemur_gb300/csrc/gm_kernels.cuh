@@ -1,0 +1,124 @@
+// gm_kernels.cuh -- device kernels of the relaxation hot path.
+//
+// One Runge-Kutta stage is one kernel launch.  Each CTA owns a column tile of
+// TX x TY points and marches through a chunk of TZ planes.  Grid positions of
+// the stage are read plane by plane into a ring of 5 shared-memory planes
+// (tile + 2-point halo); B = jac.B0/Delta is computed once per point on the
+// tile + 1-point face halo into a ring of 4 B planes; the Stokes current J,
+// the stage increment k_n = dt eps (J x B) [- dt grad p] and the next stage
+// position are formed at the tile points.  Stage 5 also forms x_new, x* and
+// the error norm and reduces its maximum.  So the reference's per-stage
+// sequence B_JacB0 + updateBbound + setPeriFace + JStokes + kk + setGridPeri
+// + cudaMemcpy (src/main.cu:260-307) and xNewStar + findDevMax
+// (main.cu:309-319) become six launches per step, and the accept/reject rule
+// (main.cu:321-383) a seventh single-thread launch.
+//
+// Storage (all SoA, component-major):
+//   positions: padded with 2 ghost layers per side, index
+//              (i+2) + px*((j+2) + py*(k+2)), component stride cs.  Periodic
+//              ghost layers hold the shifted images x -/+ (L + d) of the inner
+//              points (boundaries.cu:532-582), written by the stage that
+//              produces the positions; non-periodic ghost layers hold the
+//              fixed line-tied positions of the initial grid.
+//   B0:        same padded layout (ghost depth 1 used).
+//   k_m:       inner points only, index i + nx*(j + ny*k), component stride N.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gmk {
+
+constexpr int TX = 32;          // tile width in x = one warp
+constexpr int XRING = 5;        // planes of positions held in shared memory
+constexpr int BRING = 4;        // planes of B held in shared memory
+
+// Device-resident controller state (one per handle).
+struct DevState {
+    double t, dt, maxDelta;
+    unsigned long long maxDeltaBits;   // running max of the error norm (bits of a non-negative double)
+    int timeIndex;                     // accepted steps (main.cu loop index)
+    int nAttempted, nRejected;
+    int cur;                           // which of X[0], X[1] holds the step's start grid
+    int target;                        // stop once timeIndex >= target
+    unsigned status;                   // GM_ST_* bits
+    int done;
+    int logCap;
+    int lastAccepted;                  // outcome of the last attempted step
+};
+
+// Kernel-side run parameters (passed by value; REAL = T).
+template <typename T>
+struct KP {
+    int nx, ny, nz;
+    int px, py, pz;          // padded extents
+    long long cs;            // component stride of padded arrays
+    long long N;             // nx*ny*nz
+    T dx, dy, dz, dx1, dy1, dz1;
+    T Lx, Ly, Lz, Ox, Oy, Oz;
+    int xPeri, yPeri, zPeri, zUpdate, errMode, refDt;
+    T beta, p0Amp, p0W2;     // pressure: p0(X) = beta (1 + p0Amp exp(-(X^2+Y^2)/p0W2))
+    double maxError, dtMin;  // run-precision values widened to double
+    T db[6][6];              // b[n+1][m] - b[n][m] of the Cash-Karp tableau
+    T c[6], cst[6];          // 5th- and 4th-order weights
+    double cmc[6];           // c - c* in double (error norm of errMode 1)
+    double ar, az, phi1;     // analytic-field parameters (distance-to-analytic diagnostic)
+    int wantXbAn;
+    const T* ex;             // epsilon profile factors per axis (rungeKutta.cu:180-185)
+    const T* ey;
+    const T* ez;
+};
+
+enum { MODE_STAGE = 0, MODE_DIAG = 1 };
+
+// Reduction partial of one CTA (diagnostic mode).
+enum {
+    R_SUM_CROSS = 0, R_SUM_JB, R_SUM_PW, R_SUM_B2W, R_SUM_E1, R_SUM_E2,
+    R_MAX_JXBB2, R_MAX_B, R_MAX_J,
+    R_MIN_DET, R_MIN_WEDGE, R_MIN_CONVEX,
+    R_COUNT
+};
+
+template <typename T>
+struct StageArgs {
+    KP<T> p;
+    T* X[2];                 // start / new grid (roles swap on accept)
+    T* XS[2];                // stage positions, ping-pong
+    T* K[5];                 // k_0..k_4
+    const T* B0;
+    DevState* st;
+    double* log;             // per attempt: maxDelta, dt after the update, accepted
+    int n;                   // stage index 0..5
+    int TZ;                  // planes per CTA
+    // diagnostic mode outputs (reference layout) and partials
+    T* outB;                 // ghosted AoS
+    T* outJ;                 // inner AoS
+    T* outD;                 // ghosted scalar detJac
+    double* part;            // R_COUNT per CTA
+};
+
+// Host-side launchers (explicitly instantiated for float and double).
+template <typename T>
+cudaError_t launch_stage(const StageArgs<T>& a, int mode, int pressure, dim3 grid, dim3 block, size_t smem,
+                         cudaStream_t s);
+template <typename T>
+size_t stage_smem_bytes(int TY, int mode, int pressure);
+template <typename T>
+cudaError_t prepare_kernels();
+template <typename T>
+cudaError_t launch_control(const KP<T>& p, DevState* st, double* log, cudaStream_t s);
+template <typename T>
+cudaError_t launch_finalize(const double* part, int nparts, double* out, cudaStream_t s);
+// ghosted AoS (reference layout) <-> padded SoA
+template <typename T>
+cudaError_t launch_unpack(const KP<T>& p, const T* aos, T* soa, cudaStream_t s);
+template <typename T>
+cudaError_t launch_pack(const KP<T>& p, const T* soa, T* aos, cudaStream_t s);
+template <typename T>
+cudaError_t launch_images(const KP<T>& p, T* soa, cudaStream_t s);
+template <typename T>
+cudaError_t launch_pack_k(const KP<T>& p, const T* k, T* aos, cudaStream_t s);
+template <typename T>
+cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t s);
+
+}  // namespace gmk

@@ -1,0 +1,251 @@
+/*
+ * glemur.h -- C-ABI of the GB300-native magneto-frictional relaxation library.
+ *
+ * The reference (SimonCan/glemur) exposes no library API: its hot path is the
+ * kernel sequence that src/main.cu:259-384 drives, configured by the Fortran
+ * namelist src/readNamelist.f90 into struct Parameters (src/global.h:44-108).
+ * Each entry point below replaces one piece of that sequence; the comment on
+ * each cites the reference code it stands in for.
+ *
+ * Conventions
+ *   - Host arrays crossing this ABI use the reference layout: AoS, component
+ *     fastest, one ghost layer, index l + 3*(i + (nx+2)*(j + (ny+2)*k)) for
+ *     ghosted fields (xb, B0, B) and l + 3*(i + nx*(j + ny*k)) for the
+ *     inner-only current J (src/rungeKutta.cu:50-51, src/current.cu:401).
+ *     detJac is ghosted and scalar.  Element type is float when
+ *     params.precision == 32 and double when it is 64 (the reference REAL,
+ *     src/global.h:20-35).
+ *   - Ownership: host buffers stay with the caller; device buffers belong to
+ *     the handle.  No entry point calls exit().
+ *   - Threading: one handle per host thread; all device work runs on the
+ *     handle's stream (gm_set_stream), never on the legacy default stream.
+ *   - Errors: every call returns GM_OK (0) or a negative GM_E* code;
+ *     gm_last_error() gives a message for the calling thread.
+ */
+#ifndef GLEMUR_H_
+#define GLEMUR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GM_STR_LEN 30
+#define GM_MAX_BLOBS 10
+
+/* Status codes. */
+#define GM_OK            0
+#define GM_EPARAM       -1   /* invalid parameter or argument                  */
+#define GM_EALLOC       -2   /* device or host allocation failed              */
+#define GM_ECUDA        -3   /* a CUDA runtime call failed                    */
+#define GM_ENAN         -4   /* NaN/Inf seen in a stage increment             */
+#define GM_EDETJAC      -5   /* a cell with detJac <= 0 was seen               */
+#define GM_EDTMIN       -6   /* dt fell to dtMin (reference stop rule)         */
+#define GM_ETIMEOUT     -7   /* a bounded device wait ran out                  */
+#define GM_ENOTREADY    -8   /* call order violated (e.g. step before upload)  */
+#define GM_EIO          -9   /* file input/output error (driver helpers)       */
+
+/* Device status bits (gm_state.status). */
+#define GM_ST_NAN        1u
+#define GM_ST_DETJAC     2u
+#define GM_ST_DTMIN      4u
+#define GM_ST_DONE       8u
+
+/*
+ * Run parameters.  Mirrors struct Parameters (src/global.h:44-108) field by
+ * field and in the same order, with REAL widened to double and bool stored
+ * as int32_t.  Real values must already be rounded to the run precision
+ * (the namelist reader in this library does that, exactly as the Fortran
+ * reader reads into REAL, src/readNamelist.f90:173-255).  Strings are blank
+ * padded to 29 characters plus a NUL, as copyString produces them
+ * (src/readNamelist.f90:267-283).  Fields after the reference's last field
+ * are extensions with no counterpart in the reference.
+ */
+typedef struct gm_params {
+    int32_t nx, ny, nz;
+    double  Lx, Ly, Lz;
+    double  Ox, Oy, Oz;
+    double  dx, dy, dz;
+    double  dx1, dy1, dz1;
+    char    bInit[GM_STR_LEN];
+    char    uInit[GM_STR_LEN];
+    double  ampl;
+    double  phi1, phi2;
+    double  L1, L2;
+    double  ar, az;
+    int32_t nBlobs;
+    double  width;
+    double  minor, major;
+    double  stretch;
+    double  bGround;
+    double  blobXc[GM_MAX_BLOBS], blobYc[GM_MAX_BLOBS], blobZc[GM_MAX_BLOBS];
+    double  blobZl[GM_MAX_BLOBS], blobTwist[GM_MAX_BLOBS], blobScale[GM_MAX_BLOBS];
+    char    initDist[GM_STR_LEN];
+    int32_t initDistCode;
+    double  initShearA, initShearB, initShearK;
+    double  pert;
+    double  twist;
+    int32_t fRestart;
+    int32_t nCycle;
+    double  dt0, dtMin, maxError;
+    int32_t zUpdate, inertia, pressure;
+    double  nu, beta;
+    int32_t jxbAver;
+    double  jxbAverWeight;
+    int32_t xPeri, yPeri, zPeri;
+    int32_t epsilonProf;
+    char    jMethod[GM_STR_LEN];
+    char    pMethod[GM_STR_LEN];
+    int32_t nTs;
+    double  dtDump, dtSave;
+    int32_t dumpJ, dumpDetJac, dumpCellVol, dumpConvexity, dumpWedgeMin;
+    int32_t redB2, redB2f, redBMax, redJMax, redJxB_B2Max, redEpsilonStar;
+    int32_t redErrB_1ez, redErrXb_XbAn, redConvex, redWedgeMin, redU2, redUMax;
+    /* ---- extensions ---- */
+    int32_t precision;   /* 32: float storage, 64: double storage (PRECISION, src/Makefile:11) */
+    int32_t errMode;     /* 0: error norm |x_new - x*| in REAL as the reference
+                            (src/rungeKutta.cu:326-333); 1: |sum (c_i - c*_i) k_i|
+                            accumulated in double (no cancellation against x)  */
+    double  p0Amp;       /* pressure profile p0(X) = beta*(1 + p0Amp*exp(-r^2/p0Width^2));
+                            p0Amp = 0 gives the reference's uniform p0 = beta  */
+    double  p0Width;
+    int32_t reserved[8];
+} gm_params;
+
+/* Result of one attempted adaptive step (src/main.cu:259-384). */
+typedef struct gm_step_result {
+    double  maxDelta;    /* max over points and components of the error norm  */
+    double  t;           /* time after the step                                */
+    double  dt;          /* step size for the next attempt                     */
+    int32_t accepted;    /* 1 if maxDelta < maxError                            */
+    int32_t timeIndex;   /* accepted-step counter after the step                */
+    uint32_t status;     /* GM_ST_* bits                                        */
+    int32_t pad;
+} gm_step_result;
+
+/* Device-resident controller state. */
+typedef struct gm_state {
+    double  t, dt, maxDelta;
+    int32_t timeIndex;   /* accepted steps so far (main.cu loop index)          */
+    int32_t nAttempted;  /* attempted steps so far                              */
+    int32_t nRejected;
+    uint32_t status;
+} gm_state;
+
+/*
+ * Reductions (src/diagnostics.cu:12-134 and src/maths.cu) plus the force-free
+ * residual this library adds.  All accumulate in double.
+ */
+typedef struct gm_reduction {
+    double B2;           /* sum B^2 detJac with 1/2,1/4,1/8 boundary weights * dx dy dz (maths.cu:647-680) */
+    double BMax;         /* max |B| over inner points                           */
+    double JMax;         /* max |J| (diagnostics.cu:15-22)                      */
+    double JxB_B2Max;    /* max |JxB|/B^2 (maths.cu:168-200)                    */
+    double residual;     /* force-free residual sum|JxB| / sum(|J||B|) over inner points: the
+                            |J||B|-weighted mean of sin(angle(J,B))                          */
+    double residualPw;   /* unweighted mean over inner points of |JxB|/(|J||B|); points with
+                            |J||B| = 0 count as 0                                            */
+    double minDetJac;    /* min detJac over inner points and the ghost planes of
+                            non-periodic faces                                  */
+    double wedgeMin;     /* min of the 8 corner wedge products (maths.cu:497-569) */
+    double convex;       /* 1 if every inner point is convex, -1 otherwise (maths.cu:573-643) */
+    double errB_1ez;     /* rms |B - e_z| (maths.cu:294-328)                    */
+    double errXb_XbAn;   /* rms |x - x_analytic| (maths.cu:332-377)             */
+} gm_reduction;
+
+typedef struct gm_handle gm_handle;
+
+/* ---- parameters ---------------------------------------------------------- */
+
+/* Fill p with the namelist defaults of src/readNamelist.f90:92-150 at the given
+ * precision (32 or 64), including the single-precision literal rounding of
+ * those defaults, and derive dx..dz1 (readNamelist.f90:185-186). */
+int gm_params_default(gm_params* p, int precision);
+
+/* Recompute dx = Lx/(nx-1), dx1 = 1/dx, ... in the run precision
+ * (src/readNamelist.f90:185-186). */
+int gm_params_derive(gm_params* p);
+
+/* Read ./params.in style namelists (&comp &start &run &io) from `path` on top
+ * of gm_params_default (src/readNamelist.f90:152-178). */
+int gm_params_read(gm_params* p, const char* path, int precision);
+
+/* ---- initial state (src/init.cu:30-384, 388-419; boundaries.cu:492-634) -- */
+
+/* Build the initial B0 and grid xb on the host, ghost layers included, as
+ * initState + initDistortion + setPeriHost + setGridPeriHost do.  Supports
+ * bInit "blobs", "homZ", "analytic" and initDist "none". */
+int gm_init_state(const gm_params* p, void* B0, void* xb);
+
+/* ---- handle lifecycle (src/memory.cu:10-95, main.cu:181-256) ------------- */
+
+int gm_create(const gm_params* p, gm_handle** out);
+int gm_destroy(gm_handle* h);
+/* Use `stream` (a cudaStream_t) for all work of h; NULL selects the handle's
+ * own non-blocking stream. */
+int gm_set_stream(gm_handle* h, void* stream);
+
+/* Copy the initial state to the device (src/main.cu:181-232). */
+int gm_upload(gm_handle* h, const void* xb, const void* B0, double t, double dt);
+
+/* ---- the relaxation hot path -------------------------------------------- */
+
+/* One Runge-Kutta stage n (0..5) at the current dt: B = jac.B0/Delta
+ * (rungeKutta.cu:28-108) with ghost fill (boundaries.cu:637-658), the Stokes
+ * current (current.cu:222-409) and k_n = dt eps JxB plus the incremental stage
+ * position (rungeKutta.cu:112-247).  Stage 5 also forms x_new, x* and the
+ * error norm (rungeKutta.cu:251-353).  Exposed for stage-level parity tests. */
+int gm_stage(gm_handle* h, int n);
+
+/* Accept/reject and dt update from the error norm of the last stage 5
+ * (src/main.cu:317-383), done on the device. */
+int gm_control(gm_handle* h);
+
+/* One attempted adaptive step (6 stages + control), synchronous; fills r. */
+int gm_step(gm_handle* h, gm_step_result* r);
+
+/* Enqueue `nSteps` attempted steps without synchronising (CUDA-graph replay).
+ * Steps after the stop rule (timeIndex >= nCycle or dt <= dtMin) do no work. */
+int gm_steps_async(gm_handle* h, int nSteps);
+
+/* Run until nCycle accepted steps (counted from the handle's timeIndex) or
+ * dt <= dtMin, as the loop of src/main.cu:259-384 (without its file output). */
+int gm_run(gm_handle* h, int nCycle, gm_state* out);
+
+/* Read the device controller state (synchronises the handle's stream). */
+int gm_get_state(gm_handle* h, gm_state* out);
+int gm_set_dt(gm_handle* h, double t, double dt, int timeIndex);
+
+/* Recompute B, detJac (ghosts included) and J at the current grid, as the
+ * post-accept refresh does (src/main.cu:342-353), and evaluate the reductions
+ * (src/diagnostics.cu:12-134).  r may be NULL. */
+int gm_refresh(gm_handle* h, gm_reduction* r);
+
+/* Copy state to host arrays (any may be NULL): xb, B ghosted AoS; J inner AoS;
+ * detJac ghosted scalar -- the arrays prepareDump copies
+ * (src/diagnostics.cu:138-152).  B, J and detJac are those of the last
+ * gm_refresh. */
+int gm_download(gm_handle* h, void* xb, void* B, void* J, void* detJac);
+
+/* Stage increments k_0..k_4 of the last step (inner AoS, 3*nx*ny*nz each, in
+ * the reference kk layout src/rungeKutta.cu:236) -- for stage parity tests. */
+int gm_download_k(gm_handle* h, int m, void* k);
+
+/* Grid buffers of the last step in the reference layout (ghosted AoS):
+ * which = 0..4: stage position x_{which+1} written by stage `which`
+ * (the xb_tmp of src/rungeKutta.cu:234); 5: x_6, the start grid of a
+ * rejected retry; 6: x_new of the combine (src/rungeKutta.cu:345). */
+int gm_download_x(gm_handle* h, int which, void* xb);
+
+/* Cumulative kernel launches issued by this handle (for accounting). */
+int64_t gm_launch_count(const gm_handle* h);
+
+const char* gm_last_error(void);
+const char* gm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GLEMUR_H_ */

@@ -1,0 +1,60 @@
+"""Parity cases shared by the golden-fixture generator and the tests.
+
+Each case is a small relaxation chosen to exercise one part of the
+reference's boundary handling:
+
+* braid_f64 / braid_f32 -- periodic x, y; line-tied z; 17 points across so the
+  line-tied ghost planes cross an edge of the reference's 16-wide launch
+  blocks (src/boundaries.cu:72-109).
+* tied_f64   -- every face line-tied (the x and y ghost-face formulas).
+* zperi_f64  -- periodic y and z, line-tied x.
+* press_f64  -- the pressure term (src/gradP.cu) with uniform p0 = beta.
+* analytic_f64 -- the reference's analytic field (src/init.cu:71-78).
+"""
+from __future__ import annotations
+
+import math
+
+from glemur_gb300 import configs
+
+
+def _braid(shape, precision, peri=(1, 1, 0)):
+    p = configs.braid2(*shape, precision=precision)
+    p.xPeri, p.yPeri, p.zPeri = peri
+    p.errMode = 0
+    return configs.derive(p)
+
+
+def make(name: str):
+    if name == "braid_f64":
+        return _braid((17, 17, 18), 64)
+    if name == "braid_f32":
+        return _braid((17, 17, 18), 32)
+    if name == "tied_f64":
+        return _braid((17, 12, 17), 64, peri=(0, 0, 0))
+    if name == "zperi_f64":
+        return _braid((12, 10, 16), 64, peri=(0, 1, 1))
+    if name == "press_f64":
+        p = _braid((12, 12, 14), 64)
+        p.pressure = 1
+        p.beta = 0.05
+        return configs.derive(p)
+    if name == "analytic_f64":
+        p = configs.defaults(64)
+        p.nx, p.ny, p.nz = 16, 16, 16
+        p.Lx, p.Ly, p.Lz = 8.0, 8.0, 20.0
+        p.Ox, p.Oy, p.Oz = -4.0, -4.0, -10.0
+        p.set_str("bInit", "analytic")
+        p.ampl = 1.0
+        p.phi1 = math.pi / 2
+        p.phi2 = -math.pi / 2
+        p.dt0 = 3e-4
+        p.dtMin = 1e-8
+        p.maxError = 5e-6
+        p.errMode = 0
+        return configs.derive(p)
+    raise KeyError(name)
+
+
+NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64"]
+N_ACCEPTED = 10

@@ -1,0 +1,139 @@
+"""CPU checks of the C-ABI library: it loads, exports every entry point the
+header declares, and its host-side logic (namelist defaults and reader,
+initial state) follows src/readNamelist.f90 and src/init.cu."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from glemur_gb300 import _abi, configs
+from oracle.pyoracle import Oracle
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    text = (ROOT / "include" / "glemur.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+\*?(gm_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_entry_point():
+    lib = _abi.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if getattr(lib, n, None) is None]
+    assert not missing, missing
+    assert set(names) == set(_abi.SIGNATURES), set(names) ^ set(_abi.SIGNATURES)
+
+
+def test_defaults_use_single_precision_literals():
+    p = configs.defaults(64)
+    assert p.dt0 == float(np.float32(3e-4)) and p.dt0 != 3e-4
+    assert p.maxError == float(np.float32(5e-5))
+    assert p.ar == float(np.float32(1.414213562373095))
+    assert p.get_str("jMethod") == "Stokes" and bytes(p.jMethod)[:7] == b"Stokes "
+    assert p.nx == 16 and p.Lz == 20.0 and p.epsilonProf == 1 and p.zUpdate == 1
+    assert p.dx == 8.0 / 15 and p.dx1 == 1.0 / (8.0 / 15)
+    q = configs.defaults(32)
+    assert q.dx == float(np.float32(8.0) / np.float32(15))
+
+
+def test_namelist_reader(tmp_path):
+    text = """
+&comp
+    nx = 20;  ny = 18;  nz = 40   ! inner mesh points
+/
+&start
+    Lx = 8;     Ly = 8;     Lz = 48
+    Ox = -4;    Oy = -4;    Oz = -24
+    bInit = "blobs"      ! comment with a / slash
+    nBlobs = 2
+    blobXc = 1.0, -1.0
+    blobYc = 2*0.0
+    blobZc(1) = -4.d0, blobZc(2) = 4
+    blobZl = 2, 2
+    blobTwist = 0.7071067811865476, -0.7071067811865476
+    blobScale = 1.4142135623730951 1.4142135623730951
+    fRestart = f
+/
+&run
+    nCycle = 2000
+    dt0 = 3e-4
+    dtMin = 1e-8
+    maxError = 1e-5
+    xPeri = True;  yPeri = .true.; zPeri = False
+    jMethod = 'Stokes'
+/
+&io
+    nTs = 5
+    dtDump = 1; dtSave = .2
+    redB2 = T
+/
+"""
+    f = tmp_path / "params.in"
+    f.write_text(text)
+    p = _abi.GmParams()
+    _abi.check(_abi.load().gm_params_read(p, str(f).encode(), 64), "read")
+    assert (p.nx, p.ny, p.nz) == (20, 18, 40)
+    assert p.Lz == 48.0 and p.Oz == -24.0
+    assert p.get_str("bInit") == "blobs"
+    assert list(p.blobXc[:2]) == [1.0, -1.0] and list(p.blobYc[:2]) == [0.0, 0.0]
+    assert list(p.blobZc[:2]) == [-4.0, 4.0]
+    assert p.blobTwist[1] == -0.7071067811865476
+    assert p.xPeri == 1 and p.yPeri == 1 and p.zPeri == 0 and p.fRestart == 0
+    assert p.dt0 == 3e-4 and p.maxError == 1e-5 and p.nCycle == 2000
+    assert p.nTs == 5 and p.dtSave == 0.2 and p.redB2 == 1
+    assert p.dx == 8.0 / 19
+    p32 = _abi.GmParams()
+    _abi.check(_abi.load().gm_params_read(p32, str(f).encode(), 32), "read32")
+    assert p32.dt0 == float(np.float32(3e-4))
+
+
+def test_namelist_reader_rejects_unknown_names(tmp_path):
+    f = tmp_path / "params.in"
+    f.write_text("&comp nx = 4 /\n&start bogus = 1 /\n&run /\n&io /\n")
+    p = _abi.GmParams()
+    rc = _abi.load().gm_params_read(p, str(f).encode(), 64)
+    assert rc == -9
+    assert b"bogus" in _abi.load().gm_last_error()
+
+
+def test_namelist_reader_missing_group(tmp_path):
+    f = tmp_path / "params.in"
+    f.write_text("&comp nx = 4 /\n&start /\n")
+    p = _abi.GmParams()
+    assert _abi.load().gm_params_read(p, str(f).encode(), 64) == -9
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+def test_init_state_matches_oracle(prec):
+    p = configs.braid6(20, 16, 24, precision=prec)
+    B0, xb = configs.init_state(p)
+    B0o, xbo = Oracle.init_state(p)
+    assert np.array_equal(B0, B0o) and np.array_equal(xb, xbo)
+    # periodic ghost copies of B0 (setPeriHost order z, y, x)
+    assert np.array_equal(B0[:, :, 0], B0[:, :, -2]) and np.array_equal(B0[:, :, -1], B0[:, :, 1])
+    assert np.array_equal(B0[:, 0, :], B0[:, -2, :]) and np.array_equal(B0[:, -1, :], B0[:, 1, :])
+
+
+def test_create_rejects_unsupported_options():
+    lib = _abi.load()
+    p = configs.braid2(8, 8, 8)
+    p.set_str("jMethod", "Classic")
+    h = C.c_void_p()
+    assert lib.gm_create(p, C.byref(h)) == -1
+    p = configs.braid2(8, 8, 8)
+    p.inertia = 1
+    assert lib.gm_create(p, C.byref(h)) == -1
+
+
+def test_configs_blob_mapping():
+    p = configs.braid6()
+    assert p.nBlobs == 6 and (p.nx, p.ny, p.nz) == (128, 128, 256)
+    assert [p.blobZc[b] for b in range(6)] == [-20.0, -12.0, -4.0, 4.0, 12.0, 20.0]
+    assert p.blobXc[0] == 1.0 and p.blobXc[1] == -1.0
+    assert p.blobTwist[0] == float(np.float32(np.sqrt(2) / 2)) and p.blobTwist[1] < 0
+    q = configs.braid2()
+    assert q.precision == 64 and q.nCycle == 2000 and q.maxError == 1e-5

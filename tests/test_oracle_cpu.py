@@ -1,0 +1,164 @@
+"""CPU checks of the oracle: known answers the reference's own diagnostics
+imply (src/init.cu:13-26, 71-106; src/maths.cu:294-377) and the golden
+fixtures produced by the reference's own kernels."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import inner, relerr
+from glemur_gb300 import configs
+from oracle.pyoracle import Oracle
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def small(precision=64, shape=(12, 10, 14)):
+    p = configs.braid2(*shape, precision=precision)
+    p.errMode = 0
+    return configs.derive(p)
+
+
+def test_identity_grid_gives_b0_and_unit_jacobian():
+    p = small()
+    B0, xb = configs.init_state(p)
+    o = Oracle(p, B0, xb)
+    o.refresh()
+    f = o.get()
+    assert np.allclose(inner(f["detJac"]), 1.0, atol=1e-13)
+    assert relerr(inner(f["B"]), inner(B0)) < 1e-13
+
+
+def test_homz_is_a_fixed_point():
+    # B0 = ampl e_z gives J = 0, so k = 0 and the grid stays bit-identical
+    p = small()
+    p.set_str("bInit", "homZ")
+    B0, xb = configs.init_state(p)
+    o = Oracle(p, B0, xb)
+    n = o.run(5)
+    assert n == 5
+    assert np.array_equal(inner(o.get()["xb"]), inner(xb))
+    assert o.scalars()["maxDelta"] == 0.0
+
+
+def test_stokes_current_exact_for_linear_field_on_affine_grid():
+    # On an affine grid x = A X and B linear in x, the circulation around the
+    # planar quads is exact, so J equals the analytic curl.
+    p = small(shape=(8, 8, 8))
+    p.xPeri = p.yPeri = p.zPeri = 0
+    p = configs.derive(p)
+    B0, xb = configs.init_state(p)
+    A = np.array([[1.1, 0.2, 0.0], [0.1, 0.9, 0.15], [0.0, 0.05, 1.2]])
+    X = xb.reshape(-1, 3)
+    x = (X @ A.T).reshape(xb.shape)
+    # B0 chosen so that B = A B0 / det A equals a field with constant curl
+    M = np.array([[0.0, 0.3, -0.2], [-0.1, 0.0, 0.4], [0.25, -0.05, 0.0]])   # B(x) = M x + e_z
+    Bx = (x.reshape(-1, 3) @ M.T + np.array([0, 0, 1.0])).reshape(xb.shape)
+    detA = np.linalg.det(A)
+    B0n = (np.linalg.solve(A, Bx.reshape(-1, 3).T).T * detA).reshape(xb.shape)
+    o = Oracle(p, B0n, x)
+    o.refresh()
+    f = o.get()
+    curl = np.array([M[2, 1] - M[1, 2], M[0, 2] - M[2, 0], M[1, 0] - M[0, 1]])
+    J = f["J"].reshape(-1, 3)
+    # interior points only (the line-tied ghost formula extrapolates)
+    Jin = f["J"][1:-1, 1:-1, 1:-1].reshape(-1, 3)
+    assert np.allclose(Jin, curl[None, :], atol=1e-11), np.abs(Jin - curl).max()
+    assert J.shape[0] == 8 * 8 * 8
+
+
+def test_analytic_field_relaxes_towards_known_state():
+    # bInit = "analytic" has a known relaxed grid (src/maths.cu:332-377)
+    p = configs.defaults(64)
+    p.nx, p.ny, p.nz = 12, 12, 12
+    p.Lx, p.Ly, p.Lz = 8.0, 8.0, 20.0
+    p.Ox, p.Oy, p.Oz = -4.0, -4.0, -10.0
+    p.set_str("bInit", "analytic")
+    p.phi1 = np.pi / 2
+    p.maxError = 1e-5
+    p = configs.derive(p)
+    B0, xb = configs.init_state(p)
+    o = Oracle(p, B0, xb)
+    o.refresh()
+    e0 = o.reduce()
+    o.run(150)
+    o.refresh()
+    e1 = o.reduce()
+    assert e1["errB_1ez"] < 0.5 * e0["errB_1ez"]
+    assert e1["errXb_XbAn"] < e0["errXb_XbAn"]
+    assert e1["residual"] < e0["residual"]
+
+
+def test_energy_decreases_and_cells_stay_valid():
+    p = small()
+    B0, xb = configs.init_state(p)
+    o = Oracle(p, B0, xb)
+    o.refresh()
+    r0 = o.reduce()
+    o.run(40)
+    o.refresh()
+    r1 = o.reduce()
+    assert r1["B2"] < r0["B2"]
+    assert r1["minDetJac"] > 0 and r1["wedgeMin"] > 0
+
+
+def test_fp32_tracks_fp64():
+    # one attempted step from the same state and dt: only rounding differs
+    p64 = small(64)
+    p32 = small(32)
+    B0, xb = configs.init_state(p64)
+    o64 = Oracle(p64, B0, xb)
+    o32 = Oracle(p32, B0.astype(np.float32), xb.astype(np.float32))
+    for n in range(6):
+        o64.stage(n)
+        o32.stage(n)
+    o64.combine()
+    o32.combine()
+    assert relerr(o32.k(0), o64.k(0)) < 1e-5
+    assert relerr(o32.xnew(), o64.xnew()) < 1e-6
+
+
+# ---- pinning against the reference's own kernels ---------------------------
+
+def _golden_cases():
+    import cases
+    return [n for n in cases.NAMES if (GOLDEN / f"{n}.npz").exists()]
+
+
+def _load(name):
+    from glemur_gb300._abi import GmParams
+    z = np.load(GOLDEN / f"{name}.npz")
+    p = GmParams.from_buffer_copy(z["params"].tobytes())
+    return p, z
+
+
+@pytest.mark.parametrize("name", _golden_cases())
+def test_oracle_matches_reference_kernels(name):
+    p, z = _load(name)
+    tol_stage, tol_run = (1e-12, 1e-10) if p.precision == 64 else (2e-6, 1e-4)
+    B0 = z["B0"]
+    _, xb = configs.init_state(p)
+    o = Oracle(p, B0, xb)
+    o.stage(0)
+    assert relerr(o.k(0), z["k0"]) < tol_stage
+    assert relerr(inner(o.get()["xb"]), z["x1"]) < tol_stage
+    o.close()
+    o = Oracle(p, B0, xb)
+    o.step()
+    s = o.scalars()
+    assert abs(s["maxDelta"] - float(z["maxDelta1"])) <= tol_stage * 10 * max(abs(float(z["maxDelta1"])), 1e-300) + 1e-300
+    assert relerr(inner(o.xnew()), z["xnew1"]) < tol_stage
+    f = o.get()
+    assert relerr(inner(f["B"]), z["B1"]) < tol_stage
+    assert relerr(f["J"], z["J1"]) < tol_stage * 100
+    assert relerr(inner(f["detJac"]), z["D1"]) < tol_stage
+    import cases
+    n, lg = o.run(cases.N_ACCEPTED, max_attempts=500, log=True)
+    ref_log = z["log"][1:]
+    assert len(lg) == len(ref_log)
+    assert np.array_equal(lg[:, 2], ref_log[:, 2]), "accept/reject sequence differs"
+    assert relerr(lg[:, 1], ref_log[:, 1]) < tol_run
+    f = o.get()
+    assert relerr(inner(f["xb"]), z["xN"]) < tol_run
+    assert relerr(inner(f["B"]), z["BN"]) < tol_run
+    assert relerr(f["J"], z["JN"]) < tol_run * 100
