@@ -1,0 +1,340 @@
+"""Benchmark of the relaxation hot path (one JSON line on stdout).
+
+Workload: the six-blob braid on 128x128x256 inner points (periodic x, y;
+line-tied z), FP32 storage with the FP64 error norm and controller.  A step
+is one attempted adaptive Runge-Kutta step (6 stages + accept/reject) over
+the whole grid; the metric is cell-RK-stages/s = N x 6 x steps / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's relaxation arithmetic on the host
+cores: the reference is CUDA-only, so its CPU form is the C restatement in
+oracle/ (OpenMP over all cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-RK-stages/s (time to mean|JxB|/(|J||B|)<=1e-2 workload, plain path)"
+UNIT = "cell-RK-stages/s"
+BYTES_PER_CELL_STAGE = {32: 82, 64: 164}   # algorithmic: 20.5 REALs per cell and stage
+SHAPE = (128, 128, 256)
+
+
+def workload_params(precision=32):
+    from glemur_gb300 import configs
+    p = configs.braid6(*SHAPE, precision=precision)
+    return p
+
+
+def workload_config(p, extra=None):
+    c = {
+        "workload": f"braid6 {p.nx}x{p.ny}x{p.nz}: six alternating twisted blobs, periodic x,y, line-tied z",
+        "grid": [p.nx, p.ny, p.nz],
+        "storage": "fp32" if p.precision == 32 else "fp64",
+        "error_norm": "fp64" if p.errMode == 1 else "run precision",
+        "step": "one attempted adaptive Cash-Karp RK step (6 stages + accept/reject)",
+        "l2": "working set ~0.5 GB > 129 MB L2 (inputs larger than L2, no flush)",
+        "parallelism": "replicas" if int(os.environ.get("WORLD_SIZE", "1")) > 1 else "single",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend)
+        return dist, rank, ws
+    return None, rank, ws
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def traffic_per_launch(p):
+    """DRAM bytes per stage launch from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "stage_kernel_traffic.json"
+    if not f.exists():
+        return None, None
+    d = json.loads(f.read_text())
+    key = f"{p.nx}x{p.ny}x{p.nz}_fp{p.precision}"
+    e = d.get(key)
+    if not e:
+        return None, None
+    return float(e["bytes_per_launch"]), e.get("source")
+
+
+def cpu_baseline(p, seconds=20.0):
+    """The oracle (C restatement of the reference arithmetic, all host cores)
+    on a bounded sample of the workload: whole attempted steps on the full grid."""
+    from glemur_gb300 import configs
+    from oracle.pyoracle import Oracle
+    cores = os.cpu_count() or 1
+    B0, xb = configs.init_state(p)
+    o = Oracle(p, B0, xb)
+    o.step()                      # warm-up (first-touch of the arrays)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        o.step()
+        n += 1
+        if time.perf_counter() - t0 > seconds or n >= 50:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    N = p.nx * p.ny * p.nz
+    return {"value": N * 6 * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} attempted steps of the {p.nx}x{p.ny}x{p.nz} workload (OpenMP, {cores} threads)"}
+
+
+def run_reference(args):
+    """--impl reference: the reference arithmetic on the host cores."""
+    dist, rank, ws = dist_init()
+    if rank != 0:
+        return 0
+    from glemur_gb300 import configs
+    from oracle.pyoracle import Oracle
+    p = workload_params()
+    B0, xb = configs.init_state(p)
+    o = Oracle(p, B0, xb)
+    for _ in range(args.warmup):
+        o.step()
+    budget = 150.0
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(args.steps):
+        o.step()
+        n += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    dt = time.perf_counter() - t0
+    N = p.nx * p.ny * p.nz
+    value = N * 6 * n / dt
+    cores = os.cpu_count() or 1
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": n,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / n, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(p, {"impl_note": "reference relaxation arithmetic on host cores (C restatement; "
+                                                  "the reference itself is CUDA-only)"}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{n} attempted steps of the full grid (bounded at {budget:.0f} s)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    from glemur_gb300 import Relaxation, configs
+    dist, rank, ws = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    p = workload_params()
+    N = p.nx * p.ny * p.nz
+    B0, xb = configs.init_state(p)
+    stream = torch.cuda.Stream()
+    g = Relaxation(p)
+    g.set_stream(stream.cuda_stream)
+    g.upload(xb, B0)
+    # warm-up (also captures the step graph)
+    g.steps_async(max(args.warmup, 3))
+    g.state()
+
+    # --- device-timed whole-job throughput: K graph replays --------------------
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    l0 = g.launches
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as ck:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        g.steps_async(args.steps)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        stream.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = g.launches - l0
+    st = g.state()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = N * 6 * args.steps * ws / (ms / 1e3)
+
+    # --- roofline of the stage kernel: per-launch time with events -----------
+    reps = 3
+    stage_ms = []
+    for _ in range(reps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+        for n in range(6):
+            g.stage(n)
+        with torch.cuda.stream(stream):
+            b.record(stream)
+        g.control()
+        stream.synchronize()
+        stage_ms.append(a.elapsed_time(b) / 6)
+    launch_ms = statistics.median(stage_ms)
+    alg_bytes = BYTES_PER_CELL_STAGE[p.precision] * N
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic, traffic_src = traffic_per_launch(p)
+
+    # --- end to end through the C-ABI with host buffers ------------------------
+    xb_h = torch.from_numpy(xb).pin_memory()
+    B0_h = torch.from_numpy(B0).pin_memory()
+    out_h = torch.empty_like(xb_h).pin_memory()
+    g2 = Relaxation(p)
+    g2.set_stream(stream.cuda_stream)
+    g2.upload_ptr(xb_h.data_ptr(), B0_h.data_ptr())
+    g2.steps_async(3)
+    g2.state()
+    barrier()
+    t0 = time.perf_counter()
+    g2.upload_ptr(xb_h.data_ptr(), B0_h.data_ptr())
+    for _ in range(args.steps):
+        g2.steps_async(1)
+        g2.state()                      # the step's result (t, dt, maxDelta, accepted count) to the host
+    import ctypes as C
+    from glemur_gb300 import _abi
+    _abi.check(g2.lib.gm_download(g2.h, C.c_void_p(out_h.data_ptr()), None, None, None), "gm_download")
+    t1 = time.perf_counter()
+    barrier()
+    e2e_s = t1 - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = N * 6 * args.steps * ws / e2e_s
+    h2d = (xb.nbytes + B0.nbytes) / args.steps
+    d2h = (xb.nbytes + 40) / args.steps + 40
+    g2.close()
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline(p, seconds=args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(p, {"attempted": st["nAttempted"], "accepted": st["timeIndex"]}),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "kernel": "k_stage (one RK stage)",
+                         "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
+                         "traffic_source": traffic_src},
+            "cpu_baseline": cb,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": ck.summary(),
+        }
+        print(json.dumps(line))
+    g.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -131,13 +131,15 @@ def build_reference_harness() -> list[Path]:
     if (ref_src / "rungeKutta.cu").exists():
         deps = [wrapper] + sorted(ref_src.glob("*.cu")) + sorted(ref_src.glob("*.h"))
         cmds = []
-        for prec in (64, 32):
-            cub = ref_dir / f"glemur_ref{prec}.cubin"
+        # stock build (nvcc default --fmad=true) and, for FP64, a build without
+        # FMA contraction: two builds of the same reference that round differently
+        for prec, variant, extra in ((64, "", []), (32, "", []), (64, "_nofma", ["--fmad=false"])):
+            cub = ref_dir / f"glemur_ref{prec}{variant}.cubin"
             outs.append(cub)
             if not _newer(cub, deps):
-                cmds.append([NVCC, "-cubin"] + ARCH + ["-O3", f"-DPRECISION={prec}", "-I" + str(ref_src), "-w",
-                                                       str(wrapper), "-o", str(cub)])
-        with cf.ThreadPoolExecutor(max_workers=2) as ex:
+                cmds.append([NVCC, "-cubin"] + ARCH + ["-O3", f"-DPRECISION={prec}", "-I" + str(ref_src), "-w"]
+                            + extra + [str(wrapper), "-o", str(cub)])
+        with cf.ThreadPoolExecutor(max_workers=3) as ex:
             list(ex.map(_run, cmds))
     launcher_src = ORACLE / "ref" / "ref_launcher.cpp"
     so = ref_dir / "libref_launcher.so"

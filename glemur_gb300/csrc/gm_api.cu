@@ -135,6 +135,7 @@ struct Impl : ImplBase {
         kp.N = (long long)nx * ny * nz;
         kp.dx = (T)p->dx; kp.dy = (T)p->dy; kp.dz = (T)p->dz;
         kp.dx1 = (T)p->dx1; kp.dy1 = (T)p->dy1; kp.dz1 = (T)p->dz1;
+        kp.hdx1 = kp.dx1 / 2; kp.hdy1 = kp.dy1 / 2; kp.hdz1 = kp.dz1 / 2;
         kp.Lx = (T)p->Lx; kp.Ly = (T)p->Ly; kp.Lz = (T)p->Lz;
         kp.Ox = (T)p->Ox; kp.Oy = (T)p->Oy; kp.Oz = (T)p->Oz;
         kp.xPeri = p->xPeri != 0; kp.yPeri = p->yPeri != 0; kp.zPeri = p->zPeri != 0;
@@ -203,14 +204,30 @@ struct Impl : ImplBase {
         kp.ex = eps;
         kp.ey = eps + nx;
         kp.ez = eps + nx + ny;
-        // launch shape: 32 x TY column tiles, TZ planes per CTA; enough CTAs
-        // for two waves over the 152 SMs where the grid allows it
+        // launch shape: 32 x TY column tiles of TZ planes.  Pick (TY, TZ) to
+        // minimise the work of the busiest SM, ceil(tiles / SMs) x per-tile
+        // work (TZ + 3) x (TY + 2) (the +3 / +2 are the halo planes and rows
+        // a tile recomputes), so tiles split evenly over the 152 SMs.
         const int nbx = (nx + gmk::TX - 1) / gmk::TX;
-        auto nctas = [&](int ty, int tz) { return (long long)nbx * ((ny + ty - 1) / ty) * ((nz + tz - 1) / tz); };
-        TY = 8;
-        TZ = 32;
-        while (TZ > 4 && nctas(TY, TZ) < 2 * 152) TZ /= 2;
-        while (TY > 2 && nctas(TY, TZ) < 2 * 152) TY /= 2;
+        int dev = 0, nsm = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        double best = 1e300;
+        for (int ty : {8, 4, 2}) {
+            if (ty > 2 && ny < ty) continue;
+            const size_t sm = gmk::stage_smem_bytes<T>(ty, gmk::MODE_STAGE, p->pressure);
+            const long long slots = (long long)nsm * gmk::stage_occupancy<T>(ty, p->pressure, sm);
+            const long long ncol = (long long)nbx * ((ny + ty - 1) / ty);
+            for (int nzc = 1; nzc <= nz; nzc++) {
+                const int tz = (nz + nzc - 1) / nzc;
+                if (tz < 4 && nz >= 4) break;
+                const long long tiles = ncol * ((nz + tz - 1) / tz);
+                const long long per_sm = (tiles + nsm - 1) / nsm;
+                if (tiles < slots / 4 && ty > 2) continue;   // too few CTAs to fill the GPU
+                const double cost = (double)per_sm * (tz + 3) * (ty + 2);
+                if (cost < best * 0.999) { best = cost; TY = ty; TZ = tz; }
+            }
+        }
         grid = dim3((unsigned)nbx, (unsigned)((ny + TY - 1) / TY), (unsigned)((nz + TZ - 1) / TZ));
         block = dim3(gmk::TX, (unsigned)TY, 1);
         smem_stage = gmk::stage_smem_bytes<T>(TY, gmk::MODE_STAGE, p->pressure);

@@ -55,6 +55,7 @@ struct KP {
     long long cs;            // component stride of padded arrays
     long long N;             // nx*ny*nz
     T dx, dy, dz, dx1, dy1, dz1;
+    T hdx1, hdy1, hdz1;      // dx1/2, dy1/2, dz1/2 (exact)
     T Lx, Ly, Lz, Ox, Oy, Oz;
     int xPeri, yPeri, zPeri, zUpdate, errMode, refDt;
     T beta, p0Amp, p0W2;     // pressure: p0(X) = beta (1 + p0Amp exp(-(X^2+Y^2)/p0W2))
@@ -105,6 +106,8 @@ template <typename T>
 size_t stage_smem_bytes(int TY, int mode, int pressure);
 template <typename T>
 cudaError_t prepare_kernels();
+template <typename T>
+int stage_occupancy(int TY, int pressure, size_t smem);
 template <typename T>
 cudaError_t launch_control(const KP<T>& p, DevState* st, double* log, cudaStream_t s);
 template <typename T>

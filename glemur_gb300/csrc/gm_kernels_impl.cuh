@@ -40,6 +40,10 @@ __device__ __forceinline__ T det_guarded(const T j[3][3]) {
     return d;
 }
 
+// Correctly rounded reciprocal (the value of 1/x with IEEE division).
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+
 template <typename T>
 __device__ __forceinline__ void cross3(const T a[3], const T b[3], T c[3]) {
     c[0] = a[1] * b[2] - a[2] * b[1];
@@ -69,17 +73,18 @@ __device__ __forceinline__ void b_interior(const KP<T>& p, const Tile<T, NB>& t,
     T jac[3][3];
 #pragma unroll
     for (int l = 0; l < 3; l++) {
-        jac[l][0] = (t.x(k, l, j, i + 1) - t.x(k, l, j, i - 1)) * p.dx1 / 2;
-        jac[l][1] = (t.x(k, l, j + 1, i) - t.x(k, l, j - 1, i)) * p.dy1 / 2;
-        jac[l][2] = (t.x(k + 1, l, j, i) - t.x(k - 1, l, j, i)) * p.dz1 / 2;
+        // (a - b) * d1 / 2 == (a - b) * (d1 / 2) exactly (scaling by 2)
+        jac[l][0] = (t.x(k, l, j, i + 1) - t.x(k, l, j, i - 1)) * p.hdx1;
+        jac[l][1] = (t.x(k, l, j + 1, i) - t.x(k, l, j - 1, i)) * p.hdy1;
+        jac[l][2] = (t.x(k + 1, l, j, i) - t.x(k - 1, l, j, i)) * p.hdz1;
     }
     T det = det_guarded(jac);
-    T detJac1 = (T)1 / det;
+    T detJac1 = rcp_rn(det);
     long long g = gidx(p.px, p.py, i, j, k);
     T b0 = __ldg(&B0[g]), b1 = __ldg(&B0[p.cs + g]), b2 = __ldg(&B0[2 * p.cs + g]);
 #pragma unroll
     for (int l = 0; l < 3; l++) Bv[l] = (jac[l][0] * b0 + jac[l][1] * b1 + jac[l][2] * b2) * detJac1;
-    *D = (T)1 / detJac1;
+    *D = rcp_rn(detJac1);
 }
 
 // B and Delta on the ghost plane of a non-periodic face with normal axis a:
@@ -140,18 +145,22 @@ __device__ __forceinline__ void b_face(const KP<T>& p, const Tile<T, NB>& t, con
         jac[l][v] = (Rv[l] - Lv[l]) * d13[v] / 2;
         jac[l][a] = (side ? (Xo[l] - Xin[l]) : (Xin[l] - Xo[l])) * d13[a] / 2;
     }
-    T detJac1 = (T)1 / det_guarded(jac);
+    T detJac1 = rcp_rn(det_guarded(jac));
     long long g = gidx(p.px, p.py, i, j, k);
     T b0[3] = {__ldg(&B0[g]), __ldg(&B0[p.cs + g]), __ldg(&B0[2 * p.cs + g])};
 #pragma unroll
     for (int l = 0; l < 3; l++) Bv[l] = (jac[l][0] * b0[0] + jac[l][1] * b0[1] + jac[l][2] * b0[2]) * detJac1;
     Bv[a] = b0[a];
-    *D = (T)1 / detJac1;
+    *D = rcp_rn(detJac1);
 }
 
 // Mimetic current: circulation of B around the three quadrilaterals through
 // the face neighbours, area-weighted normals and a 3x3 solve; JStokes,
 // src/current.cu:290-406.  Neighbour order: -x, +x, -y, +y, -z, +z.
+// The circulations are accumulated without the 1/2 of the edge averages (so
+// they come out doubled) and the normals without their 1/4 (so the inverse
+// normal matrix comes out quartered); J = 2 * (quartered inverse) . (doubled
+// circulations).  Power-of-two scalings leave every rounding unchanged.
 template <typename T>
 __device__ __forceinline__ void stokes(const T xn[6][3], const T bn[6][3], T J[3]) {
     constexpr int Q[3][4] = {{0, 2, 1, 3}, {2, 4, 3, 5}, {4, 0, 5, 1}};
@@ -164,17 +173,17 @@ __device__ __forceinline__ void stokes(const T xn[6][3], const T bn[6][3], T J[3
         for (int l = 0; l < 3; l++) {
 #pragma unroll
             for (int c = 0; c < 4; c++) dxv[c][l] = xn[Q[qd][(c + 1) & 3]][l] - xn[Q[qd][c]][l];
-            I += (bn[Q[qd][1]][l] + bn[Q[qd][0]][l]) / 2 * dxv[0][l] + (bn[Q[qd][2]][l] + bn[Q[qd][1]][l]) / 2 * dxv[1][l] +
-                 (bn[Q[qd][3]][l] + bn[Q[qd][2]][l]) / 2 * dxv[2][l] + (bn[Q[qd][0]][l] + bn[Q[qd][3]][l]) / 2 * dxv[3][l];
+            I += (bn[Q[qd][1]][l] + bn[Q[qd][0]][l]) * dxv[0][l] + (bn[Q[qd][2]][l] + bn[Q[qd][1]][l]) * dxv[1][l] +
+                 (bn[Q[qd][3]][l] + bn[Q[qd][2]][l]) * dxv[2][l] + (bn[Q[qd][0]][l] + bn[Q[qd][3]][l]) * dxv[3][l];
         }
         T cr[4][3];
 #pragma unroll
         for (int c = 0; c < 4; c++) cross3(dxv[c], dxv[(c + 1) & 3], cr[c]);
         II[qd] = I;
 #pragma unroll
-        for (int l = 0; l < 3; l++) NA[qd][l] = (cr[0][l] + cr[1][l] + cr[2][l] + cr[3][l]) / 4;
+        for (int l = 0; l < 3; l++) NA[qd][l] = cr[0][l] + cr[1][l] + cr[2][l] + cr[3][l];
     }
-    T detN1 = (T)1 / det3(NA);
+    T detN1 = rcp_rn(det3(NA));
     T NA1[3][3];
     NA1[0][0] = (NA[1][1] * NA[2][2] - NA[1][2] * NA[2][1]) * detN1;
     NA1[0][1] = (NA[0][2] * NA[2][1] - NA[0][1] * NA[2][2]) * detN1;
@@ -186,7 +195,7 @@ __device__ __forceinline__ void stokes(const T xn[6][3], const T bn[6][3], T J[3
     NA1[2][1] = (NA[0][1] * NA[2][0] - NA[0][0] * NA[2][1]) * detN1;
     NA1[2][2] = (NA[0][0] * NA[1][1] - NA[0][1] * NA[1][0]) * detN1;
 #pragma unroll
-    for (int l = 0; l < 3; l++) J[l] = NA1[l][0] * II[0] + NA1[l][1] * II[1] + NA1[l][2] * II[2];
+    for (int l = 0; l < 3; l++) J[l] = (NA1[l][0] * II[0] + NA1[l][1] * II[1] + NA1[l][2] * II[2]) * (T)2;
 }
 
 // Pressure gradient grad(p) for p = p0(X)/Delta: gradPClassic,
@@ -749,6 +758,16 @@ static cudaError_t launch_one(const StageArgs<T>& a, dim3 grid, dim3 block, size
     return cudaGetLastError();
 }
 
+// Resident CTAs per SM of the stage kernel for a tile height and smem size.
+template <typename T>
+int stage_occupancy(int TY, int pressure, size_t smem) {
+    int nb = 0;
+    cudaError_t e = pressure
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage<T, true, MODE_STAGE, false>, TX * TY, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage<T, false, MODE_STAGE, false>, TX * TY, smem);
+    return e == cudaSuccess && nb > 0 ? nb : 1;
+}
+
 // Opt every stage-kernel variant in to large dynamic shared memory (once per
 // device, before any launch or stream capture).
 template <typename T>
@@ -831,6 +850,7 @@ cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t 
     template cudaError_t launch_stage<T>(const StageArgs<T>&, int, int, dim3, dim3, size_t, cudaStream_t);       \
     template size_t stage_smem_bytes<T>(int, int, int);                                                           \
     template cudaError_t prepare_kernels<T>();                                                                    \
+    template int stage_occupancy<T>(int, int, size_t);                                                            \
     template cudaError_t launch_control<T>(const KP<T>&, DevState*, double*, cudaStream_t);                       \
     template cudaError_t launch_finalize<T>(const double*, int, double*, cudaStream_t);                           \
     template cudaError_t launch_unpack<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \

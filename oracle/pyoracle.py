@@ -150,9 +150,9 @@ class RefLauncher:
     """The reference's own CUDA kernels (cubin built from the reference
     sources) driven with the launch sequence of src/main.cu.  GPU only."""
 
-    def __init__(self, params, B0, xb, t=0.0, dt=None):
+    def __init__(self, params, B0, xb, t=0.0, dt=None, variant=""):
         so = REF / "libref_launcher.so"
-        cub = REF / f"glemur_ref{params.precision}.cubin"
+        cub = REF / f"glemur_ref{params.precision}{variant}.cubin"
         if not so.exists() or not cub.exists():
             raise RuntimeError(f"reference harness missing ({so}, {cub})")
         lib = C.CDLL(str(so))

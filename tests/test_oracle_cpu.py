@@ -132,10 +132,19 @@ def _load(name):
     return p, z
 
 
+# Run-level tolerances.  With dt0 = 3e-4 the error norm of the first steps is
+# rounding noise (|x_new - x*| ~ 1e-15 against a true value ~ 1e-18), so the
+# first dt updates differ at ~1e-7 between any two builds that round
+# differently (FMA or not); after 10 accepted steps that leaves x within
+# ~1e-11, B ~ 1e-10, J ~ 1e-9 (measured by perturbing dt0 by 1e-7).
+RUN_TOL = {64: dict(dt=1e-6, x=1e-10, B=1e-9, J=1e-8), 32: dict(dt=1e-2, x=1e-4, B=1e-3, J=1e-2)}
+
+
 @pytest.mark.parametrize("name", _golden_cases())
 def test_oracle_matches_reference_kernels(name):
     p, z = _load(name)
-    tol_stage, tol_run = (1e-12, 1e-10) if p.precision == 64 else (2e-6, 1e-4)
+    tol_stage = 1e-12 if p.precision == 64 else 2e-6
+    rt = RUN_TOL[p.precision]
     B0 = z["B0"]
     _, xb = configs.init_state(p)
     o = Oracle(p, B0, xb)
@@ -157,8 +166,8 @@ def test_oracle_matches_reference_kernels(name):
     ref_log = z["log"][1:]
     assert len(lg) == len(ref_log)
     assert np.array_equal(lg[:, 2], ref_log[:, 2]), "accept/reject sequence differs"
-    assert relerr(lg[:, 1], ref_log[:, 1]) < tol_run
+    assert relerr(lg[:, 1], ref_log[:, 1]) < rt["dt"]
     f = o.get()
-    assert relerr(inner(f["xb"]), z["xN"]) < tol_run
-    assert relerr(inner(f["B"]), z["BN"]) < tol_run
-    assert relerr(f["J"], z["JN"]) < tol_run * 100
+    assert relerr(inner(f["xb"]), z["xN"]) < rt["x"]
+    assert relerr(inner(f["B"]), z["BN"]) < rt["B"]
+    assert relerr(f["J"], z["JN"]) < rt["J"]
