@@ -6,6 +6,8 @@
 // launch), so a run is graph replays with no host round trip per step; the
 // reference instead synchronises after every launch and copies maxDelta to the
 // host each step (src/main.cu:259-384, src/maths.cu:101-130).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -32,6 +34,21 @@ namespace {
         if (e_ != cudaSuccess)                                                             \
             return gm::fail(GM_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_));    \
     } while (0)
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    }
+    return fn;
+}
 
 int check_params(const gm_params* p) {
     if (!p) return gm::fail(GM_EPARAM, "null params");
@@ -79,6 +96,7 @@ struct Impl : ImplBase {
     T* XS[2] = {nullptr, nullptr};
     T* K[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     T* B0 = nullptr;
+    T* B0s = nullptr;           // B0 scaled for the algebraic B formula
     T* outB = nullptr;
     T* outJ = nullptr;
     T* outD = nullptr;
@@ -98,12 +116,17 @@ struct Impl : ImplBase {
     int nparts = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    // TMA-fed stage kernel: tensor maps of X[0], X[1], XS[0], XS[1]
+    bool use_tma = true;
+    CUtensorMap tmaps[4];
+    dim3 grid2;
+    int TZ2 = 32;
     size_t NG = 0, N = 0, NP = 0;
 
     ~Impl() override {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
-        void* ptrs[] = {X[0], X[1], XS[0], XS[1], K[0], K[1], K[2], K[3], K[4], B0, outB, outJ,
+        void* ptrs[] = {X[0], X[1], XS[0], XS[1], K[0], K[1], K[2], K[3], K[4], B0, B0s, outB, outJ,
                         outD, stage_buf, eps, st, log, part, red};
         for (void* q : ptrs)
             if (q) cudaFree(q);
@@ -166,7 +189,9 @@ struct Impl : ImplBase {
             kp.c[m] = (T)cd[m];
             kp.cst[m] = (T)csd[m];
             kp.cmc[m] = (double)(T)cd[m] - (double)(T)csd[m];
+            kp.cmcT[m] = (T)kp.cmc[m];
         }
+        kp.inv8dxdydz = (T)(1.0 / (8.0 * (double)(T)p->dx * (double)(T)p->dy * (double)(T)p->dz));
         NG = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
         N = (size_t)kp.N;
         NP = (size_t)kp.cs * 3;
@@ -178,6 +203,7 @@ struct Impl : ImplBase {
         for (int m = 0; m < 5; m++)
             if ((rc = alloc((void**)&K[m], 3 * N * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&B0, NP * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&B0s, NP * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outB, 3 * NG * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outJ, 3 * N * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outD, NG * sizeof(T)))) return rc;
@@ -233,9 +259,51 @@ struct Impl : ImplBase {
         smem_stage = gmk::stage_smem_bytes<T>(TY, gmk::MODE_STAGE, p->pressure);
         smem_diag = gmk::stage_smem_bytes<T>(TY, gmk::MODE_DIAG, p->pressure);
         nparts = (int)(grid.x * grid.y * grid.z);
+        if (use_tma) {
+            if ((rc = init_tma(nsm))) return rc;
+        }
         if ((rc = alloc((void**)&part, (size_t)nparts * gmk::R_COUNT * sizeof(double)))) return rc;
         if ((rc = alloc((void**)&red, gmk::R_COUNT * sizeof(double)))) return rc;
         CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    // Tensor maps over the padded positions viewed as (px, py, pz, component),
+    // box 36 x 12 x 1 x 3 = one position plane of a 32 x 8 tile with its
+    // 2-point halo.  Box x starts are tile starts (multiples of 32 elements),
+    // so every copy starts on a 16-byte boundary.
+    int init_tma(int nsm) {
+        CUDA_TRY(gmk::prepare_stage_tma<T>());
+        auto enc = tensor_map_encoder();
+        if (!enc) return gm::fail(GM_ECUDA, "cuTensorMapEncodeTiled is unavailable");
+        const cuuint64_t es = sizeof(T);
+        cuuint64_t dims[4] = {(cuuint64_t)kp.px, (cuuint64_t)kp.py, (cuuint64_t)kp.pz, 3};
+        cuuint64_t strides[3] = {(cuuint64_t)kp.px * es, (cuuint64_t)kp.px * kp.py * es, (cuuint64_t)kp.cs * es};
+        cuuint32_t box[4] = {gmk::TX + 4, gmk::STAGE_TMA_TY + 4, 1, 3};
+        cuuint32_t estr[4] = {1, 1, 1, 1};
+        T* bufs[4] = {X[0], X[1], XS[0], XS[1]};
+        for (int q = 0; q < 4; q++) {
+            CUresult r = enc(&tmaps[q], sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4,
+                             (void*)bufs[q], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return gm::fail(GM_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        }
+        // z chunking as for k_stage, with the tile height fixed at 8
+        const int nx = kp.nx, ny = kp.ny, nz = kp.nz;
+        const int ty = gmk::STAGE_TMA_TY;
+        const long long ncol = (long long)((nx + gmk::TX - 1) / gmk::TX) * ((ny + ty - 1) / ty);
+        double best = 1e300;
+        for (int nzc = 1; nzc <= nz; nzc++) {
+            const int tz = (nz + nzc - 1) / nzc;
+            if (tz < 4 && nz >= 4) break;
+            const long long tiles = ncol * ((nz + tz - 1) / tz);
+            const long long per_sm = (tiles + nsm - 1) / nsm;
+            const double cost = (double)per_sm * (tz + 3);
+            if (cost < best * 0.999) { best = cost; TZ2 = tz; }
+        }
+        grid2 = dim3((unsigned)((nx + gmk::TX - 1) / gmk::TX), (unsigned)((ny + ty - 1) / ty),
+                     (unsigned)((nz + TZ2 - 1) / TZ2));
         return GM_OK;
     }
 
@@ -247,6 +315,7 @@ struct Impl : ImplBase {
         a.XS[0] = XS[0]; a.XS[1] = XS[1];
         for (int m = 0; m < 5; m++) a.K[m] = K[m];
         a.B0 = B0;
+        a.B0s = B0s;
         a.st = st;
         a.log = log;
         a.n = n;
@@ -261,6 +330,7 @@ struct Impl : ImplBase {
         const size_t bytes = 3 * NG * sizeof(T);
         CUDA_TRY(cudaMemcpyAsync(stage_buf, b0, bytes, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(gmk::launch_unpack<T>(kp, stage_buf, B0, stream));
+        CUDA_TRY(gmk::launch_scale_b0<T>(kp, B0, B0s, stream));
         CUDA_TRY(cudaMemcpyAsync(outB, stage_buf, bytes, cudaMemcpyDeviceToDevice, stream));   // main.cu:195
         CUDA_TRY(cudaMemcpyAsync(stage_buf, xb, bytes, cudaMemcpyHostToDevice, stream));
         T* bufs[4] = {X[0], X[1], XS[0], XS[1]};
@@ -276,6 +346,7 @@ struct Impl : ImplBase {
         s.target = INT_MAX;
         s.logCap = logCap;
         s.done = !(s.dt > kp.dtMin);
+        if (s.done) s.status |= GM_ST_DTMIN | GM_ST_DONE;
         *h_st = s;
         CUDA_TRY(cudaMemcpyAsync(st, h_st, sizeof s, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
@@ -286,8 +357,16 @@ struct Impl : ImplBase {
     int stage(int n) override {
         if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_stage before gm_upload");
         if (n < 0 || n > 5) return gm::fail(GM_EPARAM, "stage index must be 0..5");
-        StageArgs<T> a = args(n);
-        CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_STAGE, gp.pressure, grid, block, smem_stage, stream));
+        if (use_tma) {
+            gmk::StageArgsTMA<T> A;
+            memcpy(A.tm, tmaps, sizeof tmaps);
+            A.a = args(n);
+            A.a.TZ = TZ2;
+            CUDA_TRY(gmk::launch_stage_tma<T>(A, gp.pressure, grid2, stream));
+        } else {
+            StageArgs<T> a = args(n);
+            CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_STAGE, gp.pressure, grid, block, smem_stage, stream));
+        }
         launches++;
         return GM_OK;
     }
@@ -363,8 +442,11 @@ struct Impl : ImplBase {
         if (rc) return rc;
         h_st->target = target;
         if (reset_done) {
-            h_st->done = !(h_st->dt > kp.dtMin) || (h_st->status & GM_ST_NAN) || h_st->timeIndex >= target;
-            if (!h_st->done) h_st->status &= ~(unsigned)GM_ST_DONE;
+            const bool dtmin = !(h_st->dt > kp.dtMin);
+            h_st->done = dtmin || (h_st->status & (GM_ST_NAN | GM_ST_TIMEOUT | GM_ST_ALIGN)) || h_st->timeIndex >= target;
+            if (dtmin) h_st->status |= GM_ST_DTMIN;
+            if (h_st->done) h_st->status |= GM_ST_DONE;
+            else h_st->status &= ~(unsigned)GM_ST_DONE;
         }
         CUDA_TRY(cudaMemcpyAsync(st, h_st, sizeof(DevState), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
@@ -398,6 +480,9 @@ struct Impl : ImplBase {
         }
         if (out) fill(out);
         if (h_st->status & GM_ST_NAN) return gm::fail(GM_ENAN, "NaN/Inf in a stage increment");
+        if (h_st->status & (GM_ST_TIMEOUT | GM_ST_ALIGN))
+            return gm::fail(GM_ETIMEOUT, "a stage kernel stopped: bounded wait or alignment check (status " +
+                                             std::to_string(h_st->status) + ")");
         return GM_OK;
     }
 

@@ -24,6 +24,7 @@
 //   k_m:       inner points only, index i + nx*(j + ny*k), component stride N.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -63,6 +64,8 @@ struct KP {
     T db[6][6];              // b[n+1][m] - b[n][m] of the Cash-Karp tableau
     T c[6], cst[6];          // 5th- and 4th-order weights
     double cmc[6];           // c - c* in double (error norm of errMode 1)
+    T cmcT[6];               // c - c* in the run precision
+    T inv8dxdydz;            // 1 / (8 dx dy dz): det(a, b, c) -> Delta
     double ar, az, phi1;     // analytic-field parameters (distance-to-analytic diagnostic)
     int wantXbAn;
     const T* ex;             // epsilon profile factors per axis (rungeKutta.cu:180-185)
@@ -87,6 +90,7 @@ struct StageArgs {
     T* XS[2];                // stage positions, ping-pong
     T* K[5];                 // k_0..k_4
     const T* B0;
+    const T* B0s;            // B0 scaled by (4 dy dz, 4 dx dz, 4 dx dy), padded layout
     DevState* st;
     double* log;             // per attempt: maxDelta, dt after the update, accepted
     int n;                   // stage index 0..5
@@ -120,8 +124,28 @@ cudaError_t launch_pack(const KP<T>& p, const T* soa, T* aos, cudaStream_t s);
 template <typename T>
 cudaError_t launch_images(const KP<T>& p, T* soa, cudaStream_t s);
 template <typename T>
+cudaError_t launch_scale_b0(const KP<T>& p, const T* B0, T* B0s, cudaStream_t s);
+template <typename T>
 cudaError_t launch_pack_k(const KP<T>& p, const T* k, T* aos, cudaStream_t s);
 template <typename T>
 cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t s);
+
+// TMA-fed stage kernel (gm_stage_tma.cuh): 32 x 8 tiles, position planes
+// streamed by cp.async.bulk.tensor.  tm[] are the tensor maps of X[0], X[1],
+// XS[0], XS[1] (box 36 x 12 x 1 x 3 over (px, py, pz, component)).
+template <typename T>
+struct StageArgsTMA {
+    CUtensorMap tm[4];
+    StageArgs<T> a;
+};
+template <typename T>
+size_t stage_tma_smem_bytes(int pressure);
+template <typename T>
+cudaError_t prepare_stage_tma();
+template <typename T>
+int stage_tma_occupancy(int pressure);
+template <typename T>
+cudaError_t launch_stage_tma(const StageArgsTMA<T>& A, int pressure, dim3 grid, cudaStream_t s);
+constexpr int STAGE_TMA_TY = 8;
 
 }  // namespace gmk

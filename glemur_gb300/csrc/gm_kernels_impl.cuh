@@ -51,14 +51,17 @@ __device__ __forceinline__ void cross3(const T a[3], const T b[3], T c[3]) {
     c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-// Shared-memory tile views.
-template <typename T, int NB>
+// Shared-memory tile views: a ring of XR position planes (plane k in slot
+// (k + OFF) % XR) and a ring of B planes.
+template <typename T, int NB, int XR = XRING, int OFF = 10>
 struct Tile {
     T* xs;
     T* bs;
     int i0, j0, HX, HY, BX, BY;
+    int slot = 0;     // elements between position-plane slots (0: 3 * HY * HX)
     __device__ __forceinline__ T& x(int k, int c, int j, int i) const {
-        return xs[((((k + 10) % XRING) * 3 + c) * HY + (j - j0 + 2)) * HX + (i - i0 + 2)];
+        const int ss = slot ? slot : 3 * HY * HX;
+        return xs[((k + OFF) % XR) * ss + (c * HY + (j - j0 + 2)) * HX + (i - i0 + 2)];
     }
     __device__ __forceinline__ T& b(int k, int c, int j, int i) const {
         return bs[((((k + 10) % BRING) * NB + c) * BY + (j - j0 + 1)) * BX + (i - i0 + 1)];
@@ -92,8 +95,8 @@ __device__ __forceinline__ void b_interior(const KP<T>& p, const Tile<T, NB>& t,
 // plane shifted by the grid spacing; in-plane neighbours at the edges of the
 // reference's 16x16 launch blocks are the own position shifted by the
 // spacing (boundaries.cu:72-109, 212-237, 340-365); B.n = B0.n.
-template <typename T, int NB>
-__device__ __forceinline__ void b_face(const KP<T>& p, const Tile<T, NB>& t, const T* __restrict__ B0, int a, int i,
+template <typename T, class TileT>
+__device__ __forceinline__ void b_face(const KP<T>& p, const TileT& t, const T* __restrict__ B0, int a, int i,
                                        int j, int k, T Bv[3], T* D) {
     const int u = (a == 0) ? 1 : 0;
     const int v = (a == 2) ? 1 : 2;
@@ -201,8 +204,8 @@ __device__ __forceinline__ void stokes(const T xn[6][3], const T bn[6][3], T J[3
 // Pressure gradient grad(p) for p = p0(X)/Delta: gradPClassic,
 // src/gradP.cu:91-155 (uniform p0 = beta), plus (1/Delta) J^-T grad_X p0 for
 // a non-uniform p0(X) (no counterpart in the reference).
-template <typename T, int NB>
-__device__ __forceinline__ void grad_p(const KP<T>& p, const Tile<T, NB>& t, int i, int j, int k, T D, T g[3]) {
+template <typename T, class TileT>
+__device__ __forceinline__ void grad_p(const KP<T>& p, const TileT& t, int i, int j, int k, T D, T g[3]) {
     T jac[3][3], jac1[3][3];
     const T det1 = (T)1 / D;
 #define XV(di, dj, dk, l) t.x(k + (dk), l, j + (dj), i + (di))
@@ -356,7 +359,7 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                 } else if (yo && !p.yPeri) {
                     face = 1;
                 }
-                if (face >= 0) b_face<T, NB>(p, t, a.B0, face, i, j, kb, Bv, &D);
+                if (face >= 0) b_face<T>(p, t, a.B0, face, i, j, kb, Bv, &D);
                 else b_interior<T, NB>(p, t, a.B0, i, j, kb, Bv, &D);
                 bdst[(0 * BY + jj) * BX + ii] = Bv[0];
                 bdst[(1 * BY + jj) * BX + ii] = Bv[1];
@@ -405,7 +408,7 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                     for (int l = 0; l < 3; l++) kn[l] *= f;
                     if (PRESS) {
                         T g[3];
-                        grad_p<T, NB>(p, t, i, j, kc, t.b(kc, 3, j, i), g);
+                        grad_p<T>(p, t, i, j, kc, t.b(kc, 3, j, i), g);
 #pragma unroll
                         for (int l = 0; l < 3; l++) kn[l] += -dtT * g[l];
                     }
@@ -612,7 +615,7 @@ __global__ void k_control(const __grid_constant__ KP<T> p, DevState* st, double*
         log[3 * att + 1] = st->dt;
         log[3 * att + 2] = acc ? 1.0 : 0.0;
     }
-    if (st->status & GM_ST_NAN) st->done = 1;
+    if (st->status & (GM_ST_NAN | GM_ST_TIMEOUT | GM_ST_ALIGN)) st->done = 1;
     if (!(st->dt > p.dtMin)) {
         st->status |= GM_ST_DTMIN;
         st->done = 1;
@@ -692,6 +695,17 @@ __global__ void k_images(const KP<T> p, T* __restrict__ soa) {
         soa[gd] = v0;
         soa[p.cs + gd] = v1;
         soa[2 * p.cs + gd] = v2;
+    }
+}
+
+// B0 scaled for the algebraic B formula: (4 dy dz B0x, 4 dx dz B0y, 4 dx dy B0z)
+template <typename T>
+__global__ void k_scale_b0(const KP<T> p, const T* __restrict__ B0, T* __restrict__ B0s) {
+    const T w0 = 4 * p.dy * p.dz, w1 = 4 * p.dx * p.dz, w2 = 4 * p.dx * p.dy;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < p.cs; q += (long long)gridDim.x * blockDim.x) {
+        B0s[q] = B0[q] * w0;
+        B0s[p.cs + q] = B0[p.cs + q] * w1;
+        B0s[2 * p.cs + q] = B0[2 * p.cs + q] * w2;
     }
 }
 
@@ -820,6 +834,12 @@ cudaError_t launch_unpack(const KP<T>& p, const T* aos, T* soa, cudaStream_t s) 
 }
 
 template <typename T>
+cudaError_t launch_scale_b0(const KP<T>& p, const T* B0, T* B0s, cudaStream_t s) {
+    k_scale_b0<T><<<nblk(p.cs), 256, 0, s>>>(p, B0, B0s);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_images(const KP<T>& p, T* soa, cudaStream_t s) {
     k_images<T><<<nblk((long long)(p.nx + 4) * (p.ny + 4) * (p.nz + 4)), 256, 0, s>>>(p, soa);
     return cudaGetLastError();
@@ -856,6 +876,7 @@ cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t 
     template cudaError_t launch_unpack<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \
     template cudaError_t launch_pack<T>(const KP<T>&, const T*, T*, cudaStream_t);                                \
     template cudaError_t launch_images<T>(const KP<T>&, T*, cudaStream_t);                                        \
+    template cudaError_t launch_scale_b0<T>(const KP<T>&, const T*, T*, cudaStream_t);                            \
     template cudaError_t launch_pack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \
     template cudaError_t launch_export_ghosts<T>(const KP<T>&, T*, T*, cudaStream_t);
 

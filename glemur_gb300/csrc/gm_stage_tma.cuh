@@ -1,0 +1,571 @@
+// gm_stage_tma.cuh -- the RK stage kernel with TMA-fed plane rings.
+//
+// Same arithmetic as k_stage (gm_kernels_impl.cuh); different data movement:
+//   * tiles are 32 x 8 columns (compile time), one warp per tile row;
+//   * one thread streams each grid plane (tile + 2-point halo, all three
+//     components as one 4-D box) from the padded position array into a ring of
+//     XR2 shared-memory slots with cp.async.bulk.tensor, completion tracked by
+//     one mbarrier per slot;
+//   * J for plane k is formed one iteration after B of plane k+1, so an
+//     iteration needs a single __syncthreads;
+//   * every shared-memory neighbour access is a constant offset from a
+//     per-plane base.
+// Waits on the mbarriers are bounded: after kWaitLimit polls the CTA records
+// GM_ST_TIMEOUT, drains the copies it has in flight (again bounded) and
+// returns.
+#pragma once
+
+#include <cuda.h>
+
+#include "gm_kernels_impl.cuh"
+
+namespace gmk {
+
+constexpr int TY2 = 8;                   // tile rows (= warps per CTA)
+constexpr int HX2 = TX + 4, HY2 = TY2 + 4;
+constexpr int BX2 = TX + 2, BY2 = TY2 + 2;
+constexpr int XR2 = 6;                   // position-plane ring
+constexpr int BR2 = 4;                   // B-plane ring
+constexpr int PLANE_C = HY2 * HX2;       // elements of one component of a position plane
+constexpr int PLANE_X = 3 * PLANE_C;
+constexpr unsigned kWaitLimit = 1u << 22;
+
+// Stride of a position-plane slot in elements: the plane rounded up so every
+// slot (a TMA destination) starts on a 128-byte boundary.
+template <typename T>
+constexpr int slot_elems() {
+    return (int)(((PLANE_X * sizeof(T) + 127) / 128) * 128 / sizeof(T));
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait; returns false when the limit ran out
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (unsigned it = 0; it < kWaitLimit; it++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+
+// Reciprocal for the stage kernel: FP32 uses the hardware approximation plus
+// one Newton step (within ~1 ulp; FP32 parity is judged at 1e-5), FP64 the
+// correctly rounded one.
+__device__ __forceinline__ float rcp_stage(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return fmaf(fmaf(-x, r, 1.0f), r, r);
+}
+__device__ __forceinline__ double rcp_stage(double x) { return __drcp_rn(x); }
+
+// det(a, b, c) of the columns of A.  In FP32 the determinant of a strongly
+// sheared cell (|det| small against the bound |a|_1 |b|_1 |c|_1 of the six
+// Sarrus products) is recomputed in double from the same entries.
+template <typename T>
+__device__ __forceinline__ T det_cols(const T A[3][3]) {
+    T d = det3(A);
+    if (sizeof(T) == 4) {
+        const T m = (fabs(A[0][0]) + fabs(A[1][0]) + fabs(A[2][0])) * (fabs(A[0][1]) + fabs(A[1][1]) + fabs(A[2][1])) *
+                    (fabs(A[0][2]) + fabs(A[1][2]) + fabs(A[2][2]));
+        if (fabs(d) < (T)0.03125 * m) {
+            double jd[3][3];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) jd[r][c] = (double)A[r][c];
+            d = (T)det3<double>(jd);
+        }
+    }
+    return d;
+}
+
+// B at a non-face point from the position planes (constant offsets), in the
+// form B = (s_x a + s_y b + s_z c) / det(a, b, c) with the unscaled central
+// differences a = x(+x) - x(-x), b, c and the pre-scaled field
+// s = (4 dy dz B0x, 4 dx dz B0y, 4 dx dy B0z): since jac = [a/2dx, b/2dy,
+// c/2dz], this is jac.B0 / det(jac) of B_JacB0 (rungeKutta.cu:79-99) with
+// the constant factors folded.  Returns 1/det(a, b, c) in *rdet
+// (Delta = 1 / (8 dx dy dz rdet)).
+template <typename T>
+__device__ __forceinline__ void b_point(const T* __restrict__ xm, const T* __restrict__ x0, const T* __restrict__ xp,
+                                        int o, const T* __restrict__ B0s, int g, int cs, T Bv[3], T* rdet) {
+    T A[3][3];
+#pragma unroll
+    for (int l = 0; l < 3; l++) {
+        const int q = o + l * PLANE_C;
+        A[l][0] = x0[q + 1] - x0[q - 1];
+        A[l][1] = x0[q + HX2] - x0[q - HX2];
+        A[l][2] = xp[q] - xm[q];
+    }
+    const T r = rcp_stage(det_cols(A));
+    const T s0 = __ldg(&B0s[g]), s1 = __ldg(&B0s[cs + g]), s2 = __ldg(&B0s[2 * cs + g]);
+#pragma unroll
+    for (int l = 0; l < 3; l++) Bv[l] = (A[l][0] * s0 + A[l][1] * s1 + A[l][2] * s2) * r;
+    *rdet = r;
+}
+
+// Shared memory of k_stage_tma, all in the dynamic buffer (no static
+// __shared__ variables, which would shift the dynamic base): the base is
+// rounded up to 128 bytes at run time (the launch asks for 128 bytes of
+// slack), then come the position-plane slots (each a multiple of 128 bytes,
+// the alignment TMA destinations need), the B planes, the mbarriers and flags.
+template <typename T>
+struct TmaSmem {
+    static constexpr int SLOT = slot_elems<T>();
+    static constexpr size_t bytes(int) {
+        return 128 + sizeof(T) * ((size_t)XR2 * SLOT + (size_t)BR2 * 4 * BY2 * BX2) + 8 * XR2 + 16 * TY2 + 16;
+    }
+};
+
+// Kind of a B-region point, fixed for the whole z march of a thread.
+enum { BK_SKIP = 0, BK_INNER = 1, BK_FACE_X = 2, BK_FACE_Y = 3 };
+
+template <typename T, bool PRESS, int NS>
+__global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant__ StageArgsTMA<T> A) {
+    constexpr bool LAST = NS == 5;
+    constexpr int n = NS;
+    constexpr int NB = 4;                      // B components + 1/det(a, b, c)
+    constexpr int PLANE_B = NB * BY2 * BX2;
+    constexpr int BC = BY2 * BX2;              // component stride of a B plane
+    constexpr int SLOT = TmaSmem<T>::SLOT;
+    extern __shared__ __align__(128) unsigned char smraw[];
+
+    const StageArgs<T>& a = A.a;
+    const KP<T>& p = a.p;
+    DevState* st = a.st;
+    if (st->done) return;
+
+    unsigned char* base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
+    T* xs = reinterpret_cast<T*>(base);                                         // XR2 slots of SLOT elements
+    T* bs = xs + XR2 * SLOT;                                                     // BR2 planes of PLANE_B
+    uint64_t* bars = reinterpret_cast<uint64_t*>(bs + BR2 * PLANE_B);           // XR2 mbarriers
+    T* s_wmax = reinterpret_cast<T*>(bars + XR2);                                // TY2 warp maxima
+    int* s_abort = reinterpret_cast<int*>(s_wmax + 2 * TY2);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY2, k0 = blockIdx.z * a.TZ;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const int kend = min(k0 + a.TZ, nz);
+    const int cur = st->cur;
+    const int mapi = (n == 0) ? cur : 2 + ((n - 1) & 1);
+    const CUtensorMap* tmap = &A.tm[mapi];
+    const T dtT = (T)st->dt;
+    const int N = (int)p.N;
+    const int cs = (int)p.cs;
+    const int px = p.px;
+    const int pxy = p.px * p.py;
+    const bool zPeri = p.zPeri != 0;
+    constexpr uint32_t kPlaneBytes = PLANE_X * sizeof(T);
+
+    // self-check of the alignment TMA needs: destination slots on 128 bytes,
+    // mbarriers on 8 bytes, tensor map on 64 bytes, box start on 16 bytes; on
+    // failure record a status bit and issue no copy
+    if ((smem_u32(xs) & 127u) || (smem_u32(bars) & 7u) || (reinterpret_cast<uintptr_t>(tmap) & 63u) ||
+        ((i0 * (int)sizeof(T)) & 15)) {
+        if (tid == 0) atomicOr(&st->status, (unsigned)GM_ST_ALIGN);
+        return;
+    }
+
+    // ---- per-thread descriptors, fixed for the whole z march ----------------
+    // B-phase point 1: the thread's own tile point
+    const int ic = i0 + tx, jc = j0 + ty;
+    const bool own = ic < nx && jc < ny;
+    const int ox1 = (ty + 2) * HX2 + (tx + 2);           // in a position plane
+    const int ob1 = (ty + 1) * BX2 + (tx + 1);           // in a B plane
+    const int gxy1 = (ic + 2) + px * (jc + 2);           // padded offset without the plane term
+    // in a partial tile the ghost column i = nx or row j = ny is a tile point
+    int kind1 = BK_SKIP;
+    const bool xo1 = ic >= nx, yo1 = jc >= ny;
+    if (ic <= nx && jc <= ny && !(xo1 && yo1)) {
+        if (xo1 && !p.xPeri) kind1 = BK_FACE_X;
+        else if (yo1 && !p.yPeri) kind1 = BK_FACE_Y;
+        else kind1 = BK_INNER;
+    }
+    // B-phase point 2: one of the 80 face-halo points (warps 0-2)
+    int jj2 = 0, ii2 = 0, kind2 = BK_SKIP;
+    if (ty == 0) { jj2 = 0; ii2 = tx + 1; }
+    else if (ty == 1) { jj2 = BY2 - 1; ii2 = tx + 1; }
+    else if (ty == 2 && tx < 2 * TY2) { jj2 = (tx % TY2) + 1; ii2 = tx < TY2 ? 0 : BX2 - 1; }
+    else ii2 = -1;
+    const int i2 = i0 - 1 + ii2, j2 = j0 - 1 + jj2;
+    bool xo2 = false, yo2 = false;
+    if (ii2 >= 0 && i2 <= nx && j2 <= ny) {
+        xo2 = (i2 < 0 || i2 >= nx);
+        yo2 = (j2 < 0 || j2 >= ny);
+        if (xo2 && yo2) kind2 = BK_SKIP;
+        else if (xo2 && !p.xPeri) kind2 = BK_FACE_X;
+        else if (yo2 && !p.yPeri) kind2 = BK_FACE_Y;
+        else kind2 = BK_INNER;
+    }
+    const int ox2 = (jj2 + 1) * HX2 + (ii2 + 1);
+    const int ob2 = jj2 * BX2 + ii2;
+    const int gxy2 = (i2 + 2) + px * (j2 + 2);
+    // output point
+    const T exy = own ? p.ex[ic] * p.ey[jc] : (T)0;
+    const int nxy = nx * ny;
+    const int lin0 = ic + nx * jc;
+    const bool img_xy = (p.xPeri && (ic < 2 || ic >= nx - 2)) || (p.yPeri && (jc < 2 || jc >= ny - 2));
+    const T* __restrict__ B0s = a.B0s;
+    const T* __restrict__ ezp = p.ez;
+
+    auto slot = [&](int plane) { return xs + ((plane + 12) % XR2) * SLOT; };
+    auto parity = [&](int plane) { return (uint32_t)(((plane - (k0 - 2)) / XR2) & 1); };
+    // ring positions relative to plane kk, from one modulo per iteration
+    auto xring = [&](int m, int back) { int s = m - back; s += s < 0 ? XR2 : 0; return xs + s * SLOT; };
+    auto bring = [&](int kkb, int back) { return bs + ((kkb - back) & (BR2 - 1)) * PLANE_B; };
+    auto face_b = [&](int face, int i, int j, int kb, T Bv[3]) {
+        Tile<T, NB, XR2, 12> tl;
+        tl.xs = xs;
+        tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = HY2;
+        tl.slot = SLOT;
+        T D;
+        b_face<T>(p, tl, a.B0, face, i, j, kb, Bv, &D);
+    };
+
+    if (tid == 0) {
+        *s_abort = 0;
+        for (int s = 0; s < XR2; s++) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int issued = k0 - 3;   // thread 0: last plane whose copy was issued
+    if (tid == 0) {
+        for (int q = k0 - 2; q <= min(k0 + 1, kend + 1); q++) {
+            uint64_t* b = &bars[(q + 12) % XR2];
+            mbar_expect_tx(b, kPlaneBytes);
+            tma_load_4d(slot(q), tmap, b, i0, j0, q + 2, 0);
+            issued = q;
+        }
+    }
+    int waited = k0 - 3;   // thread 0: last plane whose copy completed
+
+    T dmax = 0;
+    bool bad = false;
+
+    for (int kk = k0; kk <= kend + 2; kk++) {
+        // (1) thread 0 waits for the newest plane the B phase needs
+        if (tid == 0) {
+            const int need = min(kk, kend + 1);
+            while (waited < need && !*s_abort) {
+                const int q = waited + 1;
+                if (!mbar_wait_bounded(&bars[(q + 12) % XR2], parity(q))) {
+                    *s_abort = 1;
+                    atomicOr(&st->status, (unsigned)GM_ST_TIMEOUT);
+                } else {
+                    waited = q;
+                }
+            }
+        }
+        __syncthreads();
+        if (*s_abort) break;
+        // (2) refill: plane kk+1 goes into the slot of plane kk-5, last read in
+        // the previous iteration (all threads are past this iteration's barrier)
+        if (tid == 0 && kk + 1 <= kend + 1 && kk + 1 > issued) {
+            const int q = kk + 1;
+            uint64_t* b = &bars[(q + 12) % XR2];
+            mbar_expect_tx(b, kPlaneBytes);
+            tma_load_4d(slot(q), tmap, b, i0, j0, q + 2, 0);
+            issued = q;
+        }
+        const int mx = (kk + 12) % XR2;     // ring slot of position plane kk
+        const int kkb = kk + 12;             // B ring slot of plane kk - d is (kkb - d) & 3
+        // (3) B and 1/det(a, b, c) on plane kb = kk - 1
+        const int kb = kk - 1;
+        if (kb <= kend) {
+            T* bdst = bring(kkb, 1);
+            const T* xm = xring(mx, 2);
+            const T* x0 = xring(mx, 1);
+            const T* xq = xring(mx, 0);
+            const int gk = pxy * (kb + 2);
+            const bool zo = (kb < 0 || kb >= nz);
+            T Bv[3], R = 0;
+            if (!zo) {
+                if (kind1 != BK_SKIP) {
+                    if (kind1 == BK_INNER) b_point<T>(xm, x0, xq, ox1, B0s, gxy1 + gk, cs, Bv, &R);
+                    else face_b(kind1 == BK_FACE_X ? 0 : 1, ic, jc, kb, Bv);
+                    bdst[ob1] = Bv[0]; bdst[BC + ob1] = Bv[1]; bdst[2 * BC + ob1] = Bv[2]; bdst[3 * BC + ob1] = R;
+                }
+                if (kind2 != BK_SKIP) {
+                    if (kind2 == BK_INNER) b_point<T>(xm, x0, xq, ox2, B0s, gxy2 + gk, cs, Bv, &R);
+                    else face_b(kind2 == BK_FACE_X ? 0 : 1, i2, j2, kb, Bv);
+                    bdst[ob2] = Bv[0]; bdst[BC + ob2] = Bv[1]; bdst[2 * BC + ob2] = Bv[2]; bdst[3 * BC + ob2] = R;
+                }
+            } else if (!zPeri) {
+                // line-tied ghost plane: only the tile points are needed
+                if (own) {
+                    face_b(2, ic, jc, kb, Bv);
+                    bdst[ob1] = Bv[0]; bdst[BC + ob1] = Bv[1]; bdst[2 * BC + ob1] = Bv[2]; bdst[3 * BC + ob1] = R;
+                }
+            } else {
+                // periodic image plane: the tile points and the non-edge halo
+                if (kind1 == BK_INNER && !xo1 && !yo1) {
+                    b_point<T>(xm, x0, xq, ox1, B0s, gxy1 + gk, cs, Bv, &R);
+                    bdst[ob1] = Bv[0]; bdst[BC + ob1] = Bv[1]; bdst[2 * BC + ob1] = Bv[2]; bdst[3 * BC + ob1] = R;
+                }
+                if (kind2 == BK_INNER && !xo2 && !yo2) {
+                    b_point<T>(xm, x0, xq, ox2, B0s, gxy2 + gk, cs, Bv, &R);
+                    bdst[ob2] = Bv[0]; bdst[BC + ob2] = Bv[1]; bdst[2 * BC + ob2] = Bv[2]; bdst[3 * BC + ob2] = R;
+                }
+            }
+        }
+        // (4) J, k_n and the stage position on plane kc = kk - 3 (its B planes
+        // kc-1..kc+1 were all completed before this iteration's barrier)
+        const int kc = kk - 3;
+        if (kc >= k0 && kc < kend && own) {
+            const T* xm = xring(mx, 4);
+            const T* x0 = xring(mx, 3);
+            const T* xq = xring(mx, 2);
+            const T* bm = bring(kkb, 4);
+            const T* b0p = bring(kkb, 3);
+            const T* bq = bring(kkb, 2);
+            // neighbour positions and fields: -x, +x, -y, +y, -z, +z
+            T xn[6][3], bn[6][3], Bc[3];
+#pragma unroll
+            for (int l = 0; l < 3; l++) {
+                const int qx = ox1 + l * PLANE_C, qb = ob1 + l * BC;
+                xn[0][l] = x0[qx - 1];   bn[0][l] = b0p[qb - 1];
+                xn[1][l] = x0[qx + 1];   bn[1][l] = b0p[qb + 1];
+                xn[2][l] = x0[qx - HX2]; bn[2][l] = b0p[qb - BX2];
+                xn[3][l] = x0[qx + HX2]; bn[3][l] = b0p[qb + BX2];
+                xn[4][l] = xm[qx];       bn[4][l] = bm[qb];
+                xn[5][l] = xq[qx];       bn[5][l] = bq[qb];
+                Bc[l] = b0p[qb];
+            }
+            const T rdet = b0p[ob1 + 3 * BC];
+            // Stokes current (current.cu:290-406): the circulations around the
+            // three quadrilaterals through the face neighbours (without the
+            // 1/2 of the edge averages), then the 3x3 solve in closed form.
+            // The quads' area vectors are (1/2) a x b, (1/2) b x c, (1/2) c x a
+            // with the diagonals a = x(+x) - x(-x), b, c (for a quadrilateral,
+            // (1/4) sum of consecutive edge cross products = (1/2) d1 x d2), and
+            // the matrix with those rows has the inverse
+            // 2 [a b c] P / det(a, b, c), so J = (a I1 + b I2 + c I0) / det.
+            T I0 = 0, I1 = 0, I2 = 0;
+#pragma unroll
+            for (int l = 0; l < 3; l++) {
+                // quad 0: -x, -y, +x, +y
+                I0 += (bn[2][l] + bn[0][l]) * (xn[2][l] - xn[0][l]) + (bn[1][l] + bn[2][l]) * (xn[1][l] - xn[2][l]) +
+                      (bn[3][l] + bn[1][l]) * (xn[3][l] - xn[1][l]) + (bn[0][l] + bn[3][l]) * (xn[0][l] - xn[3][l]);
+                // quad 1: -y, -z, +y, +z
+                I1 += (bn[4][l] + bn[2][l]) * (xn[4][l] - xn[2][l]) + (bn[3][l] + bn[4][l]) * (xn[3][l] - xn[4][l]) +
+                      (bn[5][l] + bn[3][l]) * (xn[5][l] - xn[3][l]) + (bn[2][l] + bn[5][l]) * (xn[2][l] - xn[5][l]);
+                // quad 2: -z, -x, +z, +x
+                I2 += (bn[0][l] + bn[4][l]) * (xn[0][l] - xn[4][l]) + (bn[5][l] + bn[0][l]) * (xn[5][l] - xn[0][l]) +
+                      (bn[1][l] + bn[5][l]) * (xn[1][l] - xn[5][l]) + (bn[4][l] + bn[1][l]) * (xn[4][l] - xn[1][l]);
+            }
+            T Jv[3];
+#pragma unroll
+            for (int l = 0; l < 3; l++) {
+                const T al = xn[1][l] - xn[0][l], bl = xn[3][l] - xn[2][l], cl = xn[5][l] - xn[4][l];
+                Jv[l] = (al * I1 + bl * I2 + cl * I0) * rdet;
+            }
+            const int lin = lin0 + nxy * kc;
+            T kn[3];
+            cross3(Jv, Bc, kn);
+            const T f = dtT * (exy * __ldg(&ezp[kc]));
+#pragma unroll
+            for (int l = 0; l < 3; l++) kn[l] *= f;
+            if (PRESS) {
+                Tile<T, NB, XR2, 12> tl;
+                tl.xs = xs;
+                tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = HY2;
+                tl.slot = SLOT;
+                T gp[3];
+                const T D = rcp_stage(rdet) * p.inv8dxdydz;     // Delta = det(a, b, c) / (8 dx dy dz)
+                grad_p<T>(p, tl, ic, jc, kc, D, gp);
+#pragma unroll
+                for (int l = 0; l < 3; l++) kn[l] += -dtT * gp[l];
+            }
+            T xa[3];
+#pragma unroll
+            for (int l = 0; l < 3; l++) xa[l] = x0[ox1 + l * PLANE_C];
+            const bool images = img_xy || (zPeri && (kc < 2 || kc >= nz - 2));
+            const int g = gxy1 + pxy * (kc + 2);
+            if (!LAST) {
+                // x_{n+1} = x_n + sum_{m<=n} (b[n+1][m] - b[n][m]) k_m (rungeKutta.cu:216-227)
+                T km[n > 0 ? n : 1][3];
+#pragma unroll
+                for (int m = 0; m < n; m++) {
+                    km[m][0] = __ldg(&a.K[m][lin]);
+                    km[m][1] = __ldg(&a.K[m][N + lin]);
+                    km[m][2] = __ldg(&a.K[m][2 * N + lin]);
+                }
+#pragma unroll
+                for (int m = 0; m < n; m++) {
+                    const T w = p.db[n][m];
+                    xa[0] += w * km[m][0];
+                    xa[1] += w * km[m][1];
+                    xa[2] += w * km[m][2];
+                }
+                const T w = p.db[n][n];
+#pragma unroll
+                for (int l = 0; l < 3; l++) xa[l] += w * kn[l];
+                T* Kn = a.K[n];
+                Kn[lin] = kn[0];
+                Kn[N + lin] = kn[1];
+                Kn[2 * N + lin] = kn[2];
+                T* Xo = a.XS[n & 1];
+                if (images) {
+                    store_pos<T>(p, Xo, ic, jc, kc, xa);
+                } else {
+                    Xo[g] = xa[0];
+                    Xo[cs + g] = xa[1];
+                    Xo[2 * cs + g] = xa[2];
+                }
+            } else {
+                // stage 5: x_6, x_new, x* and the error norm (rungeKutta.cu:251-339)
+                T km[6][3];
+#pragma unroll
+                for (int m = 0; m < 5; m++) {
+                    km[m][0] = __ldg(&a.K[m][lin]);
+                    km[m][1] = __ldg(&a.K[m][N + lin]);
+                    km[m][2] = __ldg(&a.K[m][2 * N + lin]);
+                }
+#pragma unroll
+                for (int l = 0; l < 3; l++) km[5][l] = kn[l];
+#pragma unroll
+                for (int m = 0; m < 6; m++)
+#pragma unroll
+                    for (int l = 0; l < 3; l++) xa[l] += p.db[5][m] * km[m][l];
+                T xnew[3];
+#pragma unroll
+                for (int l = 0; l < 3; l++) {
+                    xnew[l] = xa[l];
+                    T xst = xa[l];
+                    T dl = 0;
+                    if (l < 2 || p.zUpdate) {
+                        if (p.errMode == 0) {
+#pragma unroll
+                            for (int m = 0; m < 6; m++) {
+                                xnew[l] += p.c[m] * km[m][l];
+                                xst += p.cst[m] * km[m][l];
+                            }
+                            dl = fabs(xnew[l] - xst);
+                        } else {
+                            // sum (c - c*) k: no cancellation against x
+                            T e = 0;
+#pragma unroll
+                            for (int m = 0; m < 6; m++) {
+                                xnew[l] += p.c[m] * km[m][l];
+                                e += p.cmcT[m] * km[m][l];
+                            }
+                            dl = fabs(e);
+                        }
+                    }
+                    if (dl > dmax) dmax = dl;     // NaN never wins (maths.cu:144-153)
+                    if (!isfinite(dl) || !isfinite(xnew[l])) bad = true;   // NaN/Inf anywhere in k_0..k_5
+                }
+                if (images) {
+                    store_pos<T>(p, a.X[cur], ic, jc, kc, xa);
+                    store_pos<T>(p, a.X[cur ^ 1], ic, jc, kc, xnew);
+                } else {
+                    T* X6 = a.X[cur];
+                    T* Xn = a.X[cur ^ 1];
+                    X6[g] = xa[0]; X6[cs + g] = xa[1]; X6[2 * cs + g] = xa[2];
+                    Xn[g] = xnew[0]; Xn[cs + g] = xnew[1]; Xn[2 * cs + g] = xnew[2];
+                }
+            }
+        }
+    }
+    // drain copies still in flight (after an abort), bounded
+    if (tid == 0 && *s_abort) {
+        for (int q = waited + 1; q <= issued; q++) mbar_wait_bounded(&bars[(q + 12) % XR2], parity(q));
+    }
+    if (bad) atomicOr(&st->status, (unsigned)GM_ST_NAN);
+    if (LAST) {
+        for (int o = 16; o > 0; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+        if (tx == 0) s_wmax[ty] = dmax;
+        __syncthreads();
+        if (tid == 0) {
+            T m = 0;
+            for (int w = 0; w < TY2; w++) m = fmax(m, s_wmax[w]);
+            if (m > 0) atomicMax(&st->maxDeltaBits, (unsigned long long)__double_as_longlong((double)m));
+        }
+    }
+}
+
+template <typename T>
+size_t stage_tma_smem_bytes(int pressure) {
+    return TmaSmem<T>::bytes(pressure ? 4 : 3);
+}
+
+template <typename T, bool PRESS, int NS>
+static cudaError_t prep_one() {
+    return cudaFuncSetAttribute(k_stage_tma<T, PRESS, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+template <typename T>
+cudaError_t prepare_stage_tma() {
+    cudaError_t e;
+    if ((e = prep_one<T, false, 0>()) || (e = prep_one<T, false, 1>()) || (e = prep_one<T, false, 2>()) ||
+        (e = prep_one<T, false, 3>()) || (e = prep_one<T, false, 4>()) || (e = prep_one<T, false, 5>()) ||
+        (e = prep_one<T, true, 0>()) || (e = prep_one<T, true, 1>()) || (e = prep_one<T, true, 2>()) ||
+        (e = prep_one<T, true, 3>()) || (e = prep_one<T, true, 4>()) || (e = prep_one<T, true, 5>()))
+        return e;
+    return cudaSuccess;
+}
+
+template <typename T>
+int stage_tma_occupancy(int pressure) {
+    int nb = 0;
+    const size_t sm = stage_tma_smem_bytes<T>(pressure);
+    cudaError_t e = pressure
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma<T, true, 0>, TX * TY2, sm)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma<T, false, 0>, TX * TY2, sm);
+    return e == cudaSuccess && nb > 0 ? nb : 1;
+}
+
+template <typename T>
+cudaError_t launch_stage_tma(const StageArgsTMA<T>& A, int pressure, dim3 grid, cudaStream_t s) {
+    const dim3 block(TX, TY2, 1);
+    const size_t sm = stage_tma_smem_bytes<T>(pressure);
+#define GMK_LAUNCH_N(PR)                                                              \
+    switch (A.a.n) {                                                                  \
+        case 0: k_stage_tma<T, PR, 0><<<grid, block, sm, s>>>(A); break;              \
+        case 1: k_stage_tma<T, PR, 1><<<grid, block, sm, s>>>(A); break;              \
+        case 2: k_stage_tma<T, PR, 2><<<grid, block, sm, s>>>(A); break;              \
+        case 3: k_stage_tma<T, PR, 3><<<grid, block, sm, s>>>(A); break;              \
+        case 4: k_stage_tma<T, PR, 4><<<grid, block, sm, s>>>(A); break;              \
+        default: k_stage_tma<T, PR, 5><<<grid, block, sm, s>>>(A); break;             \
+    }
+    if (pressure) {
+        GMK_LAUNCH_N(true)
+    } else {
+        GMK_LAUNCH_N(false)
+    }
+#undef GMK_LAUNCH_N
+    return cudaGetLastError();
+}
+
+#define GMK_INSTANTIATE_TMA(T)                                                                \
+    template size_t stage_tma_smem_bytes<T>(int);                                             \
+    template cudaError_t prepare_stage_tma<T>();                                              \
+    template int stage_tma_occupancy<T>(int);                                                 \
+    template cudaError_t launch_stage_tma<T>(const StageArgsTMA<T>&, int, dim3, cudaStream_t);
+
+}  // namespace gmk

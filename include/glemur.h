@@ -52,6 +52,8 @@ extern "C" {
 #define GM_ST_DETJAC     2u
 #define GM_ST_DTMIN      4u
 #define GM_ST_DONE       8u
+#define GM_ST_TIMEOUT   16u   /* a bounded wait on an asynchronous copy ran out */
+#define GM_ST_ALIGN     32u   /* a copy was skipped: its shared-memory or tensor-map alignment check failed */
 
 /*
  * Run parameters.  Mirrors struct Parameters (src/global.h:44-108) field by
