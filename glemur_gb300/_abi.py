@@ -124,6 +124,7 @@ SIGNATURES = {
     "gm_download": (C.c_int, [VP, VP, VP, VP, VP]),
     "gm_download_k": (C.c_int, [VP, C.c_int, VP]),
     "gm_download_x": (C.c_int, [VP, C.c_int, VP]),
+    "gm_reduce_noalloc": (C.c_int, [P(GmParams), VP, VP, VP, VP, VP]),
     "gm_launch_count": (C.c_int64, [VP]),
     "gm_last_error": (C.c_char_p, []),
     "gm_version": (C.c_char_p, []),

@@ -241,6 +241,34 @@ int gm_download_k(gm_handle* h, int m, void* k);
  * rejected retry; 6: x_new of the combine (src/rungeKutta.cu:345). */
 int gm_download_x(gm_handle* h, int which, void* xb);
 
+/* Largest nz that gm_reduce_noalloc accepts: the number of per-plane partial
+ * sums its fixed scratch array holds. */
+#define GM_NOALLOC_MAX_PLANES 4096
+
+/* The reductions of gm_refresh computed from fields the caller already holds
+ * on the device, without allocating any device memory.  This entry point has
+ * no counterpart in the reference.  It is for callers that cannot allocate at
+ * the point where they want diagnostics: code inside a captured CUDA graph or
+ * a stream-ordered pipeline (cudaMalloc/cudaFree synchronise or cannot be
+ * captured), host callbacks, or applications whose device memory belongs to
+ * their own allocator.
+ *   B, J, detJac: DEVICE arrays of REAL in the layouts gm_download returns
+ *                 (B ghosted AoS, J inner AoS, detJac ghosted scalar).
+ *   out:          DEVICE pointer to one gm_reduction; wedgeMin, convex and
+ *                 errXb_XbAn need the grid and are set to NaN.
+ *   stream:       cudaStream_t to run on (NULL: the legacy default stream).
+ * The per-plane partial sums live in one fixed device array of
+ * GM_NOALLOC_MAX_PLANES x 16 doubles (512 KiB, held by every GPU that loads
+ * the library until the process exits); nz above GM_NOALLOC_MAX_PLANES is
+ * rejected with GM_EPARAM.  Each call overwrites every partial it reads, so
+ * nothing has to be cleared between calls, but all calls share that array:
+ * calls that overlap on the GPU (concurrent streams) race.  The first call on
+ * a device looks up the array's device address with that device current;
+ * make that first call before any stream capture.  No cudaMalloc, cudaFree or
+ * allocating library routine is called. */
+int gm_reduce_noalloc(const gm_params* p, const void* B, const void* J, const void* detJac,
+                      gm_reduction* out, void* stream);
+
 /* Cumulative kernel launches issued by this handle (for accounting). */
 int64_t gm_launch_count(const gm_handle* h);
 
