@@ -54,7 +54,8 @@ class GmParams(C.Structure):
         ("redU2", C.c_int32), ("redUMax", C.c_int32),
         ("precision", C.c_int32), ("errMode", C.c_int32),
         ("p0Amp", C.c_double), ("p0Width", C.c_double),
-        ("reserved", C.c_int32 * 8),
+        ("stageKernel", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
     def real_dtype(self):

@@ -64,6 +64,7 @@ int check_params(const gm_params* p) {
         return gm::fail(GM_EPARAM, "initial-distortion ghost corrections (initShearA/B != 0) are not implemented");
     if (!(p->dx > 0 && p->dy > 0 && p->dz > 0)) return gm::fail(GM_EPARAM, "dx, dy, dz must be > 0 (call gm_params_derive)");
     if (p->errMode != 0 && p->errMode != 1) return gm::fail(GM_EPARAM, "errMode must be 0 or 1");
+    if (p->stageKernel != 0 && p->stageKernel != 1) return gm::fail(GM_EPARAM, "stageKernel must be 0 or 1");
     return GM_OK;
 }
 
@@ -259,6 +260,7 @@ struct Impl : ImplBase {
         smem_stage = gmk::stage_smem_bytes<T>(TY, gmk::MODE_STAGE, p->pressure);
         smem_diag = gmk::stage_smem_bytes<T>(TY, gmk::MODE_DIAG, p->pressure);
         nparts = (int)(grid.x * grid.y * grid.z);
+        use_tma = p->stageKernel == 0;
         if (use_tma) {
             if ((rc = init_tma(nsm))) return rc;
         }
@@ -299,7 +301,7 @@ struct Impl : ImplBase {
             if (tz < 4 && nz >= 4) break;
             const long long tiles = ncol * ((nz + tz - 1) / tz);
             const long long per_sm = (tiles + nsm - 1) / nsm;
-            const double cost = (double)per_sm * (tz + 3);
+            const double cost = (double)per_sm * (tz + 2);   // tz + 2 iterations per tile
             if (cost < best * 0.999) { best = cost; TZ2 = tz; }
         }
         grid2 = dim3((unsigned)((nx + gmk::TX - 1) / gmk::TX), (unsigned)((ny + ty - 1) / ty),

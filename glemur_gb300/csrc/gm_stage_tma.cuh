@@ -25,7 +25,10 @@ constexpr int TY2 = 8;                   // tile rows (= warps per CTA)
 constexpr int HX2 = TX + 4, HY2 = TY2 + 4;
 constexpr int BX2 = TX + 2, BY2 = TY2 + 2;
 constexpr int XR2 = 6;                   // position-plane ring
-constexpr int BR2 = 4;                   // B-plane ring
+// resident CTAs per SM the stage kernel is compiled for (register budget)
+#ifndef GM_STAGE_MINB
+#define GM_STAGE_MINB 3
+#endif
 constexpr int PLANE_C = HY2 * HX2;       // elements of one component of a position plane
 constexpr int PLANE_X = 3 * PLANE_C;
 constexpr unsigned kWaitLimit = 1u << 22;
@@ -110,50 +113,74 @@ __device__ __forceinline__ T det_cols(const T A[3][3]) {
 // differences a = x(+x) - x(-x), b, c and the pre-scaled field
 // s = (4 dy dz B0x, 4 dx dz B0y, 4 dx dy B0z): since jac = [a/2dx, b/2dy,
 // c/2dz], this is jac.B0 / det(jac) of B_JacB0 (rungeKutta.cu:79-99) with
-// the constant factors folded.  Returns 1/det(a, b, c) in *rdet
-// (Delta = 1 / (8 dx dy dz rdet)).
+// the constant factors folded.  Returns the columns a, b, c in Am[l][0..2]
+// and 1/det(a, b, c) in *rdet (Delta = 1 / (8 dx dy dz rdet)).
 template <typename T>
 __device__ __forceinline__ void b_point(const T* __restrict__ xm, const T* __restrict__ x0, const T* __restrict__ xp,
-                                        int o, const T* __restrict__ B0s, int g, int cs, T Bv[3], T* rdet) {
-    T A[3][3];
+                                        int o, const T* __restrict__ B0s, int g, int cs, T Bv[3], T Am[3][3],
+                                        T* rdet) {
+    const T s0 = __ldg(&B0s[g]), s1 = __ldg(&B0s[cs + g]), s2 = __ldg(&B0s[2 * cs + g]);
 #pragma unroll
     for (int l = 0; l < 3; l++) {
         const int q = o + l * PLANE_C;
-        A[l][0] = x0[q + 1] - x0[q - 1];
-        A[l][1] = x0[q + HX2] - x0[q - HX2];
-        A[l][2] = xp[q] - xm[q];
+        Am[l][0] = x0[q + 1] - x0[q - 1];
+        Am[l][1] = x0[q + HX2] - x0[q - HX2];
+        Am[l][2] = xp[q] - xm[q];
     }
-    const T r = rcp_stage(det_cols(A));
-    const T s0 = __ldg(&B0s[g]), s1 = __ldg(&B0s[cs + g]), s2 = __ldg(&B0s[2 * cs + g]);
+    const T r = rcp_stage(det_cols(Am));
 #pragma unroll
-    for (int l = 0; l < 3; l++) Bv[l] = (A[l][0] * s0 + A[l][1] * s1 + A[l][2] * s2) * r;
+    for (int l = 0; l < 3; l++) Bv[l] = (Am[l][0] * s0 + Am[l][1] * s1 + Am[l][2] * s2) * r;
     *rdet = r;
+}
+
+// One B point in a shared-memory B plane: three components and a pad, so a
+// neighbour is one 128-bit load (two for double).
+__device__ __forceinline__ void st_b(float* d, const float v[3]) {
+    *reinterpret_cast<float4*>(d) = make_float4(v[0], v[1], v[2], 0.f);
+}
+__device__ __forceinline__ void st_b(double* d, const double v[3]) {
+    reinterpret_cast<double2*>(d)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2*>(d)[1] = make_double2(v[2], 0.0);
+}
+__device__ __forceinline__ void ld_b(const float* d, float v[3]) {
+    const float4 q = *reinterpret_cast<const float4*>(d);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z;
+}
+__device__ __forceinline__ void ld_b(const double* d, double v[3]) {
+    const double2 q0 = reinterpret_cast<const double2*>(d)[0], q1 = reinterpret_cast<const double2*>(d)[1];
+    v[0] = q0.x; v[1] = q0.y; v[2] = q1.x;
 }
 
 // Shared memory of k_stage_tma, all in the dynamic buffer (no static
 // __shared__ variables, which would shift the dynamic base): the base is
 // rounded up to 128 bytes at run time (the launch asks for 128 bytes of
 // slack), then come the position-plane slots (each a multiple of 128 bytes,
-// the alignment TMA destinations need), the B planes, the mbarriers and flags.
+// the alignment TMA destinations need), the two B planes, the mbarriers and
+// flags.
 template <typename T>
 struct TmaSmem {
     static constexpr int SLOT = slot_elems<T>();
+    static constexpr int PLANE_B = 4 * BY2 * BX2;   // elements of one B plane
     static constexpr size_t bytes(int) {
-        return 128 + sizeof(T) * ((size_t)XR2 * SLOT + (size_t)BR2 * 4 * BY2 * BX2) + 8 * XR2 + 16 * TY2 + 16;
+        return 128 + sizeof(T) * ((size_t)XR2 * SLOT + 2 * (size_t)PLANE_B) + 8 * XR2 + 16 * TY2 + 16;
     }
 };
 
 // Kind of a B-region point, fixed for the whole z march of a thread.
 enum { BK_SKIP = 0, BK_INNER = 1, BK_FACE_X = 2, BK_FACE_Y = 3 };
 
+// One RK stage over a 32 x 8 x TZ block of points.  Iteration kk of the z
+// march computes B on plane kb = kk - 1 (the tile and its face halo) and
+// then J, k_n and the stage position on plane kc = kk - 2.  Each thread keeps
+// its own column's B at kc - 1, kc, kc + 1 and the diagonals a, b, c and
+// 1/det of plane kc in registers, so J needs only the four in-plane
+// neighbours' B from shared memory, written in the previous iteration.
 template <typename T, bool PRESS, int NS>
-__global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant__ StageArgsTMA<T> A) {
+__global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2) k_stage_tma(const __grid_constant__ StageArgsTMA<T> A) {
     constexpr bool LAST = NS == 5;
     constexpr int n = NS;
-    constexpr int NB = 4;                      // B components + 1/det(a, b, c)
-    constexpr int PLANE_B = NB * BY2 * BX2;
-    constexpr int BC = BY2 * BX2;              // component stride of a B plane
     constexpr int SLOT = TmaSmem<T>::SLOT;
+    constexpr int PLANE_B = TmaSmem<T>::PLANE_B;
     extern __shared__ __align__(128) unsigned char smraw[];
 
     const StageArgs<T>& a = A.a;
@@ -163,8 +190,8 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
 
     unsigned char* base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
     T* xs = reinterpret_cast<T*>(base);                                         // XR2 slots of SLOT elements
-    T* bs = xs + XR2 * SLOT;                                                     // BR2 planes of PLANE_B
-    uint64_t* bars = reinterpret_cast<uint64_t*>(bs + BR2 * PLANE_B);           // XR2 mbarriers
+    T* bs = xs + XR2 * SLOT;                                                     // 2 B planes of PLANE_B
+    uint64_t* bars = reinterpret_cast<uint64_t*>(bs + 2 * PLANE_B);             // XR2 mbarriers
     T* s_wmax = reinterpret_cast<T*>(bars + XR2);                                // TY2 warp maxima
     int* s_abort = reinterpret_cast<int*>(s_wmax + 2 * TY2);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -185,8 +212,8 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
     // self-check of the alignment TMA needs: destination slots on 128 bytes,
     // mbarriers on 8 bytes, tensor map on 64 bytes, box start on 16 bytes; on
     // failure record a status bit and issue no copy
-    if ((smem_u32(xs) & 127u) || (smem_u32(bars) & 7u) || (reinterpret_cast<uintptr_t>(tmap) & 63u) ||
-        ((i0 * (int)sizeof(T)) & 15)) {
+    if ((smem_u32(xs) & 127u) || (smem_u32(bs) & 15u) || (smem_u32(bars) & 7u) ||
+        (reinterpret_cast<uintptr_t>(tmap) & 63u) || ((i0 * (int)sizeof(T)) & 15)) {
         if (tid == 0) atomicOr(&st->status, (unsigned)GM_ST_ALIGN);
         return;
     }
@@ -196,7 +223,7 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
     const int ic = i0 + tx, jc = j0 + ty;
     const bool own = ic < nx && jc < ny;
     const int ox1 = (ty + 2) * HX2 + (tx + 2);           // in a position plane
-    const int ob1 = (ty + 1) * BX2 + (tx + 1);           // in a B plane
+    const int ob1 = 4 * ((ty + 1) * BX2 + (tx + 1));     // in a B plane
     const int gxy1 = (ic + 2) + px * (jc + 2);           // padded offset without the plane term
     // in a partial tile the ghost column i = nx or row j = ny is a tile point
     int kind1 = BK_SKIP;
@@ -223,7 +250,7 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
         else kind2 = BK_INNER;
     }
     const int ox2 = (jj2 + 1) * HX2 + (ii2 + 1);
-    const int ob2 = jj2 * BX2 + ii2;
+    const int ob2 = 4 * (jj2 * BX2 + ii2);
     const int gxy2 = (i2 + 2) + px * (j2 + 2);
     // output point
     const T exy = own ? p.ex[ic] * p.ey[jc] : (T)0;
@@ -237,9 +264,8 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
     auto parity = [&](int plane) { return (uint32_t)(((plane - (k0 - 2)) / XR2) & 1); };
     // ring positions relative to plane kk, from one modulo per iteration
     auto xring = [&](int m, int back) { int s = m - back; s += s < 0 ? XR2 : 0; return xs + s * SLOT; };
-    auto bring = [&](int kkb, int back) { return bs + ((kkb - back) & (BR2 - 1)) * PLANE_B; };
     auto face_b = [&](int face, int i, int j, int kb, T Bv[3]) {
-        Tile<T, NB, XR2, 12> tl;
+        Tile<T, 4, XR2, 12> tl;
         tl.xs = xs;
         tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = HY2;
         tl.slot = SLOT;
@@ -253,9 +279,10 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    // position planes k0-2 .. kend+1 stream through the ring two planes ahead
     int issued = k0 - 3;   // thread 0: last plane whose copy was issued
     if (tid == 0) {
-        for (int q = k0 - 2; q <= min(k0 + 1, kend + 1); q++) {
+        for (int q = k0 - 2; q <= min(k0 + 2, kend + 1); q++) {
             uint64_t* b = &bars[(q + 12) % XR2];
             mbar_expect_tx(b, kPlaneBytes);
             tma_load_4d(slot(q), tmap, b, i0, j0, q + 2, 0);
@@ -266,8 +293,12 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
 
     T dmax = 0;
     bool bad = false;
+    // own column: B at kc-1, kc, kc+1 and a, b, c, 1/det at kc
+    T Bm[3] = {0, 0, 0}, Bz[3] = {0, 0, 0}, Bp[3] = {0, 0, 0};
+    T Ac[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Rc = 0;
+    T An[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Rn = 0;
 
-    for (int kk = k0; kk <= kend + 2; kk++) {
+    for (int kk = k0; kk <= kend + 1; kk++) {
         // (1) thread 0 waits for the newest plane the B phase needs
         if (tid == 0) {
             const int need = min(kk, kend + 1);
@@ -283,120 +314,94 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
         }
         __syncthreads();
         if (*s_abort) break;
-        // (2) refill: plane kk+1 goes into the slot of plane kk-5, last read in
+        // (2) refill: plane kk+2 goes into the slot of plane kk-4, last read in
         // the previous iteration (all threads are past this iteration's barrier)
-        if (tid == 0 && kk + 1 <= kend + 1 && kk + 1 > issued) {
-            const int q = kk + 1;
+        if (tid == 0 && kk + 2 <= kend + 1 && kk + 2 > issued) {
+            const int q = kk + 2;
             uint64_t* b = &bars[(q + 12) % XR2];
             mbar_expect_tx(b, kPlaneBytes);
             tma_load_4d(slot(q), tmap, b, i0, j0, q + 2, 0);
             issued = q;
         }
         const int mx = (kk + 12) % XR2;     // ring slot of position plane kk
-        const int kkb = kk + 12;             // B ring slot of plane kk - d is (kkb - d) & 3
-        // (3) B and 1/det(a, b, c) on plane kb = kk - 1
+        // (3) B on plane kb = kk - 1 into B plane kb & 1
         const int kb = kk - 1;
-        if (kb <= kend) {
-            T* bdst = bring(kkb, 1);
+        T Bv[3] = {0, 0, 0};
+        {
+            T* bdst = bs + (kb & 1) * PLANE_B;
             const T* xm = xring(mx, 2);
             const T* x0 = xring(mx, 1);
             const T* xq = xring(mx, 0);
             const int gk = pxy * (kb + 2);
             const bool zo = (kb < 0 || kb >= nz);
-            T Bv[3], R = 0;
+            T Bh[3], Ah[3][3], Rh;
             if (!zo) {
                 if (kind1 != BK_SKIP) {
-                    if (kind1 == BK_INNER) b_point<T>(xm, x0, xq, ox1, B0s, gxy1 + gk, cs, Bv, &R);
+                    if (kind1 == BK_INNER) b_point<T>(xm, x0, xq, ox1, B0s, gxy1 + gk, cs, Bv, An, &Rn);
                     else face_b(kind1 == BK_FACE_X ? 0 : 1, ic, jc, kb, Bv);
-                    bdst[ob1] = Bv[0]; bdst[BC + ob1] = Bv[1]; bdst[2 * BC + ob1] = Bv[2]; bdst[3 * BC + ob1] = R;
+                    st_b(bdst + ob1, Bv);
                 }
                 if (kind2 != BK_SKIP) {
-                    if (kind2 == BK_INNER) b_point<T>(xm, x0, xq, ox2, B0s, gxy2 + gk, cs, Bv, &R);
-                    else face_b(kind2 == BK_FACE_X ? 0 : 1, i2, j2, kb, Bv);
-                    bdst[ob2] = Bv[0]; bdst[BC + ob2] = Bv[1]; bdst[2 * BC + ob2] = Bv[2]; bdst[3 * BC + ob2] = R;
+                    if (kind2 == BK_INNER) b_point<T>(xm, x0, xq, ox2, B0s, gxy2 + gk, cs, Bh, Ah, &Rh);
+                    else face_b(kind2 == BK_FACE_X ? 0 : 1, i2, j2, kb, Bh);
+                    st_b(bdst + ob2, Bh);
                 }
             } else if (!zPeri) {
-                // line-tied ghost plane: only the tile points are needed
-                if (own) {
-                    face_b(2, ic, jc, kb, Bv);
-                    bdst[ob1] = Bv[0]; bdst[BC + ob1] = Bv[1]; bdst[2 * BC + ob1] = Bv[2]; bdst[3 * BC + ob1] = R;
-                }
+                // line-tied ghost plane: only the own column is needed
+                if (own) face_b(2, ic, jc, kb, Bv);
             } else {
-                // periodic image plane: the tile points and the non-edge halo
-                if (kind1 == BK_INNER && !xo1 && !yo1) {
-                    b_point<T>(xm, x0, xq, ox1, B0s, gxy1 + gk, cs, Bv, &R);
-                    bdst[ob1] = Bv[0]; bdst[BC + ob1] = Bv[1]; bdst[2 * BC + ob1] = Bv[2]; bdst[3 * BC + ob1] = R;
-                }
-                if (kind2 == BK_INNER && !xo2 && !yo2) {
-                    b_point<T>(xm, x0, xq, ox2, B0s, gxy2 + gk, cs, Bv, &R);
-                    bdst[ob2] = Bv[0]; bdst[BC + ob2] = Bv[1]; bdst[2 * BC + ob2] = Bv[2]; bdst[3 * BC + ob2] = R;
-                }
+                // periodic image plane: only the own column is needed
+                if (own) b_point<T>(xm, x0, xq, ox1, B0s, gxy1 + gk, cs, Bv, An, &Rn);
             }
         }
-        // (4) J, k_n and the stage position on plane kc = kk - 3 (its B planes
-        // kc-1..kc+1 were all completed before this iteration's barrier)
-        const int kc = kk - 3;
-        if (kc >= k0 && kc < kend && own) {
-            const T* xm = xring(mx, 4);
-            const T* x0 = xring(mx, 3);
-            const T* xq = xring(mx, 2);
-            const T* bm = bring(kkb, 4);
-            const T* b0p = bring(kkb, 3);
-            const T* bq = bring(kkb, 2);
-            // neighbour positions and fields: -x, +x, -y, +y, -z, +z
-            T xn[6][3], bn[6][3], Bc[3];
 #pragma unroll
-            for (int l = 0; l < 3; l++) {
-                const int qx = ox1 + l * PLANE_C, qb = ob1 + l * BC;
-                xn[0][l] = x0[qx - 1];   bn[0][l] = b0p[qb - 1];
-                xn[1][l] = x0[qx + 1];   bn[1][l] = b0p[qb + 1];
-                xn[2][l] = x0[qx - HX2]; bn[2][l] = b0p[qb - BX2];
-                xn[3][l] = x0[qx + HX2]; bn[3][l] = b0p[qb + BX2];
-                xn[4][l] = xm[qx];       bn[4][l] = bm[qb];
-                xn[5][l] = xq[qx];       bn[5][l] = bq[qb];
-                Bc[l] = b0p[qb];
-            }
-            const T rdet = b0p[ob1 + 3 * BC];
-            // Stokes current (current.cu:290-406): the circulations around the
-            // three quadrilaterals through the face neighbours (without the
-            // 1/2 of the edge averages), then the 3x3 solve in closed form.
-            // The quads' area vectors are (1/2) a x b, (1/2) b x c, (1/2) c x a
-            // with the diagonals a = x(+x) - x(-x), b, c (for a quadrilateral,
-            // (1/4) sum of consecutive edge cross products = (1/2) d1 x d2), and
-            // the matrix with those rows has the inverse
+        for (int l = 0; l < 3; l++) { Bm[l] = Bz[l]; Bz[l] = Bp[l]; Bp[l] = Bv[l]; }
+        // (4) J, k_n and the stage position on plane kc = kk - 2
+        const int kc = kk - 2;
+        if (kc >= k0 && own) {
+            const T* bc = bs + (kc & 1) * PLANE_B;
+            // in-plane neighbours' B: -x, +x, -y, +y
+            T bxm[3], bxp[3], bym[3], byp[3];
+            ld_b(bc + ob1 - 4, bxm);
+            ld_b(bc + ob1 + 4, bxp);
+            ld_b(bc + ob1 - 4 * BX2, bym);
+            ld_b(bc + ob1 + 4 * BX2, byp);
+            // Stokes current (current.cu:290-406).  The circulation around a
+            // quadrilateral P1..P4, sum (B_a + B_b).(x_b - x_a) over its edges,
+            // regroups exactly into sum B_a.(x_{a+1} - x_{a-1}); for the quads
+            // through the face neighbours (-x,-y,+x,+y), (-y,-z,+y,+z) and
+            // (-z,-x,+z,+x) that is I0 = b.dxB - a.dyB, I1 = c.dyB - b.dzB and
+            // I2 = a.dzB - c.dxB with the diagonals a = x(+x) - x(-x), b, c and
+            // dxB = B(+x) - B(-x), ...  The quads' area vectors are
+            // (1/2) a x b, (1/2) b x c, (1/2) c x a (for a quadrilateral,
+            // (1/4) sum of consecutive edge cross products = (1/2) d1 x d2),
+            // and the matrix with those rows has the inverse
             // 2 [a b c] P / det(a, b, c), so J = (a I1 + b I2 + c I0) / det.
             T I0 = 0, I1 = 0, I2 = 0;
 #pragma unroll
             for (int l = 0; l < 3; l++) {
-                // quad 0: -x, -y, +x, +y
-                I0 += (bn[2][l] + bn[0][l]) * (xn[2][l] - xn[0][l]) + (bn[1][l] + bn[2][l]) * (xn[1][l] - xn[2][l]) +
-                      (bn[3][l] + bn[1][l]) * (xn[3][l] - xn[1][l]) + (bn[0][l] + bn[3][l]) * (xn[0][l] - xn[3][l]);
-                // quad 1: -y, -z, +y, +z
-                I1 += (bn[4][l] + bn[2][l]) * (xn[4][l] - xn[2][l]) + (bn[3][l] + bn[4][l]) * (xn[3][l] - xn[4][l]) +
-                      (bn[5][l] + bn[3][l]) * (xn[5][l] - xn[3][l]) + (bn[2][l] + bn[5][l]) * (xn[2][l] - xn[5][l]);
-                // quad 2: -z, -x, +z, +x
-                I2 += (bn[0][l] + bn[4][l]) * (xn[0][l] - xn[4][l]) + (bn[5][l] + bn[0][l]) * (xn[5][l] - xn[0][l]) +
-                      (bn[1][l] + bn[5][l]) * (xn[1][l] - xn[5][l]) + (bn[4][l] + bn[1][l]) * (xn[4][l] - xn[1][l]);
+                const T dx = bxp[l] - bxm[l], dy = byp[l] - bym[l], dz = Bp[l] - Bm[l];
+                I0 += Ac[l][1] * dx - Ac[l][0] * dy;
+                I1 += Ac[l][2] * dy - Ac[l][1] * dz;
+                I2 += Ac[l][0] * dz - Ac[l][2] * dx;
             }
             T Jv[3];
 #pragma unroll
-            for (int l = 0; l < 3; l++) {
-                const T al = xn[1][l] - xn[0][l], bl = xn[3][l] - xn[2][l], cl = xn[5][l] - xn[4][l];
-                Jv[l] = (al * I1 + bl * I2 + cl * I0) * rdet;
-            }
+            for (int l = 0; l < 3; l++) Jv[l] = (Ac[l][0] * I1 + Ac[l][1] * I2 + Ac[l][2] * I0) * Rc;
             const int lin = lin0 + nxy * kc;
             T kn[3];
-            cross3(Jv, Bc, kn);
+            cross3(Jv, Bz, kn);
             const T f = dtT * (exy * __ldg(&ezp[kc]));
 #pragma unroll
             for (int l = 0; l < 3; l++) kn[l] *= f;
+            const T* x0 = xring(mx, 2);   // position plane kc
             if (PRESS) {
-                Tile<T, NB, XR2, 12> tl;
+                Tile<T, 4, XR2, 12> tl;
                 tl.xs = xs;
                 tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = HY2;
                 tl.slot = SLOT;
                 T gp[3];
-                const T D = rcp_stage(rdet) * p.inv8dxdydz;     // Delta = det(a, b, c) / (8 dx dy dz)
+                const T D = rcp_stage(Rc) * p.inv8dxdydz;     // Delta = det(a, b, c) / (8 dx dy dz)
                 grad_p<T>(p, tl, ic, jc, kc, D, gp);
 #pragma unroll
                 for (int l = 0; l < 3; l++) kn[l] += -dtT * gp[l];
@@ -491,6 +496,12 @@ __global__ void __launch_bounds__(TX * TY2, 4) k_stage_tma(const __grid_constant
                 }
             }
         }
+        // the diagonals of plane kb become those of the next iteration's kc
+#pragma unroll
+        for (int l = 0; l < 3; l++) {
+            Ac[l][0] = An[l][0]; Ac[l][1] = An[l][1]; Ac[l][2] = An[l][2];
+        }
+        Rc = Rn;
     }
     // drain copies still in flight (after an abort), bounded
     if (tid == 0 && *s_abort) {

@@ -131,7 +131,7 @@ const Field kRun[] = {
     F_(jxbAverWeight, 'r', 1), F_(xPeri, 'l', 1), F_(yPeri, 'l', 1), F_(zPeri, 'l', 1),
     F_(epsilonProf, 'l', 1), F_(jMethod, 's', 1), F_(pMethod, 's', 1),
     // extensions of this library (absent from reference files, so harmless)
-    F_(errMode, 'i', 1), F_(p0Amp, 'r', 1), F_(p0Width, 'r', 1)};
+    F_(errMode, 'i', 1), F_(p0Amp, 'r', 1), F_(p0Width, 'r', 1), F_(stageKernel, 'i', 1)};
 const Field kIo[] = {
     F_(nTs, 'i', 1), F_(dtDump, 'r', 1), F_(dtSave, 'r', 1), F_(dumpJ, 'l', 1), F_(dumpDetJac, 'l', 1),
     F_(dumpCellVol, 'l', 1), F_(dumpConvexity, 'l', 1), F_(dumpWedgeMin, 'l', 1), F_(redB2, 'l', 1),

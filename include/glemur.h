@@ -113,7 +113,10 @@ typedef struct gm_params {
     double  p0Amp;       /* pressure profile p0(X) = beta*(1 + p0Amp*exp(-r^2/p0Width^2));
                             p0Amp = 0 gives the reference's uniform p0 = beta  */
     double  p0Width;
-    int32_t reserved[8];
+    int32_t stageKernel; /* 0: TMA-fed stage kernel (default); 1: the generic
+                            tiled stage kernel (plain loads), kept for
+                            cross-checks of the former  */
+    int32_t reserved[7];
 } gm_params;
 
 /* Result of one attempted adaptive step (src/main.cu:259-384). */
