@@ -14,6 +14,9 @@ ERRORS = {
     -6: "GM_EDTMIN", -7: "GM_ETIMEOUT", -8: "GM_ENOTREADY", -9: "GM_EIO",
 }
 GM_ST_NAN, GM_ST_DETJAC, GM_ST_DTMIN, GM_ST_DONE = 1, 2, 4, 8
+GM_ST_TIMEOUT, GM_ST_ALIGN, GM_ST_EVENT = 16, 32, 64
+GM_EV_TS, GM_EV_DUMP, GM_EV_SAVE, GM_EV_LAST = 1, 2, 4, 8
+GM_EPARAM, GM_EALLOC, GM_ECUDA, GM_ENAN, GM_EDETJAC, GM_EDTMIN, GM_ETIMEOUT, GM_ENOTREADY, GM_EIO = range(-1, -10, -1)
 STR = 30
 
 
@@ -91,12 +94,12 @@ class GmStepResult(C.Structure):
 class GmState(C.Structure):
     _fields_ = [("t", C.c_double), ("dt", C.c_double), ("maxDelta", C.c_double),
                 ("timeIndex", C.c_int32), ("nAttempted", C.c_int32), ("nRejected", C.c_int32),
-                ("status", C.c_uint32)]
+                ("status", C.c_uint32), ("dtUsed", C.c_double), ("event", C.c_int32), ("pad", C.c_int32)]
 
 
 class GmReduction(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("B2", "BMax", "JMax", "JxB_B2Max", "residual", "residualPw", "minDetJac",
-                                           "wedgeMin", "convex", "errB_1ez", "errXb_XbAn")]
+                                           "wedgeMin", "convex", "errB_1ez", "errXb_XbAn", "epsilonStar")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -119,6 +122,8 @@ SIGNATURES = {
     "gm_step": (C.c_int, [VP, P(GmStepResult)]),
     "gm_steps_async": (C.c_int, [VP, C.c_int]),
     "gm_run": (C.c_int, [VP, C.c_int, P(GmState)]),
+    "gm_run_events": (C.c_int, [VP, C.c_int, P(GmState)]),
+    "gm_grid_fields": (C.c_int, [VP, VP, VP, VP]),
     "gm_get_state": (C.c_int, [VP, P(GmState)]),
     "gm_set_dt": (C.c_int, [VP, C.c_double, C.c_double, C.c_int]),
     "gm_refresh": (C.c_int, [VP, P(GmReduction)]),
@@ -126,6 +131,14 @@ SIGNATURES = {
     "gm_download_k": (C.c_int, [VP, C.c_int, VP]),
     "gm_download_x": (C.c_int, [VP, C.c_int, VP]),
     "gm_reduce_noalloc": (C.c_int, [P(GmParams), VP, VP, VP, VP, VP]),
+    "gm_device_count": (C.c_int, [P(C.c_int)]),
+    "gm_set_device": (C.c_int, [C.c_int]),
+    "gm_io_write_cuda_info": (C.c_int, [C.c_char_p, C.c_int, C.c_long]),
+    "gm_io_write_b0": (C.c_int, [P(GmParams), C.c_char_p, VP]),
+    "gm_io_write_dump": (C.c_int, [P(GmParams), C.c_char_p, C.c_double, C.c_double, VP, VP, VP, VP, VP, VP, VP]),
+    "gm_io_read_state": (C.c_int, [P(GmParams), C.c_char_p, C.c_char_p, VP, VP, P(C.c_double), P(C.c_double)]),
+    "gm_io_ts_line": (C.c_int, [P(GmParams), P(GmReduction), C.c_double, C.c_double, C.c_double, C.c_int,
+                                C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int]),
     "gm_launch_count": (C.c_int64, [VP]),
     "gm_last_error": (C.c_char_p, []),
     "gm_version": (C.c_char_p, []),

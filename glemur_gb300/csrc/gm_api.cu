@@ -75,6 +75,8 @@ struct ImplBase {
     virtual int control() = 0;
     virtual int steps_async(int n) = 0;
     virtual int run(int nCycle, gm_state* out) = 0;
+    virtual int run_events(int nCycle, gm_state* out) = 0;
+    virtual int grid_fields(void* cellVol, void* convexity, void* wedgeMin) = 0;
     virtual int get_state(gm_state* out) = 0;
     virtual int set_dt(double t, double dt, int timeIndex) = 0;
     virtual int refresh(gm_reduction* r) = 0;
@@ -103,6 +105,7 @@ struct Impl : ImplBase {
     T* outD = nullptr;
     T* stage_buf = nullptr;     // ghosted AoS staging for transfers
     T* eps = nullptr;           // ex | ey | ez
+    T* eps_col = nullptr;       // eps* scratch: J.B/B^2 and z of the central column
     DevState* st = nullptr;
     double* log = nullptr;
     double* part = nullptr;
@@ -128,7 +131,7 @@ struct Impl : ImplBase {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
         void* ptrs[] = {X[0], X[1], XS[0], XS[1], K[0], K[1], K[2], K[3], K[4], B0, B0s, outB, outJ,
-                        outD, stage_buf, eps, st, log, part, red};
+                        outD, stage_buf, eps, eps_col, st, log, part, red};
         for (void* q : ptrs)
             if (q) cudaFree(q);
         if (h_st) cudaFreeHost(h_st);
@@ -173,6 +176,9 @@ struct Impl : ImplBase {
         kp.dtMin = (double)(T)p->dtMin;
         kp.ar = p->ar; kp.az = p->az; kp.phi1 = p->phi1;
         kp.wantXbAn = p->redErrXb_XbAn != 0;
+        kp.nTs = p->nTs;
+        kp.dtDump = (T)p->dtDump;
+        kp.dtSave = (T)p->dtSave;
         // Cash-Karp tableau, src/rungeKutta.cu:10-25
         static const double bd[7][6] = {
             {0, 0, 0, 0, 0, 0},
@@ -210,11 +216,12 @@ struct Impl : ImplBase {
         if ((rc = alloc((void**)&outD, NG * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&stage_buf, 3 * NG * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&eps, (size_t)(nx + ny + nz) * sizeof(T)))) return rc;
+        if ((rc = alloc((void**)&eps_col, (size_t)2 * nz * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&st, sizeof(DevState)))) return rc;
         logCap = 1 << 16;
         if ((rc = alloc((void**)&log, (size_t)3 * logCap * sizeof(double)))) return rc;
         CUDA_TRY(cudaMallocHost((void**)&h_st, sizeof(DevState)));
-        CUDA_TRY(cudaMallocHost((void**)&h_red, gmk::R_COUNT * sizeof(double)));
+        CUDA_TRY(cudaMallocHost((void**)&h_red, (gmk::R_COUNT + 1) * sizeof(double)));
         // epsilon profile factors, src/rungeKutta.cu:180-185 (evaluated in double)
         {
             std::vector<T> e((size_t)nx + ny + nz);
@@ -265,7 +272,7 @@ struct Impl : ImplBase {
             if ((rc = init_tma(nsm))) return rc;
         }
         if ((rc = alloc((void**)&part, (size_t)nparts * gmk::R_COUNT * sizeof(double)))) return rc;
-        if ((rc = alloc((void**)&red, gmk::R_COUNT * sizeof(double)))) return rc;
+        if ((rc = alloc((void**)&red, (gmk::R_COUNT + 1) * sizeof(double)))) return rc;   // + eps*
         CUDA_TRY(cudaStreamSynchronize(stream));
         return GM_OK;
     }
@@ -353,6 +360,7 @@ struct Impl : ImplBase {
         CUDA_TRY(cudaMemcpyAsync(st, h_st, sizeof s, cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         uploaded = true;
+        ev_base = -1;
         return GM_OK;
     }
 
@@ -430,6 +438,9 @@ struct Impl : ImplBase {
         o->nAttempted = h_st->nAttempted;
         o->nRejected = h_st->nRejected;
         o->status = h_st->status;
+        o->dtUsed = h_st->dtUsed;
+        o->event = h_st->event;
+        o->pad = 0;
     }
 
     int get_state(gm_state* out) override {
@@ -439,10 +450,12 @@ struct Impl : ImplBase {
         return GM_OK;
     }
 
-    int set_control(int target, bool reset_done) {
+    int set_control(int target, bool reset_done, bool events = false) {
         int rc = read_state();
         if (rc) return rc;
         h_st->target = target;
+        h_st->eventsOn = events ? 1 : 0;
+        h_st->status &= ~(unsigned)GM_ST_EVENT;
         if (reset_done) {
             const bool dtmin = !(h_st->dt > kp.dtMin);
             h_st->done = dtmin || (h_st->status & (GM_ST_NAN | GM_ST_TIMEOUT | GM_ST_ALIGN)) || h_st->timeIndex >= target;
@@ -462,6 +475,7 @@ struct Impl : ImplBase {
         h_st->dt = gp.errMode == 0 ? (double)(T)dt : dt;
         h_st->timeIndex = timeIndex;
         h_st->done = !(h_st->dt > kp.dtMin);
+        ev_base = -1;
         CUDA_TRY(cudaMemcpyAsync(st, h_st, sizeof(DevState), cudaMemcpyHostToDevice, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         return GM_OK;
@@ -488,14 +502,61 @@ struct Impl : ImplBase {
         return GM_OK;
     }
 
+    // As run, with a stop after every accepted step whose output is due; the
+    // step count is measured from the first call after upload / set_dt.
+    int ev_base = -1;
+    int run_events(int nCycle, gm_state* out) override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_run_events before gm_upload");
+        if (nCycle < 0) return gm::fail(GM_EPARAM, "gm_run_events: nCycle < 0");
+        int rc = read_state();
+        if (rc) return rc;
+        if (ev_base < 0) ev_base = h_st->timeIndex;
+        const long long tgt = (long long)ev_base + nCycle;
+        if ((rc = set_control(tgt > INT_MAX ? INT_MAX : (int)tgt, true, true))) return rc;
+        int chunk = 1;
+        while (!h_st->done) {
+            if ((rc = steps_async(chunk))) return rc;
+            if ((rc = read_state())) return rc;
+            if (chunk < 64) chunk *= 2;
+        }
+        if (out) {
+            fill(out);
+            if (!(h_st->status & GM_ST_EVENT)) out->event = 0;
+        }
+        if (h_st->status & GM_ST_NAN) return gm::fail(GM_ENAN, "NaN/Inf in a stage increment");
+        if (h_st->status & (GM_ST_TIMEOUT | GM_ST_ALIGN))
+            return gm::fail(GM_ETIMEOUT, "a stage kernel stopped: bounded wait or alignment check (status " +
+                                             std::to_string(h_st->status) + ")");
+        return GM_OK;
+    }
+
+    int grid_fields(void* cellVol, void* convexity, void* wedgeMin) override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_grid_fields before gm_upload");
+        int rc = read_state();
+        if (rc) return rc;
+        T* cv = stage_buf;
+        T* cx = stage_buf + N;
+        T* wm = stage_buf + 2 * N;
+        CUDA_TRY(gmk::launch_grid_fields<T>(kp, X[h_st->cur], cv, cx, wm, stream));
+        launches++;
+        if (cellVol) CUDA_TRY(cudaMemcpyAsync(cellVol, cv, N * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        if (convexity) CUDA_TRY(cudaMemcpyAsync(convexity, cx, N * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        if (wedgeMin) CUDA_TRY(cudaMemcpyAsync(wedgeMin, wm, N * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
     int refresh(gm_reduction* r) override {
         if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_refresh before gm_upload");
+        int rc = read_state();
+        if (rc) return rc;
         StageArgs<T> a = args(0);
         CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_DIAG, gp.pressure, grid, block, smem_diag, stream));
         CUDA_TRY(gmk::launch_finalize<T>(part, nparts, red, stream));
         CUDA_TRY(gmk::launch_export_ghosts<T>(kp, outB, outD, stream));
-        launches += 2 + kp.xPeri + kp.yPeri + kp.zPeri;
-        CUDA_TRY(cudaMemcpyAsync(h_red, red, gmk::R_COUNT * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(gmk::launch_eps_star<T>(kp, outB, outJ, X[h_st->cur], eps_col, red + gmk::R_COUNT, stream));
+        launches += 3 + kp.xPeri + kp.yPeri + kp.zPeri;
+        CUDA_TRY(cudaMemcpyAsync(h_red, red, (gmk::R_COUNT + 1) * sizeof(double), cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         if (r) {
             const double* v = h_red;
@@ -510,6 +571,7 @@ struct Impl : ImplBase {
             r->convex = v[gmk::R_MIN_CONVEX];
             r->errB_1ez = sqrt(v[gmk::R_SUM_E1]) / sqrt((double)N);
             r->errXb_XbAn = sqrt(v[gmk::R_SUM_E2]) / sqrt((double)N);
+            r->epsilonStar = v[gmk::R_COUNT];
         }
         return GM_OK;
     }
@@ -643,6 +705,16 @@ int gm_steps_async(gm_handle* h, int nSteps) {
 int gm_run(gm_handle* h, int nCycle, gm_state* out) {
     if (!h) return gm::fail(GM_EPARAM, "null handle");
     return h->impl->run(nCycle, out);
+}
+
+int gm_run_events(gm_handle* h, int nCycle, gm_state* out) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->run_events(nCycle, out);
+}
+
+int gm_grid_fields(gm_handle* h, void* cellVol, void* convexity, void* wedgeMin) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->grid_fields(cellVol, convexity, wedgeMin);
 }
 
 int gm_get_state(gm_handle* h, gm_state* out) {

@@ -46,6 +46,9 @@ struct DevState {
     int done;
     int logCap;
     int lastAccepted;                  // outcome of the last attempted step
+    double dtUsed;                     // step size of the last attempted step
+    int event;                         // GM_EV_* bits of the last accepted step
+    int eventsOn;                      // stop (done) after an accepted step with output due
 };
 
 // Kernel-side run parameters (passed by value; REAL = T).
@@ -68,6 +71,8 @@ struct KP {
     T inv8dxdydz;            // 1 / (8 dx dy dz): det(a, b, c) -> Delta
     double ar, az, phi1;     // analytic-field parameters (distance-to-analytic diagnostic)
     int wantXbAn;
+    int nTs;                 // output cadences (main.cu:355-377)
+    T dtDump, dtSave;
     const T* ex;             // epsilon profile factors per axis (rungeKutta.cu:180-185)
     const T* ey;
     const T* ez;
@@ -129,6 +134,14 @@ template <typename T>
 cudaError_t launch_pack_k(const KP<T>& p, const T* k, T* aos, cudaStream_t s);
 template <typename T>
 cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t s);
+// grid-quality fields (inner layout) of a padded grid
+template <typename T>
+cudaError_t launch_grid_fields(const KP<T>& p, const T* X, T* cellVol, T* convexity, T* wedgeMin, cudaStream_t s);
+// eps* of the central column from the exported B (ghosted AoS), J (inner AoS)
+// and the padded grid, into *out; scratch holds 2 nz REALs
+template <typename T>
+cudaError_t launch_eps_star(const KP<T>& p, const T* B, const T* J, const T* X, T* scratch, double* out,
+                            cudaStream_t s);
 
 // TMA-fed stage kernel (gm_stage_tma.cuh): 32 x 8 tiles, position planes
 // streamed by cp.async.bulk.tensor.  tm[] are the tensor maps of X[0], X[1],

@@ -597,6 +597,7 @@ __global__ void k_control(const __grid_constant__ KP<T> p, DevState* st, double*
     st->maxDelta = md;
     const int att = st->nAttempted++;
     const bool acc = md < p.maxError;
+    const double dtOld = st->dt;
     st->lastAccepted = acc ? 1 : 0;
     if (acc) {
         st->t = p.refDt ? (double)((T)st->t + (T)st->dt) : st->t + st->dt;
@@ -610,6 +611,20 @@ __global__ void k_control(const __grid_constant__ KP<T> p, DevState* st, double*
         const double nd = st->dt * pow(0.9 * p.maxError / md, ex);
         st->dt = p.refDt ? (double)(T)nd : nd;
     }
+    st->dtUsed = dtOld;
+    // output due after this step (main.cu:355-377): the time-series cadence
+    // uses the loop index of the step, the dump triggers t and the adapted dt
+    // in REAL, the last step is the one that reaches the target
+    int ev = 0;
+    if (acc) {
+        const int ti = st->timeIndex - 1;
+        if (p.nTs > 0 && ti % p.nTs == 0) ev |= GM_EV_TS;
+        const T tt = (T)st->t, dd = (T)st->dt;
+        if (ceil((T)(tt - dd) / p.dtDump) != ceil(tt / p.dtDump)) ev |= GM_EV_DUMP;
+        if (ceil((T)(tt - dd) / p.dtSave) != ceil(tt / p.dtSave)) ev |= GM_EV_SAVE;
+        if (st->timeIndex >= st->target) ev |= GM_EV_LAST;
+    }
+    st->event = ev;
     if (log && att < st->logCap) {
         log[3 * att] = md;
         log[3 * att + 1] = st->dt;
@@ -621,6 +636,10 @@ __global__ void k_control(const __grid_constant__ KP<T> p, DevState* st, double*
         st->done = 1;
     }
     if (st->timeIndex >= st->target) st->done = 1;
+    if (st->eventsOn && ev) {
+        st->done = 1;
+        st->status |= GM_ST_EVENT;
+    }
     if (st->done) st->status |= GM_ST_DONE;
 }
 
@@ -756,6 +775,93 @@ __global__ void k_export_peri(const KP<T> p, T* __restrict__ B, T* __restrict__ 
     }
 }
 
+// Grid-quality fields at the inner points of a padded grid, inner layout:
+// the signed volume of the cell towards +x,+y,+z (dirCellVol,
+// maths.cu:441-490), the convexity flag and the minimum of the 8 corner
+// wedge products with the sign convention of gridConvexity / gridWedgeMin
+// (maths.cu:494-643).
+template <typename T>
+__global__ void k_grid_fields(const KP<T> p, const T* __restrict__ X, T* __restrict__ cellVol,
+                              T* __restrict__ convexity, T* __restrict__ wedgeMin) {
+    const long long cs = p.cs;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < p.N; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % p.nx), j = (int)((q / p.nx) % p.ny), k = (int)(q / ((long long)p.nx * p.ny));
+        auto at = [&](int ii, int jj, int kk, int l) {
+            return X[l * cs + (ii + 2) + (long long)p.px * ((jj + 2) + (long long)p.py * (kk + 2))];
+        };
+        T xc[3];
+        for (int l = 0; l < 3; l++) xc[l] = at(i, j, k, l);
+        if (cellVol) {
+            T d1[3], d2[3], d3[3], cc[3];
+            for (int l = 0; l < 3; l++) {
+                d1[l] = at(i + 1, j, k, l) - xc[l];
+                d2[l] = at(i, j + 1, k, l) - xc[l];
+                d3[l] = at(i, j, k + 1, l) - xc[l];
+            }
+            cross3(d1, d2, cc);
+            cellVol[q] = cc[0] * d3[0] + cc[1] * d3[1] + cc[2] * d3[2];
+        }
+        T wmin = 0, conv = 1;
+        for (int u = 0; u < 2; u++)
+            for (int v = 0; v < 2; v++)
+                for (int w = 0; w < 2; w++) {
+                    T d1[3], d2[3], d3[3], cc[3];
+                    for (int l = 0; l < 3; l++) {
+                        d1[l] = at(i + 2 * u - 1, j, k, l) - xc[l];
+                        d2[l] = at(i, j + 2 * v - 1, k, l) - xc[l];
+                        d3[l] = at(i, j, k + 2 * w - 1, l) - xc[l];
+                    }
+                    cross3(d1, d2, cc);
+                    T wc = cc[0] * d3[0] + cc[1] * d3[1] + cc[2] * d3[2];
+                    const int s = 2 * (u + v + w);
+                    if ((wc < 0) && (s == 2 || s == 6)) conv = -1;
+                    if ((wc > 0) && (s == 0 || s == 4)) conv = -1;
+                    if (s == 0) wmin = -wc;
+                    if (s == 0 || s == 4) wc = -wc;
+                    if (wc < wmin) wmin = wc;
+                }
+        if (convexity) convexity[q] = conv;
+        if (wedgeMin) wedgeMin[q] = wmin;
+    }
+}
+
+// eps* (maths.cu:203-290 with diagnostics.cu:32-47): along the central column
+// i = nx/2, j = ny/2, a_k = J.B/B^2 and z_k = x_z; eps* is the largest
+// sqrt(2) |(a_n - a_p)/(z_n - z_p)| over the pairs with z_n != z_p, in REAL;
+// NaN values never win (maths.cu:144-153).  One CTA.
+template <typename T>
+__global__ void k_eps_star(const KP<T> p, const T* __restrict__ B, const T* __restrict__ J, const T* __restrict__ X,
+                           T* __restrict__ sc, double* __restrict__ out) {
+    const int i = p.nx / 2, j = p.ny / 2, nz = p.nz;
+    T* a = sc;
+    T* z = sc + nz;
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        const long long g = (long long)(i + 1) + (long long)(p.nx + 2) * ((j + 1) + (long long)(p.ny + 2) * (k + 1));
+        const long long l = (long long)i + (long long)p.nx * (j + (long long)p.ny * k);
+        const T b0 = B[3 * g], b1 = B[3 * g + 1], b2 = B[3 * g + 2];
+        const T j0 = J[3 * l], j1 = J[3 * l + 1], j2 = J[3 * l + 2];
+        a[k] = (j0 * b0 + j1 * b1 + j2 * b2) / (b0 * b0 + b1 * b1 + b2 * b2);
+        z[k] = X[2 * p.cs + (i + 2) + (long long)p.px * ((j + 2) + (long long)p.py * (k + 2))];
+    }
+    __syncthreads();
+    T m = 0;    // every value is >= 0, and the pairs n == p give 0
+    for (int q = threadIdx.x; q < nz * nz; q += blockDim.x) {
+        const int pp = q / nz, n = q % nz;
+        if (z[n] != z[pp]) {
+            const T v = (T)(1.414213562373095 * (double)fabs((a[n] - a[pp]) / (z[n] - z[pp])));
+            if (v > m) m = v;
+        }
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = (double)m;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
 // ---- host launchers ---------------------------------------------------------
 
 template <typename T>
@@ -866,6 +972,19 @@ cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t 
     return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_grid_fields(const KP<T>& p, const T* X, T* cellVol, T* convexity, T* wedgeMin, cudaStream_t s) {
+    k_grid_fields<T><<<nblk(p.N), 256, 0, s>>>(p, X, cellVol, convexity, wedgeMin);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_eps_star(const KP<T>& p, const T* B, const T* J, const T* X, T* scratch, double* out,
+                            cudaStream_t s) {
+    k_eps_star<T><<<1, 256, 0, s>>>(p, B, J, X, scratch, out);
+    return cudaGetLastError();
+}
+
 #define GMK_INSTANTIATE(T)                                                                                        \
     template cudaError_t launch_stage<T>(const StageArgs<T>&, int, int, dim3, dim3, size_t, cudaStream_t);       \
     template size_t stage_smem_bytes<T>(int, int, int);                                                           \
@@ -878,6 +997,8 @@ cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t 
     template cudaError_t launch_images<T>(const KP<T>&, T*, cudaStream_t);                                        \
     template cudaError_t launch_scale_b0<T>(const KP<T>&, const T*, T*, cudaStream_t);                            \
     template cudaError_t launch_pack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \
-    template cudaError_t launch_export_ghosts<T>(const KP<T>&, T*, T*, cudaStream_t);
+    template cudaError_t launch_export_ghosts<T>(const KP<T>&, T*, T*, cudaStream_t);                            \
+    template cudaError_t launch_grid_fields<T>(const KP<T>&, const T*, T*, T*, T*, cudaStream_t);                 \
+    template cudaError_t launch_eps_star<T>(const KP<T>&, const T*, const T*, const T*, T*, double*, cudaStream_t);
 
 }  // namespace gmk

@@ -90,6 +90,21 @@ class Relaxation:
         return dict(t=s.t, dt=s.dt, maxDelta=s.maxDelta, timeIndex=s.timeIndex, nAttempted=s.nAttempted,
                     nRejected=s.nRejected, status=s.status)
 
+    def run_events(self, nCycle: int) -> dict:
+        """gm_run_events: run until nCycle accepted steps, stopping after each
+        step whose output is due; 'event' holds the GM_EV_* bits."""
+        s = GmState()
+        check(self.lib.gm_run_events(self.h, nCycle, C.byref(s)), "gm_run_events")
+        return dict(t=s.t, dt=s.dt, maxDelta=s.maxDelta, timeIndex=s.timeIndex, nAttempted=s.nAttempted,
+                    nRejected=s.nRejected, status=s.status, dtUsed=s.dtUsed, event=s.event)
+
+    def grid_fields(self) -> dict:
+        """Cell volume, convexity and minimum wedge product per inner point."""
+        out = {k: np.empty(self.I, self.dtype) for k in ("cellVol", "convexity", "wedgeMin")}
+        check(self.lib.gm_grid_fields(self.h, ptr(out["cellVol"]), ptr(out["convexity"]), ptr(out["wedgeMin"])),
+              "gm_grid_fields")
+        return out
+
     def refresh(self) -> dict:
         r = GmReduction()
         check(self.lib.gm_refresh(self.h, C.byref(r)), "gm_refresh")

@@ -54,6 +54,14 @@ extern "C" {
 #define GM_ST_DONE       8u
 #define GM_ST_TIMEOUT   16u   /* a bounded wait on an asynchronous copy ran out */
 #define GM_ST_ALIGN     32u   /* a copy was skipped: its shared-memory or tensor-map alignment check failed */
+#define GM_ST_EVENT     64u   /* gm_run_events stopped after an accepted step with output due */
+
+/* Output events of an accepted step (gm_state.event), the triggers of
+ * src/main.cu:355-377 evaluated on the device after the dt update. */
+#define GM_EV_TS         1    /* timeIndex % nTs == 0: reductions + time-series row */
+#define GM_EV_DUMP       2    /* ceil((t-dt)/dtDump) != ceil(t/dtDump): data/dump<n>.vtk */
+#define GM_EV_SAVE       4    /* ceil((t-dt)/dtSave) != ceil(t/dtSave): data/save.vtk */
+#define GM_EV_LAST       8    /* last accepted step of the run (timeIndex == nCycle-1): data/save.vtk */
 
 /*
  * Run parameters.  Mirrors struct Parameters (src/global.h:44-108) field by
@@ -109,7 +117,8 @@ typedef struct gm_params {
     int32_t precision;   /* 32: float storage, 64: double storage (PRECISION, src/Makefile:11) */
     int32_t errMode;     /* 0: error norm |x_new - x*| in REAL as the reference
                             (src/rungeKutta.cu:326-333); 1: |sum (c_i - c*_i) k_i|
-                            accumulated in double (no cancellation against x)  */
+                            (no cancellation against x), with t and dt kept in
+                            double by the controller                           */
     double  p0Amp;       /* pressure profile p0(X) = beta*(1 + p0Amp*exp(-r^2/p0Width^2));
                             p0Amp = 0 gives the reference's uniform p0 = beta  */
     double  p0Width;
@@ -137,6 +146,10 @@ typedef struct gm_state {
     int32_t nAttempted;  /* attempted steps so far                              */
     int32_t nRejected;
     uint32_t status;
+    double  dtUsed;      /* step size of the last attempted step (the dt that
+                            writeTs prints, main.cu:357)                        */
+    int32_t event;       /* GM_EV_* bits of the step gm_run_events stopped at   */
+    int32_t pad;
 } gm_state;
 
 /*
@@ -158,6 +171,8 @@ typedef struct gm_reduction {
     double convex;       /* 1 if every inner point is convex, -1 otherwise (maths.cu:573-643) */
     double errB_1ez;     /* rms |B - e_z| (maths.cu:294-328)                    */
     double errXb_XbAn;   /* rms |x - x_analytic| (maths.cu:332-377)             */
+    double epsilonStar;  /* force-free parameter eps* along the central column
+                            (maths.cu:203-290, diagnostics.cu:32-47)            */
 } gm_reduction;
 
 typedef struct gm_handle gm_handle;
@@ -219,6 +234,14 @@ int gm_steps_async(gm_handle* h, int nSteps);
  * dt <= dtMin, as the loop of src/main.cu:259-384 (without its file output). */
 int gm_run(gm_handle* h, int nCycle, gm_state* out);
 
+/* As gm_run, but also stop after every accepted step whose output is due
+ * (the nTs, dtDump, dtSave and last-step triggers of src/main.cu:355-377,
+ * from the handle's parameters); out->event then holds the GM_EV_* bits,
+ * out->dtUsed the step size of that step and out->dt the adapted one.  Call
+ * again to continue; nCycle counts from the handle's timeIndex of the first
+ * call after gm_upload or gm_set_dt. */
+int gm_run_events(gm_handle* h, int nCycle, gm_state* out);
+
 /* Read the device controller state (synchronises the handle's stream). */
 int gm_get_state(gm_handle* h, gm_state* out);
 int gm_set_dt(gm_handle* h, double t, double dt, int timeIndex);
@@ -233,6 +256,12 @@ int gm_refresh(gm_handle* h, gm_reduction* r);
  * (src/diagnostics.cu:138-152).  B, J and detJac are those of the last
  * gm_refresh. */
 int gm_download(gm_handle* h, void* xb, void* B, void* J, void* detJac);
+
+/* Grid-quality fields at the current grid, inner layout i + nx*(j + ny*k)
+ * (any may be NULL): the signed cell volume (dirCellVol, maths.cu:441-490),
+ * the convexity flag +-1 (gridConvexity, maths.cu:573-643) and the minimum of
+ * the 8 corner wedge products (gridWedgeMin, maths.cu:494-569). */
+int gm_grid_fields(gm_handle* h, void* cellVol, void* convexity, void* wedgeMin);
 
 /* Stage increments k_0..k_4 of the last step (inner AoS, 3*nx*ny*nz each, in
  * the reference kk layout src/rungeKutta.cu:236) -- for stage parity tests. */
@@ -271,6 +300,41 @@ int gm_download_x(gm_handle* h, int which, void* xb);
  * allocating library routine is called. */
 int gm_reduce_noalloc(const gm_params* p, const void* B, const void* J, const void* detJac,
                       gm_reduction* out, void* stream);
+
+/* Number of CUDA devices and selection of the device the calling thread
+ * uses (the cudaGetDeviceCount / cudaSetDevice of src/main.cu:47-80). */
+int gm_device_count(int* n);
+int gm_set_device(int dev);
+
+/* ---- run-directory files (src/io.cu), host only ------------------------- */
+/* Arrays are REAL of p->precision in the reference layouts above; files are
+ * legacy VTK with big-endian binary payloads, byte for byte as io.cu writes
+ * them.  All return GM_OK or GM_EIO. */
+
+/* cuda.info (io.cu:10-82) for the devices of this machine. */
+int gm_io_write_cuda_info(const char* path, int precision, long activeDevice);
+/* data/B0.vtk: STRUCTURED_POINTS, ghosts included (io.cu:167-205). */
+int gm_io_write_b0(const gm_params* p, const char* path, const void* B0);
+/* data/dump<n>.vtk or data/save.vtk: STRUCTURED_GRID with the 9 parameter
+ * fields, POINTS xb, VECTORS bfield and, as p->dump* select, VECTORS jfield
+ * (zero ghosts), SCALARS detJac / cellVol / convexity / wedgeMin
+ * (io.cu:209-386, 503-538).  J, cellVol, convexity, wedgeMin are inner
+ * layout; the others ghosted. */
+int gm_io_write_dump(const gm_params* p, const char* path, double t, double dt, const void* xb, const void* B,
+                     const void* J, const void* detJac, const void* cellVol, const void* convexity,
+                     const void* wedgeMin);
+/* Restart: t, dt and xb from a save file, B0 from a B0 file (io.cu:390-499).
+ * Grid sizes come from p, as in the reference, which passes its parameters to
+ * readState by value. */
+int gm_io_read_state(const gm_params* p, const char* save_path, const char* b0_path, void* xb, void* B0,
+                     double* t, double* dt);
+/* One time-series line (io.cu:542-678) into buf: the header line when
+ * header != 0 (toFile != 0 labels the error column "maxDelta" as the file
+ * does, else "maxError" as stdout does), else the row for (it, t, dt,
+ * maxDelta) with the reductions p->red* select; B2f = B2 - B2res.  Returns
+ * the length written, or GM_EPARAM when buf is too small. */
+int gm_io_ts_line(const gm_params* p, const gm_reduction* r, double B2res, double t, double dt, int it,
+                  double maxDelta, int header, int toFile, char* buf, int bufSize);
 
 /* Cumulative kernel launches issued by this handle (for accounting). */
 int64_t gm_launch_count(const gm_handle* h);
