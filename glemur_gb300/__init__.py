@@ -9,6 +9,7 @@ path) behind the C-ABI of include/glemur.h.
 """
 from ._abi import GlemurError, GmParams, load  # noqa: F401
 from .relax import Relaxation  # noqa: F401
+from .batch import BatchRelaxation  # noqa: F401
 from . import configs  # noqa: F401
 
-__all__ = ["Relaxation", "GmParams", "GlemurError", "configs", "load"]
+__all__ = ["Relaxation", "BatchRelaxation", "GmParams", "GlemurError", "configs", "load"]

@@ -105,6 +105,14 @@ class GmReduction(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class GmBatchCase(C.Structure):
+    _fields_ = [("seconds", C.c_double), ("residual", C.c_double), ("t", C.c_double), ("dt", C.c_double),
+                ("attempted", C.c_int32), ("accepted", C.c_int32), ("status", C.c_uint32), ("converged", C.c_int32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 # name -> (restype, argtypes) of every entry point declared in include/glemur.h
 P = C.POINTER
 VP = C.c_void_p
@@ -131,6 +139,16 @@ SIGNATURES = {
     "gm_download_k": (C.c_int, [VP, C.c_int, VP]),
     "gm_download_x": (C.c_int, [VP, C.c_int, VP]),
     "gm_reduce_noalloc": (C.c_int, [P(GmParams), VP, VP, VP, VP, VP]),
+    "gm_batch_create": (C.c_int, [P(GmParams), C.c_int, P(VP)]),
+    "gm_batch_destroy": (C.c_int, [VP]),
+    "gm_batch_upload": (C.c_int, [VP, C.c_int, VP, VP, C.c_double, C.c_double]),
+    "gm_batch_steps_async": (C.c_int, [VP, C.c_int]),
+    "gm_batch_get_state": (C.c_int, [VP, C.c_int, P(GmState)]),
+    "gm_batch_refresh": (C.c_int, [VP, C.c_int, P(GmReduction)]),
+    "gm_batch_download": (C.c_int, [VP, C.c_int, VP, VP, VP, VP]),
+    "gm_batch_stop": (C.c_int, [VP, C.c_int]),
+    "gm_batch_run": (C.c_int, [VP, C.c_int, C.c_double, C.c_int, C.c_int, P(GmBatchCase)]),
+    "gm_batch_launch_count": (C.c_int64, [VP]),
     "gm_device_count": (C.c_int, [P(C.c_int)]),
     "gm_set_device": (C.c_int, [C.c_int]),
     "gm_io_write_cuda_info": (C.c_int, [C.c_char_p, C.c_int, C.c_long]),

@@ -10,6 +10,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -25,6 +27,7 @@
 using gmk::DevState;
 using gmk::KP;
 using gmk::StageArgs;
+using gmk::StageArgsTMA;
 
 namespace {
 
@@ -631,11 +634,224 @@ struct Impl : ImplBase {
     }
 };
 
+// ---- many cases in one launch per stage ------------------------------------
+struct BatchBase {
+    virtual ~BatchBase() {}
+    virtual int upload(int c, const void* xb, const void* B0, double t, double dt) = 0;
+    virtual int steps_async(int n) = 0;
+    virtual int get_state(int c, gm_state* out) = 0;
+    virtual int refresh(int c, gm_reduction* r) = 0;
+    virtual int download(int c, void* xb, void* B, void* J, void* D) = 0;
+    virtual int stop(int c) = 0;
+    virtual int run(int nCycle, double residual, int pointwise, int checkEvery, gm_batch_case* out) = 0;
+    int ncases = 0;
+    int64_t launches = 0;
+};
+
+template <typename T>
+struct Batch : BatchBase {
+    static constexpr int TZB = 32;          // planes per work item
+    std::vector<std::unique_ptr<Impl<T>>> cs;
+    cudaStream_t stream = nullptr;
+    StageArgsTMA<T>* d_cases = nullptr;
+    int4* d_work = nullptr;
+    int* d_counters = nullptr;
+    int nwork = 0, nblocks = 0, pressure = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+
+    ~Batch() override {
+        if (stream) cudaStreamSynchronize(stream);
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        if (d_cases) cudaFree(d_cases);
+        if (d_work) cudaFree(d_work);
+        if (d_counters) cudaFree(d_counters);
+        cs.clear();
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int init(const gm_params* ps, int n) {
+        ncases = n;
+        pressure = ps[0].pressure != 0;
+        for (int c = 0; c < n; c++)
+            if ((ps[c].pressure != 0) != (pressure != 0) || ps[c].precision != ps[0].precision)
+                return gm::fail(GM_EPARAM, "gm_batch_create: all cases need the same precision and pressure flag");
+        CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        std::vector<StageArgsTMA<T>> h(n);
+        std::vector<std::pair<long long, int>> order;
+        for (int c = 0; c < n; c++) {
+            gm_params p = ps[c];
+            p.stageKernel = 0;
+            int rc = check_params(&p);
+            if (rc) return rc;
+            cs.emplace_back(new Impl<T>());
+            if ((rc = cs.back()->init(&p))) return rc;
+            cs.back()->stream = stream;
+            memcpy(h[c].tm, cs.back()->tmaps, sizeof h[c].tm);
+            h[c].a = cs.back()->args(0);
+            h[c].a.TZ = TZB;
+            order.emplace_back(-(long long)p.nx * p.ny * p.nz, c);
+        }
+        // work items, largest cases first
+        std::sort(order.begin(), order.end());
+        std::vector<int4> work;
+        for (auto& o : order) {
+            const gm_params& p = ps[o.second];
+            const int nbx = (p.nx + gmk::TX - 1) / gmk::TX, nby = (p.ny + gmk::STAGE_TMA_TY - 1) / gmk::STAGE_TMA_TY;
+            const int nbz = (p.nz + TZB - 1) / TZB;
+            for (int bz = 0; bz < nbz; bz++)
+                for (int by = 0; by < nby; by++)
+                    for (int bx = 0; bx < nbx; bx++) work.push_back(make_int4(o.second, bx, by, bz));
+        }
+        nwork = (int)work.size();
+        CUDA_TRY(cudaMalloc((void**)&d_cases, n * sizeof(StageArgsTMA<T>)));
+        CUDA_TRY(cudaMalloc((void**)&d_work, work.size() * sizeof(int4)));
+        CUDA_TRY(cudaMalloc((void**)&d_counters, 8 * sizeof(int)));
+        CUDA_TRY(cudaMemcpyAsync(d_cases, h.data(), n * sizeof(StageArgsTMA<T>), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(d_work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemsetAsync(d_counters, 0, 8 * sizeof(int), stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        int dev = 0, nsm = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        nblocks = nsm * gmk::stage_tma_batch_occupancy<T>(pressure);
+        return GM_OK;
+    }
+
+    bool uploaded_all() const {
+        for (auto& c : cs)
+            if (!c->uploaded) return false;
+        return true;
+    }
+
+    int enqueue_step(cudaStream_t s) {
+        for (int n = 0; n < 6; n++)
+            CUDA_TRY(gmk::launch_stage_tma_batch<T>(d_cases, d_work, nwork, d_counters + n, n, pressure, nblocks, s));
+        CUDA_TRY(gmk::launch_control_batch<T>(d_cases, ncases, d_counters, s));
+        return GM_OK;
+    }
+
+    int upload(int c, const void* xb, const void* B0, double t, double dt) override {
+        if (c < 0 || c >= ncases) return gm::fail(GM_EPARAM, "gm_batch_upload: case index out of range");
+        return cs[c]->upload(xb, B0, t, dt);
+    }
+
+    int steps_async(int nsteps) override {
+        if (!uploaded_all()) return gm::fail(GM_ENOTREADY, "gm_batch_steps_async before every case is uploaded");
+        if (nsteps <= 0) return GM_OK;
+        if (!gexec) {
+            cudaStream_t cap;
+            CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+            int rc = e == cudaSuccess ? enqueue_step(cap) : GM_ECUDA;
+            cudaGraph_t g = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+            cudaStreamDestroy(cap);
+            if (e != cudaSuccess || rc != GM_OK || e2 != cudaSuccess)
+                return gm::fail(GM_ECUDA, "capture of the batch step graph failed");
+            graph = g;
+            CUDA_TRY(cudaGraphInstantiate(&gexec, graph, 0));
+        }
+        for (int q = 0; q < nsteps; q++) {
+            CUDA_TRY(cudaGraphLaunch(gexec, stream));
+            launches += 7;
+        }
+        return GM_OK;
+    }
+
+    int check_case(int c, const char* what) {
+        if (c < 0 || c >= ncases) return gm::fail(GM_EPARAM, std::string(what) + ": case index out of range");
+        return GM_OK;
+    }
+
+    int get_state(int c, gm_state* out) override {
+        int rc = check_case(c, "gm_batch_get_state");
+        return rc ? rc : cs[c]->get_state(out);
+    }
+    int refresh(int c, gm_reduction* r) override {
+        int rc = check_case(c, "gm_batch_refresh");
+        return rc ? rc : cs[c]->refresh(r);
+    }
+    int download(int c, void* xb, void* B, void* J, void* D) override {
+        int rc = check_case(c, "gm_batch_download");
+        return rc ? rc : cs[c]->download(xb, B, J, D);
+    }
+    int stop(int c) override {
+        int rc = check_case(c, "gm_batch_stop");
+        if (rc) return rc;
+        Impl<T>& im = *cs[c];
+        if ((rc = im.read_state())) return rc;
+        im.h_st->done = 1;
+        im.h_st->status |= GM_ST_DONE;
+        CUDA_TRY(cudaMemcpyAsync(im.st, im.h_st, sizeof(DevState), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    int run(int nCycle, double residual, int pointwise, int checkEvery, gm_batch_case* out) override {
+        if (!uploaded_all()) return gm::fail(GM_ENOTREADY, "gm_batch_run before every case is uploaded");
+        if (checkEvery < 1 || nCycle < 0) return gm::fail(GM_EPARAM, "gm_batch_run: checkEvery >= 1, nCycle >= 0");
+        int rc;
+        for (int c = 0; c < ncases; c++) {
+            Impl<T>& im = *cs[c];
+            if ((rc = im.read_state())) return rc;
+            const long long tgt = (long long)im.h_st->timeIndex + nCycle;
+            if ((rc = im.set_control(tgt > INT_MAX ? INT_MAX : (int)tgt, true))) return rc;
+        }
+        std::vector<int> pending;
+        for (int c = 0; c < ncases; c++) pending.push_back(c);
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        const auto t0 = std::chrono::steady_clock::now();
+        auto record = [&](int c, double res, bool conv, double sec) {
+            if (!out) return;
+            gm_state s;
+            cs[c]->fill(&s);
+            out[c].seconds = sec;
+            out[c].residual = res;
+            out[c].t = s.t;
+            out[c].dt = s.dt;
+            out[c].attempted = s.nAttempted;
+            out[c].accepted = s.timeIndex;
+            out[c].status = s.status;
+            out[c].converged = conv ? 1 : 0;
+        };
+        while (!pending.empty()) {
+            if ((rc = steps_async(checkEvery))) return rc;
+            CUDA_TRY(cudaStreamSynchronize(stream));
+            const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            std::vector<int> still;
+            for (int c : pending) {
+                Impl<T>& im = *cs[c];
+                if ((rc = im.read_state())) return rc;
+                const bool done = im.h_st->done != 0;
+                gm_reduction r;
+                if ((rc = im.refresh(&r))) return rc;
+                const double res = pointwise ? r.residualPw : r.residual;
+                const bool conv = res <= residual;
+                if (conv && !done && (rc = stop(c))) return rc;
+                if (conv || done) {
+                    if ((rc = im.read_state())) return rc;
+                    record(c, res, conv, sec);
+                } else {
+                    still.push_back(c);
+                }
+            }
+            pending.swap(still);
+        }
+        return GM_OK;
+    }
+};
+
 }  // namespace
 
 struct gm_handle {
     std::unique_ptr<ImplBase> impl;
     int precision;
+};
+
+struct gm_batch {
+    std::unique_ptr<BatchBase> impl;
 };
 
 extern "C" {
@@ -748,5 +964,70 @@ int gm_download_x(gm_handle* h, int which, void* xb) {
 }
 
 int64_t gm_launch_count(const gm_handle* h) { return h ? h->impl->launches : 0; }
+
+int gm_batch_create(const gm_params* cases, int nCases, gm_batch** out) {
+    if (!out || !cases || nCases < 1) return gm::fail(GM_EPARAM, "gm_batch_create: need cases and an output");
+    *out = nullptr;
+    gm_batch* b = new gm_batch();
+    int rc;
+    if (cases[0].precision == 32) {
+        auto* im = new Batch<float>();
+        b->impl.reset(im);
+        rc = im->init(cases, nCases);
+    } else {
+        auto* im = new Batch<double>();
+        b->impl.reset(im);
+        rc = im->init(cases, nCases);
+    }
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return GM_OK;
+}
+
+int gm_batch_destroy(gm_batch* b) {
+    delete b;
+    return GM_OK;
+}
+
+int gm_batch_upload(gm_batch* b, int c, const void* xb, const void* B0, double t, double dt) {
+    if (!b) return gm::fail(GM_EPARAM, "null batch");
+    return b->impl->upload(c, xb, B0, t, dt);
+}
+
+int gm_batch_steps_async(gm_batch* b, int nSteps) {
+    if (!b) return gm::fail(GM_EPARAM, "null batch");
+    return b->impl->steps_async(nSteps);
+}
+
+int gm_batch_get_state(gm_batch* b, int c, gm_state* out) {
+    if (!b) return gm::fail(GM_EPARAM, "null batch");
+    return b->impl->get_state(c, out);
+}
+
+int gm_batch_refresh(gm_batch* b, int c, gm_reduction* r) {
+    if (!b) return gm::fail(GM_EPARAM, "null batch");
+    return b->impl->refresh(c, r);
+}
+
+int gm_batch_download(gm_batch* b, int c, void* xb, void* B, void* J, void* detJac) {
+    if (!b) return gm::fail(GM_EPARAM, "null batch");
+    return b->impl->download(c, xb, B, J, detJac);
+}
+
+int gm_batch_stop(gm_batch* b, int c) {
+    if (!b) return gm::fail(GM_EPARAM, "null batch");
+    return b->impl->stop(c);
+}
+
+int gm_batch_run(gm_batch* b, int nCycle, double residual, int pointwise, int checkEvery, gm_batch_case* out) {
+    if (!b) return gm::fail(GM_EPARAM, "null batch");
+    return b->impl->run(nCycle, residual, pointwise, checkEvery, out);
+}
+
+int64_t gm_batch_launch_count(const gm_batch* b) { return b ? b->impl->launches : 0; }
+
 
 }  // extern "C"

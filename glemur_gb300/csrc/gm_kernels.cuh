@@ -160,5 +160,16 @@ int stage_tma_occupancy(int pressure);
 template <typename T>
 cudaError_t launch_stage_tma(const StageArgsTMA<T>& A, int pressure, dim3 grid, cudaStream_t s);
 constexpr int STAGE_TMA_TY = 8;
+// Batched stage launch: `work` holds (case, bx, by, bz) items over the
+// device array `cases`; `counter` is this stage's work counter (zero on
+// entry).  `nblocks` CTAs, persistent.
+template <typename T>
+cudaError_t launch_stage_tma_batch(const StageArgsTMA<T>* cases, const int4* work, int nwork, int* counter, int n,
+                                   int pressure, int nblocks, cudaStream_t s);
+template <typename T>
+int stage_tma_batch_occupancy(int pressure);
+// The controllers of all cases of a batch (and the re-arm of the counters).
+template <typename T>
+cudaError_t launch_control_batch(const StageArgsTMA<T>* cases, int ncases, int* counters, cudaStream_t s);
 
 }  // namespace gmk

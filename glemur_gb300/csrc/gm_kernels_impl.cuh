@@ -590,7 +590,7 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
 
 // Accept/reject and the dt rule, src/main.cu:321-383, on the device.
 template <typename T>
-__global__ void k_control(const __grid_constant__ KP<T> p, DevState* st, double* log) {
+__device__ __forceinline__ void control_one(const KP<T>& p, DevState* st, double* log) {
     if (st->done) return;
     const double md = __longlong_as_double((long long)st->maxDeltaBits);
     st->maxDeltaBits = 0ull;
@@ -641,6 +641,20 @@ __global__ void k_control(const __grid_constant__ KP<T> p, DevState* st, double*
         st->status |= GM_ST_EVENT;
     }
     if (st->done) st->status |= GM_ST_DONE;
+}
+
+template <typename T>
+__global__ void k_control(const __grid_constant__ KP<T> p, DevState* st, double* log) {
+    control_one<T>(p, st, log);
+}
+
+// The controllers of a batch of cases, one thread each; also re-arms the six
+// work counters of the batched stage launches for the next step.
+template <typename T>
+__global__ void k_control_batch(const StageArgsTMA<T>* __restrict__ cases, int ncases, int* __restrict__ counters) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < 6) counters[c] = 0;
+    if (c < ncases) control_one<T>(cases[c].a.p, cases[c].a.st, cases[c].a.log);
 }
 
 // Fixed-order reduction of the CTA partials.
@@ -923,6 +937,13 @@ cudaError_t launch_control(const KP<T>& p, DevState* st, double* log, cudaStream
 }
 
 template <typename T>
+cudaError_t launch_control_batch(const StageArgsTMA<T>* cases, int ncases, int* counters, cudaStream_t s) {
+    const int n = ncases > 6 ? ncases : 6;
+    k_control_batch<T><<<(n + 127) / 128, 128, 0, s>>>(cases, ncases, counters);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_finalize(const double* part, int nparts, double* out, cudaStream_t s) {
     k_finalize<T><<<1, 256, 0, s>>>(part, nparts, out);
     return cudaGetLastError();
@@ -991,6 +1012,7 @@ cudaError_t launch_eps_star(const KP<T>& p, const T* B, const T* J, const T* X, 
     template cudaError_t prepare_kernels<T>();                                                                    \
     template int stage_occupancy<T>(int, int, size_t);                                                            \
     template cudaError_t launch_control<T>(const KP<T>&, DevState*, double*, cudaStream_t);                       \
+    template cudaError_t launch_control_batch<T>(const StageArgsTMA<T>*, int, int*, cudaStream_t);                \
     template cudaError_t launch_finalize<T>(const double*, int, double*, cudaStream_t);                           \
     template cudaError_t launch_unpack<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \
     template cudaError_t launch_pack<T>(const KP<T>&, const T*, T*, cudaStream_t);                                \

@@ -169,33 +169,36 @@ struct TmaSmem {
 // Kind of a B-region point, fixed for the whole z march of a thread.
 enum { BK_SKIP = 0, BK_INNER = 1, BK_FACE_X = 2, BK_FACE_Y = 3 };
 
-// One RK stage over a 32 x 8 x TZ block of points.  Iteration kk of the z
-// march computes B on plane kb = kk - 1 (the tile and its face halo) and
-// then J, k_n and the stage position on plane kc = kk - 2.  Each thread keeps
-// its own column's B at kc - 1, kc, kc + 1 and the diagonals a, b, c and
-// 1/det of plane kc in registers, so J needs only the four in-plane
-// neighbours' B from shared memory, written in the previous iteration.
+// One RK stage over the 32 x 8 x TZ block (bx, by, bz) of one case.
+// Iteration kk of the z march computes B on plane kb = kk - 1 (the tile and
+// its face halo) and then J, k_n and the stage position on plane kc = kk - 2.
+// Each thread keeps its own column's B at kc - 1, kc, kc + 1 and the
+// diagonals a, b, c and 1/det of plane kc in registers, so J needs only the
+// four in-plane neighbours' B from shared memory, written in the previous
+// iteration.  `base` is the 128-byte aligned shared buffer with initialised
+// mbarriers; thread 0's `ph` holds the next completion parity of each ring
+// slot and carries over to the next tile.  Returns false after a bounded
+// wait ran out or an alignment check failed (the status word says which).
 template <typename T, bool PRESS, int NS>
-__global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2) k_stage_tma(const __grid_constant__ StageArgsTMA<T> A) {
+__device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int by, int bz, unsigned char* base,
+                                           uint32_t& ph) {
     constexpr bool LAST = NS == 5;
     constexpr int n = NS;
     constexpr int SLOT = TmaSmem<T>::SLOT;
     constexpr int PLANE_B = TmaSmem<T>::PLANE_B;
-    extern __shared__ __align__(128) unsigned char smraw[];
 
     const StageArgs<T>& a = A.a;
     const KP<T>& p = a.p;
     DevState* st = a.st;
-    if (st->done) return;
+    if (st->done) return true;
 
-    unsigned char* base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
     T* xs = reinterpret_cast<T*>(base);                                         // XR2 slots of SLOT elements
     T* bs = xs + XR2 * SLOT;                                                     // 2 B planes of PLANE_B
     uint64_t* bars = reinterpret_cast<uint64_t*>(bs + 2 * PLANE_B);             // XR2 mbarriers
     T* s_wmax = reinterpret_cast<T*>(bars + XR2);                                // TY2 warp maxima
     int* s_abort = reinterpret_cast<int*>(s_wmax + 2 * TY2);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY2, k0 = blockIdx.z * a.TZ;
+    const int i0 = bx * TX, j0 = by * TY2, k0 = bz * a.TZ;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const int kend = min(k0 + a.TZ, nz);
     const int cur = st->cur;
@@ -215,7 +218,7 @@ __global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2) 
     if ((smem_u32(xs) & 127u) || (smem_u32(bs) & 15u) || (smem_u32(bars) & 7u) ||
         (reinterpret_cast<uintptr_t>(tmap) & 63u) || ((i0 * (int)sizeof(T)) & 15)) {
         if (tid == 0) atomicOr(&st->status, (unsigned)GM_ST_ALIGN);
-        return;
+        return false;
     }
 
     // ---- per-thread descriptors, fixed for the whole z march ----------------
@@ -261,7 +264,13 @@ __global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2) 
     const T* __restrict__ ezp = p.ez;
 
     auto slot = [&](int plane) { return xs + ((plane + 12) % XR2) * SLOT; };
-    auto parity = [&](int plane) { return (uint32_t)(((plane - (k0 - 2)) / XR2) & 1); };
+    // thread 0: wait for the copy into the slot of `plane`, then flip that slot's parity
+    auto wait_plane = [&](int plane) {
+        const int sl = (plane + 12) % XR2;
+        const bool ok = mbar_wait_bounded(&bars[sl], (ph >> sl) & 1u);
+        ph ^= 1u << sl;
+        return ok;
+    };
     // ring positions relative to plane kk, from one modulo per iteration
     auto xring = [&](int m, int back) { int s = m - back; s += s < 0 ? XR2 : 0; return xs + s * SLOT; };
     auto face_b = [&](int face, int i, int j, int kb, T Bv[3]) {
@@ -273,12 +282,6 @@ __global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2) 
         b_face<T>(p, tl, a.B0, face, i, j, kb, Bv, &D);
     };
 
-    if (tid == 0) {
-        *s_abort = 0;
-        for (int s = 0; s < XR2; s++) mbar_init(&bars[s], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
     // position planes k0-2 .. kend+1 stream through the ring two planes ahead
     int issued = k0 - 3;   // thread 0: last plane whose copy was issued
     if (tid == 0) {
@@ -304,7 +307,7 @@ __global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2) 
             const int need = min(kk, kend + 1);
             while (waited < need && !*s_abort) {
                 const int q = waited + 1;
-                if (!mbar_wait_bounded(&bars[(q + 12) % XR2], parity(q))) {
+                if (!wait_plane(q)) {
                     *s_abort = 1;
                     atomicOr(&st->status, (unsigned)GM_ST_TIMEOUT);
                 } else {
@@ -505,7 +508,7 @@ __global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2) 
     }
     // drain copies still in flight (after an abort), bounded
     if (tid == 0 && *s_abort) {
-        for (int q = waited + 1; q <= issued; q++) mbar_wait_bounded(&bars[(q + 12) % XR2], parity(q));
+        for (int q = waited + 1; q <= issued; q++) wait_plane(q);
     }
     if (bad) atomicOr(&st->status, (unsigned)GM_ST_NAN);
     if (LAST) {
@@ -517,6 +520,61 @@ __global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2) 
             for (int w = 0; w < TY2; w++) m = fmax(m, s_wmax[w]);
             if (m > 0) atomicMax(&st->maxDeltaBits, (unsigned long long)__double_as_longlong((double)m));
         }
+    }
+    return *s_abort == 0;
+}
+
+// Shared-memory set-up common to the stage kernels: the 128-byte aligned
+// base, the ring's mbarriers and the abort flag.
+template <typename T>
+__device__ __forceinline__ unsigned char* stage_smem_setup(unsigned char* smraw) {
+    unsigned char* base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<T*>(base) + XR2 * TmaSmem<T>::SLOT +
+                                                 2 * TmaSmem<T>::PLANE_B);
+    int* s_abort = reinterpret_cast<int*>(reinterpret_cast<T*>(bars + XR2) + 2 * TY2);
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        *s_abort = 0;
+        for (int s = 0; s < XR2; s++) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    return base;
+}
+
+// One RK stage of one case: one CTA per 32 x 8 x TZ block.
+template <typename T, bool PRESS, int NS>
+__global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2)
+    k_stage_tma(const __grid_constant__ StageArgsTMA<T> A) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    if (A.a.st->done) return;
+    unsigned char* base = stage_smem_setup<T>(smraw);
+    uint32_t ph = 0;
+    stage_tile<T, PRESS, NS>(A, blockIdx.x, blockIdx.y, blockIdx.z, base, ph);
+}
+
+// One RK stage of many cases: a persistent launch whose CTAs take work items
+// (case, tile) from a counter until none is left; cases whose controller has
+// stopped are skipped.  The counter is reset by the batched controller.
+template <typename T, bool PRESS, int NS>
+__global__ void __launch_bounds__(TX * TY2, 2)
+    k_stage_tma_batch(const StageArgsTMA<T>* __restrict__ cases, const int4* __restrict__ work, int nwork,
+                      int* __restrict__ counter) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    unsigned char* base = stage_smem_setup<T>(smraw);
+    // work-item slot: the int after the abort flag, in the dynamic buffer's tail
+    int* s_w = reinterpret_cast<int*>(reinterpret_cast<T*>(reinterpret_cast<uint64_t*>(
+                   reinterpret_cast<T*>(base) + XR2 * TmaSmem<T>::SLOT + 2 * TmaSmem<T>::PLANE_B) + XR2) +
+               2 * TY2) + 1;
+    uint32_t ph = 0;
+    for (;;) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) *s_w = atomicAdd(counter, 1);
+        __syncthreads();
+        const int w = *s_w;
+        __syncthreads();   // s_w is rewritten only after every thread has read it
+        if (w >= nwork) break;
+        const int4 it = work[w];
+        if (!stage_tile<T, PRESS, NS>(cases[it.x], it.y, it.z, it.w, base, ph)) break;
+        __syncthreads();   // the next tile's copies overwrite slots this one read
     }
 }
 
@@ -530,6 +588,12 @@ static cudaError_t prep_one() {
     return cudaFuncSetAttribute(k_stage_tma<T, PRESS, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
+template <typename T, bool PRESS, int NS>
+static cudaError_t prep_batch() {
+    return cudaFuncSetAttribute(k_stage_tma_batch<T, PRESS, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                200 * 1024);
+}
+
 template <typename T>
 cudaError_t prepare_stage_tma() {
     cudaError_t e;
@@ -538,7 +602,45 @@ cudaError_t prepare_stage_tma() {
         (e = prep_one<T, true, 0>()) || (e = prep_one<T, true, 1>()) || (e = prep_one<T, true, 2>()) ||
         (e = prep_one<T, true, 3>()) || (e = prep_one<T, true, 4>()) || (e = prep_one<T, true, 5>()))
         return e;
+    if ((e = prep_batch<T, false, 0>()) || (e = prep_batch<T, false, 1>()) || (e = prep_batch<T, false, 2>()) ||
+        (e = prep_batch<T, false, 3>()) || (e = prep_batch<T, false, 4>()) || (e = prep_batch<T, false, 5>()) ||
+        (e = prep_batch<T, true, 0>()) || (e = prep_batch<T, true, 1>()) || (e = prep_batch<T, true, 2>()) ||
+        (e = prep_batch<T, true, 3>()) || (e = prep_batch<T, true, 4>()) || (e = prep_batch<T, true, 5>()))
+        return e;
     return cudaSuccess;
+}
+
+template <typename T>
+int stage_tma_batch_occupancy(int pressure) {
+    int nb = 0;
+    const size_t sm = stage_tma_smem_bytes<T>(pressure);
+    cudaError_t e = pressure
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma_batch<T, true, 0>, TX * TY2, sm)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma_batch<T, false, 0>, TX * TY2, sm);
+    return e == cudaSuccess && nb > 0 ? nb : 1;
+}
+
+template <typename T>
+cudaError_t launch_stage_tma_batch(const StageArgsTMA<T>* cases, const int4* work, int nwork, int* counter, int n,
+                                   int pressure, int nblocks, cudaStream_t s) {
+    const dim3 block(TX, TY2, 1);
+    const size_t sm = stage_tma_smem_bytes<T>(pressure);
+#define GMK_LAUNCH_B(PR)                                                                                        \
+    switch (n) {                                                                                                \
+        case 0: k_stage_tma_batch<T, PR, 0><<<nblocks, block, sm, s>>>(cases, work, nwork, counter); break;      \
+        case 1: k_stage_tma_batch<T, PR, 1><<<nblocks, block, sm, s>>>(cases, work, nwork, counter); break;      \
+        case 2: k_stage_tma_batch<T, PR, 2><<<nblocks, block, sm, s>>>(cases, work, nwork, counter); break;      \
+        case 3: k_stage_tma_batch<T, PR, 3><<<nblocks, block, sm, s>>>(cases, work, nwork, counter); break;      \
+        case 4: k_stage_tma_batch<T, PR, 4><<<nblocks, block, sm, s>>>(cases, work, nwork, counter); break;      \
+        default: k_stage_tma_batch<T, PR, 5><<<nblocks, block, sm, s>>>(cases, work, nwork, counter); break;     \
+    }
+    if (pressure) {
+        GMK_LAUNCH_B(true)
+    } else {
+        GMK_LAUNCH_B(false)
+    }
+#undef GMK_LAUNCH_B
+    return cudaGetLastError();
 }
 
 template <typename T>
@@ -577,6 +679,9 @@ cudaError_t launch_stage_tma(const StageArgsTMA<T>& A, int pressure, dim3 grid, 
     template size_t stage_tma_smem_bytes<T>(int);                                             \
     template cudaError_t prepare_stage_tma<T>();                                              \
     template int stage_tma_occupancy<T>(int);                                                 \
-    template cudaError_t launch_stage_tma<T>(const StageArgsTMA<T>&, int, dim3, cudaStream_t);
+    template cudaError_t launch_stage_tma<T>(const StageArgsTMA<T>&, int, dim3, cudaStream_t);                 \
+    template int stage_tma_batch_occupancy<T>(int);                                                           \
+    template cudaError_t launch_stage_tma_batch<T>(const StageArgsTMA<T>*, const int4*, int, int*, int, int, int, \
+                                                   cudaStream_t);
 
 }  // namespace gmk

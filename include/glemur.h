@@ -301,6 +301,45 @@ int gm_download_x(gm_handle* h, int which, void* xb);
 int gm_reduce_noalloc(const gm_params* p, const void* B, const void* J, const void* detJac,
                       gm_reduction* out, void* stream);
 
+/* ---- many independent cases (no counterpart in the reference, which runs
+ * one case per process) ------------------------------------------------------
+ * Cases of uneven grid sizes advance together: each Runge-Kutta stage is ONE
+ * persistent launch whose CTAs take 32 x 8 x 32 tiles of every case from a
+ * work counter, one launch runs every case's controller (src/main.cu:321-383
+ * per case), and a step of all cases is one CUDA graph replay.  A case whose
+ * controller has stopped (nCycle, dtMin, NaN) or that gm_batch_stop /
+ * gm_batch_run stopped is skipped by the launches.  All cases share the
+ * precision and the pressure flag; each has its own dt and time. */
+typedef struct gm_batch gm_batch;
+
+/* Outcome of one case of gm_batch_run. */
+typedef struct gm_batch_case {
+    double  seconds;     /* wall time from the start of gm_batch_run to the check that ended the case */
+    double  residual;    /* residual at that check (weighted, or pointwise when asked) */
+    double  t, dt;
+    int32_t attempted, accepted;
+    uint32_t status;     /* GM_ST_* bits */
+    int32_t converged;   /* 1 when the residual reached the target */
+} gm_batch_case;
+
+int gm_batch_create(const gm_params* cases, int nCases, gm_batch** out);
+int gm_batch_destroy(gm_batch* b);
+int gm_batch_upload(gm_batch* b, int c, const void* xb, const void* B0, double t, double dt);
+/* Enqueue nSteps attempted steps of every case (graph replays, no sync). */
+int gm_batch_steps_async(gm_batch* b, int nSteps);
+int gm_batch_get_state(gm_batch* b, int c, gm_state* out);
+int gm_batch_refresh(gm_batch* b, int c, gm_reduction* r);
+int gm_batch_download(gm_batch* b, int c, void* xb, void* B, void* J, void* detJac);
+/* Stop case c: the launches skip it from the next step on. */
+int gm_batch_stop(gm_batch* b, int c);
+/* Advance all cases; every checkEvery steps each running case's residual
+ * (gm_reduction.residual, or residualPw when pointwise != 0) is evaluated and
+ * a case at or below `residual` is stopped.  Cases also stop at nCycle
+ * accepted steps (counted from this call) or by their own stop rule.  Returns
+ * when every case has stopped; out[c] (may be NULL) gets each case's outcome. */
+int gm_batch_run(gm_batch* b, int nCycle, double residual, int pointwise, int checkEvery, gm_batch_case* out);
+int64_t gm_batch_launch_count(const gm_batch* b);
+
 /* Number of CUDA devices and selection of the device the calling thread
  * uses (the cudaGetDeviceCount / cudaSetDevice of src/main.cu:47-80). */
 int gm_device_count(int* n);
