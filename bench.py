@@ -6,6 +6,14 @@ is one attempted adaptive Runge-Kutta step (6 stages + accept/reject) over
 the whole grid; the metric is cell-RK-stages/s = N x 6 x steps / time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py --workload batch64 [--batch-residual R] [--batch-cycles C]
+
+--workload batch64 runs the batched configuration instead: 64 seeded random
+braids of uneven sizes (seeds 1000..1063, drawn as configs.random_braid) in
+one persistent launch per RK stage, each case until its weighted force-free
+residual reaches R, its dt falls to dtMin, or C accepted steps; it reports
+the aggregate cell-RK-stages/s and the p50/p99 time per case, and the same
+cases run one after another through the single-case path for comparison.
 
 --impl reference times the reference's relaxation arithmetic on the host
 cores: the reference is CUDA-only, so its CPU form is the C restatement in
@@ -320,6 +328,74 @@ def run_gpu(args):
     return 0
 
 
+def run_batch(args):
+    """--workload batch64: the batched configuration (see the module docstring)."""
+    import torch
+    from glemur_gb300 import BatchRelaxation, Relaxation, configs
+    dist, rank, ws = dist_init()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    ps = [configs.random_braid(1000 + i, precision=32) for i in range(64)]
+    inits = [configs.init_state(p) for p in ps]
+    Ns = [p.nx * p.ny * p.nz for p in ps]
+    b = BatchRelaxation(ps)
+    for c, (B0, xb) in enumerate(inits):
+        b.upload(c, xb, B0)
+    b.steps_async(max(args.warmup, 3))       # warm-up, captures the step graph
+    b.state(0)
+    for c, (B0, xb) in enumerate(inits):     # start every case afresh
+        b.upload(c, xb, B0)
+    l0 = b.launches()
+    torch.cuda.synchronize()
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as ck:
+        t0 = time.perf_counter()
+        out = b.run(args.batch_cycles, args.batch_residual, pointwise=False, check_every=10)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = b.launches() - l0
+    att = [o["attempted"] for o in out]
+    work = sum(N * 6 * a for N, a in zip(Ns, att))
+    value = work / wall
+    secs = sorted(o["seconds"] for o in out)
+    conv = sum(o["converged"] for o in out)
+    folded = sum(1 for o in out if not o["converged"] and o["status"] & 4)
+    b.close()
+    # the same cases, one after another, same attempted steps, single-case path
+    seq_t = 0.0
+    for p, (B0, xb), a in zip(ps, inits, att):
+        g = Relaxation(p)
+        g.upload(xb, B0)
+        g.steps_async(3)
+        g.state()
+        g.upload(xb, B0)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        g.steps_async(a)
+        g.state()
+        seq_t += time.perf_counter() - t1
+        g.close()
+    if rank == 0:
+        shapes = {}
+        for p in ps:
+            k = f"{p.nx}x{p.ny}x{p.nz}"
+            shapes[k] = shapes.get(k, 0) + 1
+        line = {
+            "metric": "cell-RK-stages/s (64 batched random braids, each to weighted residual <= R)",
+            "value": value, "unit": UNIT, "n_gpus": 1, "steps": int(sum(att)), "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch64: random braids, seeds 1000..1063, 2-8 blobs, sizes drawn from "
+                                   "32^3, 48x48x96, 64x64x128, 96x96x192", "shapes": shapes,
+                       "residual_target": args.batch_residual, "max_accepted": args.batch_cycles,
+                       "check_every": 10, "parallelism": "single"},
+            "wall_s": wall, "p50_case_s": secs[len(secs) // 2], "p99_case_s": secs[min(len(secs) - 1, int(0.99 * len(secs)))],
+            "converged": conv, "folded_dtmin": folded, "budget_reached": len(out) - conv - folded,
+            "sequential_single_case": {"value": work / seq_t, "unit": UNIT, "seconds": seq_t},
+            "gpu_launches": launches, "clocks": ck.summary(),
+        }
+        print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -328,11 +404,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--workload", default="braid6", choices=["braid6", "batch64"])
+    ap.add_argument("--batch-residual", type=float, default=0.2)
+    ap.add_argument("--batch-cycles", type=int, default=3000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch64":
+        return run_batch(args)
     return run_gpu(args)
 
 
