@@ -125,7 +125,7 @@ struct Impl : ImplBase {
     cudaGraphExec_t gexec = nullptr;
     // TMA-fed stage kernel: tensor maps of X[0], X[1], XS[0], XS[1]
     bool use_tma = true;
-    CUtensorMap tmaps[4];
+    CUtensorMap tmaps[10];
     dim3 grid2;
     int TZ2 = 32;
     size_t NG = 0, N = 0, NP = 0;
@@ -163,6 +163,8 @@ struct Impl : ImplBase {
         kp.pz = nz + 4;
         kp.cs = ((long long)kp.px * kp.py * kp.pz + 63) / 64 * 64;
         kp.N = (long long)nx * ny * nz;
+        kp.kpx = (nx + 7) / 8 * 8;
+        kp.kcs = ((long long)kp.kpx * ny * nz + 63) / 64 * 64;
         kp.dx = (T)p->dx; kp.dy = (T)p->dy; kp.dz = (T)p->dz;
         kp.dx1 = (T)p->dx1; kp.dy1 = (T)p->dy1; kp.dz1 = (T)p->dz1;
         kp.hdx1 = kp.dx1 / 2; kp.hdy1 = kp.dy1 / 2; kp.hdz1 = kp.dz1 / 2;
@@ -211,7 +213,7 @@ struct Impl : ImplBase {
             if ((rc = alloc((void**)&XS[q], NP * sizeof(T)))) return rc;
         }
         for (int m = 0; m < 5; m++)
-            if ((rc = alloc((void**)&K[m], 3 * N * sizeof(T)))) return rc;
+            if ((rc = alloc((void**)&K[m], 3 * (size_t)kp.kcs * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&B0, NP * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&B0s, NP * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outB, 3 * NG * sizeof(T)))) return rc;
@@ -293,13 +295,24 @@ struct Impl : ImplBase {
         cuuint64_t strides[3] = {(cuuint64_t)kp.px * es, (cuuint64_t)kp.px * kp.py * es, (cuuint64_t)kp.cs * es};
         cuuint32_t box[4] = {gmk::TX + 4, gmk::STAGE_TMA_TY + 4, 1, 3};
         cuuint32_t estr[4] = {1, 1, 1, 1};
-        T* bufs[4] = {X[0], X[1], XS[0], XS[1]};
-        for (int q = 0; q < 4; q++) {
-            CUresult r = enc(&tmaps[q], sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4,
-                             (void*)bufs[q], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        const CUtensorMapDataType dtype = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+        T* bufs[5] = {X[0], X[1], XS[0], XS[1], B0s};
+        for (int q = 0; q < 5; q++) {
+            CUresult r = enc(&tmaps[q], dtype, 4, (void*)bufs[q], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             if (r != CUDA_SUCCESS) return gm::fail(GM_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        }
+        // k_m over (nx, ny, nz, component), row pitch kpx: box 32 x 8 x 1 x 3, the tile
+        // (rows start on 16-byte boundaries: kpx is a multiple of 8)
+        cuuint64_t kdims[4] = {(cuuint64_t)kp.nx, (cuuint64_t)kp.ny, (cuuint64_t)kp.nz, 3};
+        cuuint64_t kstrides[3] = {(cuuint64_t)kp.kpx * es, (cuuint64_t)kp.kpx * kp.ny * es, (cuuint64_t)kp.kcs * es};
+        cuuint32_t kbox[4] = {gmk::TX, gmk::STAGE_TMA_TY, 1, 3};
+        for (int m = 0; m < 5; m++) {
+            CUresult r = enc(&tmaps[5 + m], dtype, 4, (void*)K[m], kdims, kstrides, kbox, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return gm::fail(GM_ECUDA, "cuTensorMapEncodeTiled (k) failed: " + std::to_string((int)r));
         }
         // z chunking as for k_stage, with the tile height fixed at 8
         const int nx = kp.nx, ny = kp.ny, nz = kp.nz;

@@ -21,7 +21,9 @@
 //              produces the positions; non-periodic ghost layers hold the
 //              fixed line-tied positions of the initial grid.
 //   B0:        same padded layout (ghost depth 1 used).
-//   k_m:       inner points only, index i + nx*(j + ny*k), component stride N.
+//   k_m:       inner points only, index i + kpx*(j + ny*k) with the row pitch
+//              kpx = nx rounded up to 8 (so rows start on 16-byte boundaries,
+//              as tensor-map copies need), component stride kcs.
 #pragma once
 
 #include <cuda.h>
@@ -58,6 +60,8 @@ struct KP {
     int px, py, pz;          // padded extents
     long long cs;            // component stride of padded arrays
     long long N;             // nx*ny*nz
+    int kpx;                 // row pitch of the k_m arrays (nx rounded up to 8)
+    long long kcs;           // component stride of the k_m arrays
     T dx, dy, dz, dx1, dy1, dz1;
     T hdx1, hdy1, hdz1;      // dx1/2, dy1/2, dz1/2 (exact)
     T Lx, Ly, Lz, Ox, Oy, Oz;
@@ -143,16 +147,18 @@ template <typename T>
 cudaError_t launch_eps_star(const KP<T>& p, const T* B, const T* J, const T* X, T* scratch, double* out,
                             cudaStream_t s);
 
-// TMA-fed stage kernel (gm_stage_tma.cuh): 32 x 8 tiles, position planes
-// streamed by cp.async.bulk.tensor.  tm[] are the tensor maps of X[0], X[1],
-// XS[0], XS[1] (box 36 x 12 x 1 x 3 over (px, py, pz, component)).
+// TMA-fed stage kernel (gm_stage_tma.cuh): 32 x 8 tiles, operand planes
+// streamed by cp.async.bulk.tensor.  tm[0..3] are the tensor maps of X[0],
+// X[1], XS[0], XS[1] and tm[4] of B0s (box 36 x 12 x 1 x 3 over (px, py, pz,
+// component)); tm[5..9] those of k_0..k_4 (box 32 x 8 x 1 x 3 over
+// (nx, ny, nz, component) with row pitch kpx).
 template <typename T>
 struct StageArgsTMA {
-    CUtensorMap tm[4];
+    CUtensorMap tm[10];
     StageArgs<T> a;
 };
 template <typename T>
-size_t stage_tma_smem_bytes(int pressure);
+size_t stage_tma_smem_bytes(int pressure, int n);
 template <typename T>
 cudaError_t prepare_stage_tma();
 template <typename T>

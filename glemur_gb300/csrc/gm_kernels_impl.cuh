@@ -399,6 +399,8 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                 for (int l = 0; l < 3; l++) Bc[l] = t.b(kc, l, j, i);
                 stokes<T>(xn, bn, Jv);
                 const long long lin = (long long)i + (long long)p.nx * ((long long)j + (long long)p.ny * kc);
+                const long long klin = (long long)i + (long long)p.kpx * ((long long)j + (long long)p.ny * kc);
+                const long long KC = p.kcs;
                 if (MODE == MODE_STAGE) {
                     T kn[3];
                     cross3(Jv, Bc, kn);
@@ -420,7 +422,7 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                         // x_{n+1} = x_n + sum_{m<=n} (b[n+1][m] - b[n][m]) k_m  (rungeKutta.cu:216-227)
                         for (int m = 0; m < n; m++) {
                             const T* Km = a.K[m];
-                            const T k0v = __ldg(&Km[lin]), k1v = __ldg(&Km[N + lin]), k2v = __ldg(&Km[2 * N + lin]);
+                            const T k0v = __ldg(&Km[klin]), k1v = __ldg(&Km[KC + klin]), k2v = __ldg(&Km[2 * KC + klin]);
                             const T w = p.db[n][m];
                             xa[0] += w * k0v;
                             xa[1] += w * k1v;
@@ -430,18 +432,18 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
 #pragma unroll
                         for (int l = 0; l < 3; l++) xa[l] += w * kn[l];
                         T* Kn = a.K[n];
-                        Kn[lin] = kn[0];
-                        Kn[N + lin] = kn[1];
-                        Kn[2 * N + lin] = kn[2];
+                        Kn[klin] = kn[0];
+                        Kn[KC + klin] = kn[1];
+                        Kn[2 * KC + klin] = kn[2];
                         store_pos<T>(p, a.XS[n & 1], i, j, kc, xa);
                     } else {
                         // stage 5: x_6, then x_new, x* and the error norm (rungeKutta.cu:251-339)
                         T km[6][3];
 #pragma unroll
                         for (int m = 0; m < 5; m++) {
-                            km[m][0] = __ldg(&a.K[m][lin]);
-                            km[m][1] = __ldg(&a.K[m][N + lin]);
-                            km[m][2] = __ldg(&a.K[m][2 * N + lin]);
+                            km[m][0] = __ldg(&a.K[m][klin]);
+                            km[m][1] = __ldg(&a.K[m][KC + klin]);
+                            km[m][2] = __ldg(&a.K[m][2 * KC + klin]);
                         }
 #pragma unroll
                         for (int l = 0; l < 3; l++) km[5][l] = kn[l];
@@ -757,12 +759,15 @@ __global__ void k_pack(const KP<T> p, const T* __restrict__ soa, T* __restrict__
     }
 }
 
+// k_m from the pitched SoA layout to the reference kk layout (inner AoS).
 template <typename T>
 __global__ void k_pack_k(const KP<T> p, const T* __restrict__ k, T* __restrict__ aos) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < p.N; q += (long long)gridDim.x * blockDim.x) {
-        aos[3 * q] = k[q];
-        aos[3 * q + 1] = k[p.N + q];
-        aos[3 * q + 2] = k[2 * p.N + q];
+        const long long i = q % p.nx, r = q / p.nx;
+        const long long g = i + (long long)p.kpx * r;
+        aos[3 * q] = k[g];
+        aos[3 * q + 1] = k[p.kcs + g];
+        aos[3 * q + 2] = k[2 * p.kcs + g];
     }
 }
 

@@ -2,14 +2,14 @@
 //
 // Same arithmetic as k_stage (gm_kernels_impl.cuh); different data movement:
 //   * tiles are 32 x 8 columns (compile time), one warp per tile row;
-//   * one thread streams each grid plane (tile + 2-point halo, all three
-//     components as one 4-D box) from the padded position array into a ring of
-//     XR2 shared-memory slots with cp.async.bulk.tensor, completion tracked by
-//     one mbarrier per slot;
-//   * J for plane k is formed one iteration after B of plane k+1, so an
+//   * one thread streams, plane by plane, every operand of the stage with
+//     cp.async.bulk.tensor into shared-memory rings: the grid positions
+//     (tile + 2-point halo, all three components as one 4-D box), the scaled
+//     field B0s (same box) and the increments k_0..k_{n-1} over the tile;
+//     completion is tracked by one mbarrier per ring slot;
+//   * J for plane k is formed in the same iteration as B of plane k+1, so an
 //     iteration needs a single __syncthreads;
-//   * every shared-memory neighbour access is a constant offset from a
-//     per-plane base.
+//   * every shared-memory access is a constant offset from a per-plane base.
 // Waits on the mbarriers are bounded: after kWaitLimit polls the CTA records
 // GM_ST_TIMEOUT, drains the copies it has in flight (again bounded) and
 // returns.
@@ -24,7 +24,6 @@ namespace gmk {
 constexpr int TY2 = 8;                   // tile rows (= warps per CTA)
 constexpr int HX2 = TX + 4, HY2 = TY2 + 4;
 constexpr int BX2 = TX + 2, BY2 = TY2 + 2;
-constexpr int XR2 = 6;                   // position-plane ring
 // resident CTAs per SM the stage kernel is compiled for (register budget)
 #ifndef GM_STAGE_MINB
 #define GM_STAGE_MINB 3
@@ -113,13 +112,13 @@ __device__ __forceinline__ T det_cols(const T A[3][3]) {
 // differences a = x(+x) - x(-x), b, c and the pre-scaled field
 // s = (4 dy dz B0x, 4 dx dz B0y, 4 dx dy B0z): since jac = [a/2dx, b/2dy,
 // c/2dz], this is jac.B0 / det(jac) of B_JacB0 (rungeKutta.cu:79-99) with
-// the constant factors folded.  Returns the columns a, b, c in Am[l][0..2]
-// and 1/det(a, b, c) in *rdet (Delta = 1 / (8 dx dy dz rdet)).
+// the constant factors folded.  x and s come from shared-memory planes at the
+// same offset o.  Returns the columns a, b, c in Am[l][0..2] and
+// 1/det(a, b, c) in *rdet (Delta = 1 / (8 dx dy dz rdet)).
 template <typename T>
 __device__ __forceinline__ void b_point(const T* __restrict__ xm, const T* __restrict__ x0, const T* __restrict__ xp,
-                                        int o, const T* __restrict__ B0s, int g, int cs, T Bv[3], T Am[3][3],
-                                        T* rdet) {
-    const T s0 = __ldg(&B0s[g]), s1 = __ldg(&B0s[cs + g]), s2 = __ldg(&B0s[2 * cs + g]);
+                                        int o, const T* __restrict__ b0s, T Bv[3], T Am[3][3], T* rdet) {
+    const T s0 = b0s[o], s1 = b0s[o + PLANE_C], s2 = b0s[o + 2 * PLANE_C];
 #pragma unroll
     for (int l = 0; l < 3; l++) {
         const int q = o + l * PLANE_C;
@@ -151,19 +150,43 @@ __device__ __forceinline__ void ld_b(const double* d, double v[3]) {
     v[0] = q0.x; v[1] = q0.y; v[2] = q1.x;
 }
 
-// Shared memory of k_stage_tma, all in the dynamic buffer (no static
-// __shared__ variables, which would shift the dynamic base): the base is
-// rounded up to 128 bytes at run time (the launch asks for 128 bytes of
-// slack), then come the position-plane slots (each a multiple of 128 bytes,
-// the alignment TMA destinations need), the two B planes, the mbarriers and
-// flags.
-template <typename T>
-struct TmaSmem {
+// Shared memory of the stage kernels, all in the dynamic buffer (the base is
+// rounded up to 128 bytes at run time; the launch asks for 128 bytes of
+// slack):
+//   XR position-plane slots (the tile + 2-point halo, three components),
+//   2 slots of B0s planes (same box),
+//   2 slots of k-planes (the n arrays k_0..k_{n-1} over the tile),
+//   2 B planes (float4 per point: B and a pad),
+//   XR + 4 mbarriers, warp maxima, the abort flag and the work-item slot.
+// Every slot is a multiple of 128 bytes, the alignment TMA destinations need.
+template <typename T, bool PRESS, int NS>
+struct StageSmem {
+    static constexpr int XR = PRESS ? 5 : 4;                      // position ring (one plane of prefetch)
     static constexpr int SLOT = slot_elems<T>();
-    static constexpr int PLANE_B = 4 * BY2 * BX2;   // elements of one B plane
-    static constexpr size_t bytes(int) {
-        return 128 + sizeof(T) * ((size_t)XR2 * SLOT + 2 * (size_t)PLANE_B) + 8 * XR2 + 16 * TY2 + 16;
-    }
+    static constexpr int NK = NS;                                 // k arrays read by stage NS
+    static constexpr int KBOX = 3 * TY2 * TX;                     // elements of one k-array plane
+    static constexpr int KSLOT = NK * KBOX;
+    static constexpr int PLANE_B = 4 * BY2 * BX2;
+    static constexpr size_t OFF_B0 = sizeof(T) * (size_t)XR * SLOT;
+    static constexpr size_t OFF_K = OFF_B0 + sizeof(T) * 2 * (size_t)SLOT;
+    static constexpr size_t OFF_B = OFF_K + sizeof(T) * 2 * (size_t)KSLOT;
+    static constexpr size_t OFF_BAR = OFF_B + sizeof(T) * 2 * (size_t)PLANE_B;
+    static constexpr int NBAR = XR + 4;                          // x slots, 2 B0s slots, 2 k slots
+    static constexpr size_t OFF_WMAX = OFF_BAR + 8 * NBAR;
+    static constexpr size_t OFF_CTL = OFF_WMAX + 16 * TY2;
+    static constexpr size_t BYTES = 128 + OFF_CTL + 64;
+};
+
+// Copy bookkeeping of a CTA, kept in shared memory and touched by the
+// producer thread only (abort and the work item are read by all threads after
+// a barrier).
+struct StageCtl {
+    uint32_t ph;                 // next completion parity of each mbarrier
+    int x_iss, x_done;           // position planes issued / completed
+    int b_iss, b_done;           // B0s planes
+    int k_iss, k_done;           // k planes
+    int abort;                   // a bounded wait ran out
+    int work;                    // batched launch: the current work item
 };
 
 // Kind of a B-region point, fixed for the whole z march of a thread.
@@ -175,49 +198,62 @@ enum { BK_SKIP = 0, BK_INNER = 1, BK_FACE_X = 2, BK_FACE_Y = 3 };
 // Each thread keeps its own column's B at kc - 1, kc, kc + 1 and the
 // diagonals a, b, c and 1/det of plane kc in registers, so J needs only the
 // four in-plane neighbours' B from shared memory, written in the previous
-// iteration.  `base` is the 128-byte aligned shared buffer with initialised
-// mbarriers; thread 0's `ph` holds the next completion parity of each ring
-// slot and carries over to the next tile.  Returns false after a bounded
-// wait ran out or an alignment check failed (the status word says which).
+// iteration.  Operands arrive by TMA one iteration ahead: position plane
+// kk + 1 (into the slot of plane kk + 1 - XR: the B phase last read it in the
+// previous iteration, and so did the pressure gradient, which reads planes
+// kc - 1 .. kc + 1, with its fifth slot), the B0s plane of the next B phase
+// and the k planes of the next J phase.  `base` is the 128-byte aligned shared buffer
+// with initialised mbarriers; the mbarrier parities in its StageCtl carry
+// over to the next tile.  Returns false
+// after a bounded wait ran out or an alignment check failed (the status word
+// says which).
 template <typename T, bool PRESS, int NS>
-__device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int by, int bz, unsigned char* base,
-                                           uint32_t& ph) {
+__device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int by, int bz, unsigned char* base) {
+    using L = StageSmem<T, PRESS, NS>;
     constexpr bool LAST = NS == 5;
     constexpr int n = NS;
-    constexpr int SLOT = TmaSmem<T>::SLOT;
-    constexpr int PLANE_B = TmaSmem<T>::PLANE_B;
+    constexpr int XR = L::XR;
+    constexpr int SLOT = L::SLOT;
+    constexpr int PLANE_B = L::PLANE_B;
 
     const StageArgs<T>& a = A.a;
     const KP<T>& p = a.p;
     DevState* st = a.st;
     if (st->done) return true;
 
-    T* xs = reinterpret_cast<T*>(base);                                         // XR2 slots of SLOT elements
-    T* bs = xs + XR2 * SLOT;                                                     // 2 B planes of PLANE_B
-    uint64_t* bars = reinterpret_cast<uint64_t*>(bs + 2 * PLANE_B);             // XR2 mbarriers
-    T* s_wmax = reinterpret_cast<T*>(bars + XR2);                                // TY2 warp maxima
-    int* s_abort = reinterpret_cast<int*>(s_wmax + 2 * TY2);
+    T* xs = reinterpret_cast<T*>(base);                                   // XR position slots
+    T* b0r = reinterpret_cast<T*>(base + L::OFF_B0);                       // 2 B0s slots
+    T* kr = reinterpret_cast<T*>(base + L::OFF_K);                         // 2 k slots
+    T* bs = reinterpret_cast<T*>(base + L::OFF_B);                         // 2 B planes
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + L::OFF_BAR);       // x | B0s | k
+    T* s_wmax = reinterpret_cast<T*>(base + L::OFF_WMAX);
+    StageCtl* ctl = reinterpret_cast<StageCtl*>(base + L::OFF_CTL);
+    int* s_abort = &ctl->abort;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    // the producer (copy issue and waits) is lane 0 of the last warp, which
+    // computes no face-halo B points
+    const bool producer = tid == (TY2 - 1) * TX;
     const int i0 = bx * TX, j0 = by * TY2, k0 = bz * a.TZ;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const int kend = min(k0 + a.TZ, nz);
     const int cur = st->cur;
     const int mapi = (n == 0) ? cur : 2 + ((n - 1) & 1);
     const CUtensorMap* tmap = &A.tm[mapi];
+    const CUtensorMap* tmb0 = &A.tm[4];
     const T dtT = (T)st->dt;
-    const int N = (int)p.N;
+    const int KC = (int)p.kcs;
     const int cs = (int)p.cs;
-    const int px = p.px;
     const int pxy = p.px * p.py;
     const bool zPeri = p.zPeri != 0;
     constexpr uint32_t kPlaneBytes = PLANE_X * sizeof(T);
+    constexpr uint32_t kKBytes = (uint32_t)(L::KSLOT * sizeof(T));
 
     // self-check of the alignment TMA needs: destination slots on 128 bytes,
-    // mbarriers on 8 bytes, tensor map on 64 bytes, box start on 16 bytes; on
+    // mbarriers on 8 bytes, tensor maps on 64 bytes, box start on 16 bytes; on
     // failure record a status bit and issue no copy
-    if ((smem_u32(xs) & 127u) || (smem_u32(bs) & 15u) || (smem_u32(bars) & 7u) ||
-        (reinterpret_cast<uintptr_t>(tmap) & 63u) || ((i0 * (int)sizeof(T)) & 15)) {
-        if (tid == 0) atomicOr(&st->status, (unsigned)GM_ST_ALIGN);
+    if ((smem_u32(xs) & 127u) || (smem_u32(b0r) & 127u) || (smem_u32(kr) & 127u) || (smem_u32(bs) & 15u) ||
+        (smem_u32(bars) & 7u) || (reinterpret_cast<uintptr_t>(&A.tm[0]) & 63u) || ((i0 * (int)sizeof(T)) & 15)) {
+        if (producer) atomicOr(&st->status, (unsigned)GM_ST_ALIGN);
         return false;
     }
 
@@ -225,9 +261,9 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     // B-phase point 1: the thread's own tile point
     const int ic = i0 + tx, jc = j0 + ty;
     const bool own = ic < nx && jc < ny;
-    const int ox1 = (ty + 2) * HX2 + (tx + 2);           // in a position plane
+    const int ox1 = (ty + 2) * HX2 + (tx + 2);           // in a position / B0s plane
     const int ob1 = 4 * ((ty + 1) * BX2 + (tx + 1));     // in a B plane
-    const int gxy1 = (ic + 2) + px * (jc + 2);           // padded offset without the plane term
+    const int tyx = ty * TX + tx;                        // in a k plane
     // in a partial tile the ghost column i = nx or row j = ny is a tile point
     int kind1 = BK_SKIP;
     const bool xo1 = ic >= nx, yo1 = jc >= ny;
@@ -254,27 +290,42 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     }
     const int ox2 = (jj2 + 1) * HX2 + (ii2 + 1);
     const int ob2 = 4 * (jj2 * BX2 + ii2);
-    const int gxy2 = (i2 + 2) + px * (j2 + 2);
     // output point
     const T exy = own ? p.ex[ic] * p.ey[jc] : (T)0;
-    const int nxy = nx * ny;
-    const int lin0 = ic + nx * jc;
+    const int gxy1 = (ic + 2) + p.px * (jc + 2);         // padded offset without the plane term
+    const int lin0 = ic + p.kpx * jc;                    // k_m index of the own column
+    const int kplane = p.kpx * ny;
     const bool img_xy = (p.xPeri && (ic < 2 || ic >= nx - 2)) || (p.yPeri && (jc < 2 || jc >= ny - 2));
-    const T* __restrict__ B0s = a.B0s;
     const T* __restrict__ ezp = p.ez;
 
-    auto slot = [&](int plane) { return xs + ((plane + 12) % XR2) * SLOT; };
-    // thread 0: wait for the copy into the slot of `plane`, then flip that slot's parity
-    auto wait_plane = [&](int plane) {
-        const int sl = (plane + 12) % XR2;
-        const bool ok = mbar_wait_bounded(&bars[sl], (ph >> sl) & 1u);
-        ph ^= 1u << sl;
+    auto xslot = [&](int plane) { return (plane + 20) % XR; };
+    // thread 0: wait for the copy tracked by mbarrier b, then flip its parity
+    auto wait_bar = [&](int b) {
+        const bool ok = mbar_wait_bounded(&bars[b], (ctl->ph >> b) & 1u);
+        ctl->ph ^= 1u << b;
         return ok;
     };
+    auto issue_x = [&](int q) {
+        uint64_t* b = &bars[xslot(q)];
+        mbar_expect_tx(b, kPlaneBytes);
+        tma_load_4d(xs + xslot(q) * SLOT, tmap, b, i0, j0, q + 2, 0);
+    };
+    auto issue_b0 = [&](int q) {
+        uint64_t* b = &bars[XR + (q & 1)];
+        mbar_expect_tx(b, kPlaneBytes);
+        tma_load_4d(b0r + (q & 1) * SLOT, tmb0, b, i0, j0, q + 2, 0);
+    };
+    auto issue_k = [&](int q) {
+        uint64_t* b = &bars[XR + 2 + (q & 1)];
+        mbar_expect_tx(b, kKBytes);
+#pragma unroll
+        for (int m = 0; m < n; m++)
+            tma_load_4d(kr + (q & 1) * L::KSLOT + m * L::KBOX, &A.tm[5 + m], b, i0, j0, q, 0);
+    };
     // ring positions relative to plane kk, from one modulo per iteration
-    auto xring = [&](int m, int back) { int s = m - back; s += s < 0 ? XR2 : 0; return xs + s * SLOT; };
+    auto xring = [&](int m, int back) { int s = m - back; s += s < 0 ? XR : 0; return xs + s * SLOT; };
     auto face_b = [&](int face, int i, int j, int kb, T Bv[3]) {
-        Tile<T, 4, XR2, 12> tl;
+        Tile<T, 4, XR, 20> tl;
         tl.xs = xs;
         tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = HY2;
         tl.slot = SLOT;
@@ -282,17 +333,18 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
         b_face<T>(p, tl, a.B0, face, i, j, kb, Bv, &D);
     };
 
-    // position planes k0-2 .. kend+1 stream through the ring two planes ahead
-    int issued = k0 - 3;   // thread 0: last plane whose copy was issued
-    if (tid == 0) {
-        for (int q = k0 - 2; q <= min(k0 + 2, kend + 1); q++) {
-            uint64_t* b = &bars[(q + 12) % XR2];
-            mbar_expect_tx(b, kPlaneBytes);
-            tma_load_4d(slot(q), tmap, b, i0, j0, q + 2, 0);
-            issued = q;
-        }
+    // copies issued / completed so far (the producer): position planes
+    // k0-2 .. kend+1, B0s planes k0-1 .. kend, k planes k0 .. kend-1
+    if (producer) {
+        for (int q = k0 - 2; q <= min(k0 + 1, kend + 1); q++) issue_x(q);
+        ctl->x_iss = min(k0 + 1, kend + 1);
+        ctl->x_done = k0 - 3;
+        issue_b0(k0 - 1);
+        ctl->b_iss = k0 - 1;
+        ctl->b_done = k0 - 2;
+        ctl->k_iss = k0 - 1;
+        ctl->k_done = k0 - 1;
     }
-    int waited = k0 - 3;   // thread 0: last plane whose copy completed
 
     T dmax = 0;
     bool bad = false;
@@ -302,31 +354,31 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     T An[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Rn = 0;
 
     for (int kk = k0; kk <= kend + 1; kk++) {
-        // (1) thread 0 waits for the newest plane the B phase needs
-        if (tid == 0) {
+        // (1) the producer waits for position plane kk, the B0s plane of
+        // kb = kk-1 and the k planes of kc = kk-2
+        if (producer) {
             const int need = min(kk, kend + 1);
-            while (waited < need && !*s_abort) {
-                const int q = waited + 1;
-                if (!wait_plane(q)) {
-                    *s_abort = 1;
-                    atomicOr(&st->status, (unsigned)GM_ST_TIMEOUT);
-                } else {
-                    waited = q;
-                }
+            bool ok = true;
+            while (ok && ctl->x_done < need) { ok = wait_bar(xslot(ctl->x_done + 1)); ctl->x_done++; }
+            while (ok && ctl->b_done < kk - 1) { ok = wait_bar(XR + ((ctl->b_done + 1) & 1)); ctl->b_done++; }
+            if (n > 0)
+                while (ok && ctl->k_done < kk - 2) { ok = wait_bar(XR + 2 + ((ctl->k_done + 1) & 1)); ctl->k_done++; }
+            if (!ok) {
+                *s_abort = 1;
+                atomicOr(&st->status, (unsigned)GM_ST_TIMEOUT);
             }
         }
         __syncthreads();
         if (*s_abort) break;
-        // (2) refill: plane kk+2 goes into the slot of plane kk-4, last read in
-        // the previous iteration (all threads are past this iteration's barrier)
-        if (tid == 0 && kk + 2 <= kend + 1 && kk + 2 > issued) {
-            const int q = kk + 2;
-            uint64_t* b = &bars[(q + 12) % XR2];
-            mbar_expect_tx(b, kPlaneBytes);
-            tma_load_4d(slot(q), tmap, b, i0, j0, q + 2, 0);
-            issued = q;
+        // (2) refills, into slots whose last reader was the previous iteration
+        // (every thread is past this iteration's barrier)
+        if (producer) {
+            const int qx = kk + 1;
+            if (qx <= kend + 1 && qx > ctl->x_iss) { issue_x(qx); ctl->x_iss = qx; }
+            if (kk <= kend && kk > ctl->b_iss) { issue_b0(kk); ctl->b_iss = kk; }
+            if (n > 0 && kk - 1 >= k0 && kk - 1 < kend && kk - 1 > ctl->k_iss) { issue_k(kk - 1); ctl->k_iss = kk - 1; }
         }
-        const int mx = (kk + 12) % XR2;     // ring slot of position plane kk
+        const int mx = (kk + 20) % XR;      // ring slot of position plane kk
         // (3) B on plane kb = kk - 1 into B plane kb & 1
         const int kb = kk - 1;
         T Bv[3] = {0, 0, 0};
@@ -335,17 +387,17 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             const T* xm = xring(mx, 2);
             const T* x0 = xring(mx, 1);
             const T* xq = xring(mx, 0);
-            const int gk = pxy * (kb + 2);
+            const T* s0 = b0r + (kb & 1) * SLOT;
             const bool zo = (kb < 0 || kb >= nz);
             T Bh[3], Ah[3][3], Rh;
             if (!zo) {
                 if (kind1 != BK_SKIP) {
-                    if (kind1 == BK_INNER) b_point<T>(xm, x0, xq, ox1, B0s, gxy1 + gk, cs, Bv, An, &Rn);
+                    if (kind1 == BK_INNER) b_point<T>(xm, x0, xq, ox1, s0, Bv, An, &Rn);
                     else face_b(kind1 == BK_FACE_X ? 0 : 1, ic, jc, kb, Bv);
                     st_b(bdst + ob1, Bv);
                 }
                 if (kind2 != BK_SKIP) {
-                    if (kind2 == BK_INNER) b_point<T>(xm, x0, xq, ox2, B0s, gxy2 + gk, cs, Bh, Ah, &Rh);
+                    if (kind2 == BK_INNER) b_point<T>(xm, x0, xq, ox2, s0, Bh, Ah, &Rh);
                     else face_b(kind2 == BK_FACE_X ? 0 : 1, i2, j2, kb, Bh);
                     st_b(bdst + ob2, Bh);
                 }
@@ -354,7 +406,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
                 if (own) face_b(2, ic, jc, kb, Bv);
             } else {
                 // periodic image plane: only the own column is needed
-                if (own) b_point<T>(xm, x0, xq, ox1, B0s, gxy1 + gk, cs, Bv, An, &Rn);
+                if (own) b_point<T>(xm, x0, xq, ox1, s0, Bv, An, &Rn);
             }
         }
 #pragma unroll
@@ -391,7 +443,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             T Jv[3];
 #pragma unroll
             for (int l = 0; l < 3; l++) Jv[l] = (Ac[l][0] * I1 + Ac[l][1] * I2 + Ac[l][2] * I0) * Rc;
-            const int lin = lin0 + nxy * kc;
+            const int lin = lin0 + kplane * kc;
             T kn[3];
             cross3(Jv, Bz, kn);
             const T f = dtT * (exy * __ldg(&ezp[kc]));
@@ -399,7 +451,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             for (int l = 0; l < 3; l++) kn[l] *= f;
             const T* x0 = xring(mx, 2);   // position plane kc
             if (PRESS) {
-                Tile<T, 4, XR2, 12> tl;
+                Tile<T, 4, XR, 20> tl;
                 tl.xs = xs;
                 tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = HY2;
                 tl.slot = SLOT;
@@ -414,29 +466,22 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             for (int l = 0; l < 3; l++) xa[l] = x0[ox1 + l * PLANE_C];
             const bool images = img_xy || (zPeri && (kc < 2 || kc >= nz - 2));
             const int g = gxy1 + pxy * (kc + 2);
+            const T* kp = kr + (kc & 1) * L::KSLOT + tyx;    // k_m component l at kp[(3m + l) * TX * TY2]
             if (!LAST) {
                 // x_{n+1} = x_n + sum_{m<=n} (b[n+1][m] - b[n][m]) k_m (rungeKutta.cu:216-227)
-                T km[n > 0 ? n : 1][3];
-#pragma unroll
-                for (int m = 0; m < n; m++) {
-                    km[m][0] = __ldg(&a.K[m][lin]);
-                    km[m][1] = __ldg(&a.K[m][N + lin]);
-                    km[m][2] = __ldg(&a.K[m][2 * N + lin]);
-                }
 #pragma unroll
                 for (int m = 0; m < n; m++) {
                     const T w = p.db[n][m];
-                    xa[0] += w * km[m][0];
-                    xa[1] += w * km[m][1];
-                    xa[2] += w * km[m][2];
+#pragma unroll
+                    for (int l = 0; l < 3; l++) xa[l] += w * kp[(3 * m + l) * TX * TY2];
                 }
                 const T w = p.db[n][n];
 #pragma unroll
                 for (int l = 0; l < 3; l++) xa[l] += w * kn[l];
                 T* Kn = a.K[n];
                 Kn[lin] = kn[0];
-                Kn[N + lin] = kn[1];
-                Kn[2 * N + lin] = kn[2];
+                Kn[KC + lin] = kn[1];
+                Kn[2 * KC + lin] = kn[2];
                 T* Xo = a.XS[n & 1];
                 if (images) {
                     store_pos<T>(p, Xo, ic, jc, kc, xa);
@@ -449,11 +494,9 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
                 // stage 5: x_6, x_new, x* and the error norm (rungeKutta.cu:251-339)
                 T km[6][3];
 #pragma unroll
-                for (int m = 0; m < 5; m++) {
-                    km[m][0] = __ldg(&a.K[m][lin]);
-                    km[m][1] = __ldg(&a.K[m][N + lin]);
-                    km[m][2] = __ldg(&a.K[m][2 * N + lin]);
-                }
+                for (int m = 0; m < 5; m++)
+#pragma unroll
+                    for (int l = 0; l < 3; l++) km[m][l] = kp[(3 * m + l) * TX * TY2];
 #pragma unroll
                 for (int l = 0; l < 3; l++) km[5][l] = kn[l];
 #pragma unroll
@@ -507,8 +550,11 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
         Rc = Rn;
     }
     // drain copies still in flight (after an abort), bounded
-    if (tid == 0 && *s_abort) {
-        for (int q = waited + 1; q <= issued; q++) wait_plane(q);
+    if (producer && *s_abort) {
+        for (int q = ctl->x_done + 1; q <= ctl->x_iss; q++) wait_bar(xslot(q));
+        for (int q = ctl->b_done + 1; q <= ctl->b_iss; q++) wait_bar(XR + (q & 1));
+        if (n > 0)
+            for (int q = ctl->k_done + 1; q <= ctl->k_iss; q++) wait_bar(XR + 2 + (q & 1));
     }
     if (bad) atomicOr(&st->status, (unsigned)GM_ST_NAN);
     if (LAST) {
@@ -525,16 +571,17 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
 }
 
 // Shared-memory set-up common to the stage kernels: the 128-byte aligned
-// base, the ring's mbarriers and the abort flag.
-template <typename T>
+// base, the mbarriers and the abort flag.
+template <typename T, bool PRESS, int NS>
 __device__ __forceinline__ unsigned char* stage_smem_setup(unsigned char* smraw) {
+    using L = StageSmem<T, PRESS, NS>;
     unsigned char* base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<T*>(base) + XR2 * TmaSmem<T>::SLOT +
-                                                 2 * TmaSmem<T>::PLANE_B);
-    int* s_abort = reinterpret_cast<int*>(reinterpret_cast<T*>(bars + XR2) + 2 * TY2);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + L::OFF_BAR);
+    StageCtl* ctl = reinterpret_cast<StageCtl*>(base + L::OFF_CTL);
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-        *s_abort = 0;
-        for (int s = 0; s < XR2; s++) mbar_init(&bars[s], 1);
+        ctl->ph = 0;
+        ctl->abort = 0;
+        for (int s = 0; s < L::NBAR; s++) mbar_init(&bars[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -547,9 +594,8 @@ __global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2)
     k_stage_tma(const __grid_constant__ StageArgsTMA<T> A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     if (A.a.st->done) return;
-    unsigned char* base = stage_smem_setup<T>(smraw);
-    uint32_t ph = 0;
-    stage_tile<T, PRESS, NS>(A, blockIdx.x, blockIdx.y, blockIdx.z, base, ph);
+    unsigned char* base = stage_smem_setup<T, PRESS, NS>(smraw);
+    stage_tile<T, PRESS, NS>(A, blockIdx.x, blockIdx.y, blockIdx.z, base);
 }
 
 // One RK stage of many cases: a persistent launch whose CTAs take work items
@@ -559,13 +605,10 @@ template <typename T, bool PRESS, int NS>
 __global__ void __launch_bounds__(TX * TY2, 2)
     k_stage_tma_batch(const StageArgsTMA<T>* __restrict__ cases, const int4* __restrict__ work, int nwork,
                       int* __restrict__ counter) {
+    using L = StageSmem<T, PRESS, NS>;
     extern __shared__ __align__(128) unsigned char smraw[];
-    unsigned char* base = stage_smem_setup<T>(smraw);
-    // work-item slot: the int after the abort flag, in the dynamic buffer's tail
-    int* s_w = reinterpret_cast<int*>(reinterpret_cast<T*>(reinterpret_cast<uint64_t*>(
-                   reinterpret_cast<T*>(base) + XR2 * TmaSmem<T>::SLOT + 2 * TmaSmem<T>::PLANE_B) + XR2) +
-               2 * TY2) + 1;
-    uint32_t ph = 0;
+    unsigned char* base = stage_smem_setup<T, PRESS, NS>(smraw);
+    int* s_w = &reinterpret_cast<StageCtl*>(base + L::OFF_CTL)->work;
     for (;;) {
         if (threadIdx.x == 0 && threadIdx.y == 0) *s_w = atomicAdd(counter, 1);
         __syncthreads();
@@ -573,14 +616,21 @@ __global__ void __launch_bounds__(TX * TY2, 2)
         __syncthreads();   // s_w is rewritten only after every thread has read it
         if (w >= nwork) break;
         const int4 it = work[w];
-        if (!stage_tile<T, PRESS, NS>(cases[it.x], it.y, it.z, it.w, base, ph)) break;
+        if (!stage_tile<T, PRESS, NS>(cases[it.x], it.y, it.z, it.w, base)) break;
         __syncthreads();   // the next tile's copies overwrite slots this one read
     }
 }
 
 template <typename T>
-size_t stage_tma_smem_bytes(int pressure) {
-    return TmaSmem<T>::bytes(pressure ? 4 : 3);
+size_t stage_tma_smem_bytes(int pressure, int n) {
+    switch (n) {
+        case 0: return pressure ? StageSmem<T, true, 0>::BYTES : StageSmem<T, false, 0>::BYTES;
+        case 1: return pressure ? StageSmem<T, true, 1>::BYTES : StageSmem<T, false, 1>::BYTES;
+        case 2: return pressure ? StageSmem<T, true, 2>::BYTES : StageSmem<T, false, 2>::BYTES;
+        case 3: return pressure ? StageSmem<T, true, 3>::BYTES : StageSmem<T, false, 3>::BYTES;
+        case 4: return pressure ? StageSmem<T, true, 4>::BYTES : StageSmem<T, false, 4>::BYTES;
+        default: return pressure ? StageSmem<T, true, 5>::BYTES : StageSmem<T, false, 5>::BYTES;
+    }
 }
 
 template <typename T, bool PRESS, int NS>
@@ -613,10 +663,10 @@ cudaError_t prepare_stage_tma() {
 template <typename T>
 int stage_tma_batch_occupancy(int pressure) {
     int nb = 0;
-    const size_t sm = stage_tma_smem_bytes<T>(pressure);
+    const size_t sm = stage_tma_smem_bytes<T>(pressure, 5);
     cudaError_t e = pressure
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma_batch<T, true, 0>, TX * TY2, sm)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma_batch<T, false, 0>, TX * TY2, sm);
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma_batch<T, true, 5>, TX * TY2, sm)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma_batch<T, false, 5>, TX * TY2, sm);
     return e == cudaSuccess && nb > 0 ? nb : 1;
 }
 
@@ -624,7 +674,7 @@ template <typename T>
 cudaError_t launch_stage_tma_batch(const StageArgsTMA<T>* cases, const int4* work, int nwork, int* counter, int n,
                                    int pressure, int nblocks, cudaStream_t s) {
     const dim3 block(TX, TY2, 1);
-    const size_t sm = stage_tma_smem_bytes<T>(pressure);
+    const size_t sm = stage_tma_smem_bytes<T>(pressure, n);
 #define GMK_LAUNCH_B(PR)                                                                                        \
     switch (n) {                                                                                                \
         case 0: k_stage_tma_batch<T, PR, 0><<<nblocks, block, sm, s>>>(cases, work, nwork, counter); break;      \
@@ -646,17 +696,17 @@ cudaError_t launch_stage_tma_batch(const StageArgsTMA<T>* cases, const int4* wor
 template <typename T>
 int stage_tma_occupancy(int pressure) {
     int nb = 0;
-    const size_t sm = stage_tma_smem_bytes<T>(pressure);
+    const size_t sm = stage_tma_smem_bytes<T>(pressure, 5);
     cudaError_t e = pressure
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma<T, true, 0>, TX * TY2, sm)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma<T, false, 0>, TX * TY2, sm);
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma<T, true, 5>, TX * TY2, sm)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma<T, false, 5>, TX * TY2, sm);
     return e == cudaSuccess && nb > 0 ? nb : 1;
 }
 
 template <typename T>
 cudaError_t launch_stage_tma(const StageArgsTMA<T>& A, int pressure, dim3 grid, cudaStream_t s) {
     const dim3 block(TX, TY2, 1);
-    const size_t sm = stage_tma_smem_bytes<T>(pressure);
+    const size_t sm = stage_tma_smem_bytes<T>(pressure, A.a.n);
 #define GMK_LAUNCH_N(PR)                                                              \
     switch (A.a.n) {                                                                  \
         case 0: k_stage_tma<T, PR, 0><<<grid, block, sm, s>>>(A); break;              \
@@ -676,7 +726,7 @@ cudaError_t launch_stage_tma(const StageArgsTMA<T>& A, int pressure, dim3 grid, 
 }
 
 #define GMK_INSTANTIATE_TMA(T)                                                                \
-    template size_t stage_tma_smem_bytes<T>(int);                                             \
+    template size_t stage_tma_smem_bytes<T>(int, int);                                             \
     template cudaError_t prepare_stage_tma<T>();                                              \
     template int stage_tma_occupancy<T>(int);                                                 \
     template cudaError_t launch_stage_tma<T>(const StageArgsTMA<T>&, int, dim3, cudaStream_t);                 \
