@@ -149,6 +149,23 @@ SIGNATURES = {
     "gm_batch_stop": (C.c_int, [VP, C.c_int]),
     "gm_batch_run": (C.c_int, [VP, C.c_int, C.c_double, C.c_int, C.c_int, P(GmBatchCase)]),
     "gm_batch_launch_count": (C.c_int64, [VP]),
+    "gm_nn_tc_gemm_check": (C.c_int, [VP, VP, VP, C.c_int, C.c_int, VP]),
+    "gm_nn_conv": (C.c_int, [VP, C.c_int, C.c_int, VP, C.c_int, C.c_int, VP, P(C.c_float), VP, C.c_int, C.c_int,
+                             VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                             VP, VP]),
+    "gm_nn_conv_wgrad": (C.c_int, [VP, C.c_int, C.c_int, VP, C.c_int, C.c_int, VP, C.c_int, C.c_int, P(C.c_float),
+                                   C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, VP, VP]),
+    "gm_nn_bias_grad": (C.c_int, [VP, C.c_int, C.c_int, C.c_longlong, P(C.c_float), VP]),
+    "gm_nn_pool": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, VP]),
+    "gm_nn_upsample": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, VP]),
+    "gm_nn_relu_bwd": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, C.c_longlong, VP]),
+    "gm_nn_mse": (C.c_int, [VP, C.c_int, P(C.c_float), VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                            P(C.c_float), VP]),
+    "gm_nn_adam": (C.c_int, [P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float),
+                             P(C.c_float), P(C.c_float), C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
+                             C.c_float, VP, C.c_int, C.c_int, VP, C.c_int, C.c_int, P(C.c_float), VP]),
+    "gm_nn_input": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, VP, C.c_int, VP]),
+    "gm_nn_zero": (C.c_int, [VP, C.c_size_t, VP]),
     "gm_device_count": (C.c_int, [P(C.c_int)]),
     "gm_set_device": (C.c_int, [C.c_int]),
     "gm_io_write_cuda_info": (C.c_int, [C.c_char_p, C.c_int, C.c_long]),

@@ -1,0 +1,644 @@
+// nn_kernels.cu -- kernels of the learned warm start: a 3-D U-Net mapping the
+// initial field B0 to a grid displacement x(X) - X.  Activations are BF16,
+// channels-last ([voxel][channel], voxel = x + nx (y + ny z)), viewed with a
+// channel stride so that a concatenation is two views into one buffer.  The
+// 3x3x3 convolutions (forward, input gradient, weight gradient) are implicit
+// GEMMs on the 5th-generation tensor cores with FP32 accumulation in tensor
+// memory (nn_tc.cuh); padding is periodic in x and y and zero in z, as the
+// relaxation's boundaries are.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "glemur.h"
+#include "gm_internal.h"
+#include "nn_tc.cuh"
+
+namespace gmnn {
+
+// ---- tensor-core GEMM check -------------------------------------------------
+
+// D[128 x N] = A[128 x K] . B[N x K]^T with BF16 operands (row-major in global
+// memory) and FP32 accumulation in tensor memory; one CTA of 128 threads.
+// status[0] is set to 1 when the completion wait gives up.
+__global__ void __launch_bounds__(128) k_tc_gemm(const __nv_bfloat16* __restrict__ A,
+                                                 const __nv_bfloat16* __restrict__ B, float* __restrict__ D, int N,
+                                                 int K, int* status) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    unsigned char* sA = sm;                               // 128 x K
+    unsigned char* sB = sm + 128 * K * 2;                 // N x K
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sB + N * K * 2);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int e = tid; e < 128 * K; e += 128) {
+        const int r = e / K, k = e % K;
+        *reinterpret_cast<__nv_bfloat16*>(sA + kmajor_off(r, k, K)) = A[e];
+    }
+    for (int e = tid; e < N * K; e += 128) {
+        const int r = e / K, k = e % K;
+        *reinterpret_cast<__nv_bfloat16*>(sB + kmajor_off(r, k, K)) = B[e];
+    }
+    if (tid == 0) mbar_init_tc(bar);
+    fence_async_smem();
+    uint32_t ncols = 32;
+    while ((int)ncols < N) ncols <<= 1;
+    if (warp == 0) tmem_alloc(tslot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tslot;
+    if (tid == 0) {
+        const uint32_t id = idesc_bf16(128, N);
+        for (int kk = 0; kk < K / 16; kk++) {
+            const uint64_t ad = smem_desc(sm_addr(sA) + kk * 256, 128, (uint32_t)K * 16);
+            const uint64_t bd = smem_desc(sm_addr(sB) + kk * 256, 128, (uint32_t)K * 16);
+            mma_bf16(tbase, ad, bd, id, kk > 0);
+        }
+        mma_commit(bar);
+    }
+    const bool ok = mbar_wait_tc(bar, 0);
+    tc_fence_after();
+    if (ok) {
+        for (int c = 0; c < N; c += 16) {
+            float v[16];
+            tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+#pragma unroll
+            for (int q = 0; q < 16; q++) D[(32 * warp + lane) * N + c + q] = v[q];
+        }
+    } else if (lane == 0) {
+        atomicExch(status, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_free(tbase, ncols);
+}
+
+// ---- convolution: forward and input gradient --------------------------------
+
+struct ConvArgs {
+    const __nv_bfloat16* in1; int ld1, c1;   // first input view (channels 0 .. c1-1)
+    const __nv_bfloat16* in2; int ld2, c2;   // optional second view (channels c1 .. c1+c2-1)
+    const __nv_bfloat16* W;                  // [27][Np][Kc] BF16: rows = output channels, K = input channels
+    const float* bias;                       // [Np] or null
+    __nv_bfloat16* out; int ldo, co;         // output view (co channels written)
+    const __nv_bfloat16* mask; int ldm;      // optional: out *= (mask > 0), mask has co channels
+    int relu;
+    int nx, ny, nz, xper, yper;
+    int Kc, Np;                              // padded input channels (multiple of 16), padded outputs
+    int* status;
+};
+
+__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// 16 bytes (8 channels starting at channel c) of voxel (i, j, k) of the
+// concatenated input, zero outside the z range and beyond the channels.
+__device__ __forceinline__ uint4 gather8(const ConvArgs& a, int i, int j, int k, int c) {
+    uint4 z = make_uint4(0, 0, 0, 0);
+    if (k < 0 || k >= a.nz) return z;
+    if (!a.xper && (i < 0 || i >= a.nx)) return z;
+    if (!a.yper && (j < 0 || j >= a.ny)) return z;
+    i = wrap(i, a.nx);
+    j = wrap(j, a.ny);
+    const long long v = (long long)i + (long long)a.nx * (j + (long long)a.ny * k);
+    if (c < a.c1) return *reinterpret_cast<const uint4*>(a.in1 + v * a.ld1 + c);
+    c -= a.c1;
+    if (c < a.c2) return *reinterpret_cast<const uint4*>(a.in2 + v * a.ld2 + c);
+    return z;
+}
+
+// One CTA: 128 consecutive voxels x all Np output channels, accumulated over
+// the 27 taps.  The A tile (128 voxels x Kc input channels at the tap's
+// offset) and the tap's B tile (Np x Kc weights) are gathered into one of two
+// shared-memory stages while the tensor cores work on the other.
+__global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    const int Kc = a.Kc, Np = a.Np;
+    const int aBytes = 128 * Kc * 2, bBytes = Np * Kc * 2;
+    unsigned char* stA[2] = {sm, sm + aBytes};
+    unsigned char* stB[2] = {sm + 2 * aBytes, sm + 2 * aBytes + bBytes};
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * aBytes + 2 * bBytes);   // 2 stages
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long V = (long long)a.nx * a.ny * a.nz;
+    const long long v = (long long)blockIdx.x * 128 + tid;
+    const bool valid = v < V;
+    const int vi = valid ? (int)(v % a.nx) : 0;
+    const int vj = valid ? (int)((v / a.nx) % a.ny) : 0;
+    const int vk = valid ? (int)(v / ((long long)a.nx * a.ny)) : 0;
+    uint32_t ncols = 32;
+    while ((int)ncols < Np) ncols <<= 1;
+    if (tid == 0) {
+        mbar_init_tc(&bars[0]);
+        mbar_init_tc(&bars[1]);
+    }
+    if (warp == 0) tmem_alloc(tslot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tslot;
+    const uint32_t id = idesc_bf16(128, Np);
+    uint32_t ph[2] = {0, 0};
+    bool ok = true;
+    for (int t = 0; t < 27; t++) {
+        const int s = t & 1;
+        // the MMAs of tap t-2 read this stage: wait for them
+        if (t >= 2) {
+            if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
+            ph[s] ^= 1;
+        }
+        const int dk = t / 9 - 1, dj = (t / 3) % 3 - 1, di = t % 3 - 1;
+        // A: row tid = this thread's voxel, Kc channels in 16-byte chunks
+        for (int c = 0; c < Kc; c += 8) {
+            const uint4 q = valid ? gather8(a, vi + di, vj + dj, vk + dk, c) : make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4*>(stA[s] + kmajor_off(tid, c, Kc)) = q;
+        }
+        // B: the tap's Np x Kc weights
+        const __nv_bfloat16* Wt = a.W + (size_t)t * Np * Kc;
+        for (int e = tid; e < Np * Kc / 8; e += 128) {
+            const int r = e / (Kc / 8), c = (e % (Kc / 8)) * 8;
+            *reinterpret_cast<uint4*>(stB[s] + kmajor_off(r, c, Kc)) =
+                *reinterpret_cast<const uint4*>(Wt + (size_t)r * Kc + c);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            for (int kk = 0; kk < Kc / 16; kk++) {
+                const uint64_t ad = smem_desc(sm_addr(stA[s]) + kk * 256, 128, (uint32_t)Kc * 16);
+                const uint64_t bd = smem_desc(sm_addr(stB[s]) + kk * 256, 128, (uint32_t)Kc * 16);
+                mma_bf16(tbase, ad, bd, id, t > 0 || kk > 0);
+            }
+            mma_commit(&bars[s]);
+        }
+    }
+    // the commits of taps 26 (stage 0) and 25 (stage 1) are still unwaited
+    if (!mbar_wait_tc(&bars[26 & 1], ph[26 & 1])) ok = false;
+    ph[26 & 1] ^= 1;
+    if (!mbar_wait_tc(&bars[25 & 1], ph[25 & 1])) ok = false;
+    tc_fence_after();
+    if (ok) {
+        for (int c0 = 0; c0 < Np; c0 += 16) {
+            float acc[16];
+            tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, acc);
+            if (valid) {
+                const long long vv = v;
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int c = c0 + q;
+                    if (c >= a.co) break;
+                    float y = acc[q] + (a.bias ? a.bias[c] : 0.f);
+                    if (a.relu) y = fmaxf(y, 0.f);
+                    if (a.mask && !(__bfloat162float(a.mask[vv * a.ldm + c]) > 0.f)) y = 0.f;
+                    a.out[vv * a.ldo + c] = __float2bfloat16_rn(y);
+                }
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(a.status, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_free(tbase, ncols);
+}
+
+// ---- convolution: weight gradient --------------------------------------------
+
+struct WgradArgs {
+    const __nv_bfloat16* dout; int ldd, co;  // upstream gradient (co channels)
+    const __nv_bfloat16* in1; int ld1, c1;   // forward input views
+    const __nv_bfloat16* in2; int ld2, c2;
+    float* dW;                               // [27][co][ci] FP32, accumulated with atomics
+    int ci;                                  // input channels of the weights (<= c1 + c2)
+    int nx, ny, nz, xper, yper;
+    int Kin;                                 // padded input channels (multiple of 16, <= 256)
+    int vchunk;                              // voxels per CTA (multiple of 64)
+    int* status;
+};
+
+// dW[t][o][i] += sum_v dout[v][o] in[v + off(t)][i] over a voxel chunk, on the
+// tensor cores: M = 128 rows (output channels, zero-padded), N = Kin input
+// channels, K = voxels in steps of 64.  grid = (chunks, 27).
+__global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    constexpr int KV = 64;                                   // voxels per K step
+    const int Kin = a.Kin;
+    const int aBytes = 128 * KV * 2, bBytes = Kin * KV * 2;
+    unsigned char* stA[2] = {sm, sm + aBytes};
+    unsigned char* stB[2] = {sm + 2 * aBytes, sm + 2 * aBytes + bBytes};
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * aBytes + 2 * bBytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int t = blockIdx.y;
+    const int dk = t / 9 - 1, dj = (t / 3) % 3 - 1, di = t % 3 - 1;
+    const long long V = (long long)a.nx * a.ny * a.nz;
+    const long long v0 = (long long)blockIdx.x * a.vchunk;
+    const int nsteps = (int)((min(V - v0, (long long)a.vchunk) + KV - 1) / KV);
+    uint32_t ncols = 32;
+    while ((int)ncols < Kin) ncols <<= 1;
+    if (tid == 0) {
+        mbar_init_tc(&bars[0]);
+        mbar_init_tc(&bars[1]);
+    }
+    if (warp == 0) tmem_alloc(tslot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tslot;
+    const uint32_t id = idesc_bf16(128, Kin);
+    uint32_t ph[2] = {0, 0};
+    bool ok = true;
+    for (int st = 0; st < nsteps; st++) {
+        const int s = st & 1;
+        if (st >= 2) {
+            if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
+            ph[s] ^= 1;
+        }
+        // voxel rows of this step: thread pairs split the 64 voxels
+        const int r = tid & 63, half = tid >> 6;
+        const long long v = v0 + (long long)st * KV + r;
+        const bool valid = v < V && v - v0 < a.vchunk;
+        int vi = 0, vj = 0, vk = 0;
+        if (valid) {
+            vi = (int)(v % a.nx);
+            vj = (int)((v / a.nx) % a.ny);
+            vk = (int)(v / ((long long)a.nx * a.ny));
+        }
+        // A[o][r] = dout[v][o], o < 128 (zero beyond co): half 0 writes o < 64, half 1 o >= 64
+        for (int o = half * 64; o < half * 64 + 64; o++) {
+            __nv_bfloat16 x = __float2bfloat16_rn(0.f);
+            if (valid && o < a.co) x = a.dout[v * a.ldd + o];
+            *reinterpret_cast<__nv_bfloat16*>(stA[s] + kmajor_off(o, r, KV)) = x;
+        }
+        // B[i][r] = in[v + off][i]
+        ConvArgs g;
+        g.in1 = a.in1; g.ld1 = a.ld1; g.c1 = a.c1; g.in2 = a.in2; g.ld2 = a.ld2; g.c2 = a.c2;
+        g.nx = a.nx; g.ny = a.ny; g.nz = a.nz; g.xper = a.xper; g.yper = a.yper;
+        for (int c = half * 8; c < Kin; c += 16) {
+            uint4 q = valid ? gather8(g, vi + di, vj + dj, vk + dk, c) : make_uint4(0, 0, 0, 0);
+            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                *reinterpret_cast<__nv_bfloat16*>(stB[s] + kmajor_off(c + u, r, KV)) = e[u];
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            for (int kk = 0; kk < KV / 16; kk++) {
+                const uint64_t ad = smem_desc(sm_addr(stA[s]) + kk * 256, 128, (uint32_t)KV * 16);
+                const uint64_t bd = smem_desc(sm_addr(stB[s]) + kk * 256, 128, (uint32_t)KV * 16);
+                mma_bf16(tbase, ad, bd, id, st > 0 || kk > 0);
+            }
+            mma_commit(&bars[s]);
+        }
+    }
+    if (nsteps >= 1) {
+        const int sl = (nsteps - 1) & 1;
+        if (!mbar_wait_tc(&bars[sl], ph[sl])) ok = false;
+        ph[sl] ^= 1;
+    }
+    if (nsteps >= 2) {
+        const int sp = (nsteps - 2) & 1;
+        if (!mbar_wait_tc(&bars[sp], ph[sp])) ok = false;
+    }
+    tc_fence_after();
+    const int o = 32 * warp + lane;                      // this thread's row = output channel
+    if (ok && nsteps > 0) {
+        for (int c0 = 0; c0 < Kin; c0 += 16) {
+            float acc[16];
+            tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, acc);
+            if (o < a.co) {
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int i = c0 + q;
+                    if (i < a.ci) atomicAdd(&a.dW[((size_t)t * a.co + o) * a.ci + i], acc[q]);
+                }
+            }
+        }
+    } else if (!ok && tid == 0) {
+        atomicExch(a.status, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_free(tbase, ncols);
+}
+
+// ---- elementwise and resampling kernels ---------------------------------------
+
+// Sum over voxels of an upstream gradient per channel (bias gradient).
+__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ d, int ld, int c, long long V, float* __restrict__ db) {
+    __shared__ float red[256];
+    const int ch = blockIdx.y;
+    float s = 0.f;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+        s += __bfloat162float(d[v * ld + ch]);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(&db[ch], red[0]);
+}
+
+// 2x2x2 average pooling (forward) and its adjoint (backward: each child gets
+// 1/8 of the parent's gradient).  Fine grid (nx, ny, nz), coarse (nx/2, ...).
+__global__ void k_pool(const __nv_bfloat16* __restrict__ in, int ldi, __nv_bfloat16* __restrict__ out, int ldo, int c,
+                       int nx, int ny, int nz, int backward, int accumulate) {
+    const int cx = nx / 2, cy = ny / 2, cz = nz / 2;
+    const long long Vc = (long long)cx * cy * cz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < Vc * c; q += (long long)gridDim.x * blockDim.x) {
+        const int ch = (int)(q % c);
+        const long long vc = q / c;
+        const int i = (int)(vc % cx), j = (int)((vc / cx) % cy), k = (int)(vc / ((long long)cx * cy));
+        if (!backward) {
+            float s = 0.f;
+            for (int d = 0; d < 8; d++) {
+                const long long vf = (2 * i + (d & 1)) + (long long)nx * ((2 * j + ((d >> 1) & 1)) + (long long)ny * (2 * k + (d >> 2)));
+                s += __bfloat162float(in[vf * ldi + ch]);
+            }
+            out[vc * ldo + ch] = __float2bfloat16_rn(0.125f * s);
+        } else {
+            // in = coarse gradient, out = fine gradient
+            const float g = 0.125f * __bfloat162float(in[vc * ldi + ch]);
+            for (int d = 0; d < 8; d++) {
+                const long long vf = (2 * i + (d & 1)) + (long long)nx * ((2 * j + ((d >> 1) & 1)) + (long long)ny * (2 * k + (d >> 2)));
+                const float o = accumulate ? __bfloat162float(out[vf * ldo + ch]) : 0.f;
+                out[vf * ldo + ch] = __float2bfloat16_rn(o + g);
+            }
+        }
+    }
+}
+
+// Nearest-neighbour 2x upsampling (forward) and its adjoint (backward: the sum
+// of the 8 children).  Coarse grid (nx/2, ...), fine (nx, ny, nz).
+__global__ void k_upsample(const __nv_bfloat16* __restrict__ in, int ldi, __nv_bfloat16* __restrict__ out, int ldo,
+                           int c, int nx, int ny, int nz, int backward) {
+    const int cx = nx / 2, cy = ny / 2, cz = nz / 2;
+    const long long Vc = (long long)cx * cy * cz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < Vc * c; q += (long long)gridDim.x * blockDim.x) {
+        const int ch = (int)(q % c);
+        const long long vc = q / c;
+        const int i = (int)(vc % cx), j = (int)((vc / cx) % cy), k = (int)(vc / ((long long)cx * cy));
+        if (!backward) {
+            const __nv_bfloat16 x = in[vc * ldi + ch];
+            for (int d = 0; d < 8; d++) {
+                const long long vf = (2 * i + (d & 1)) + (long long)nx * ((2 * j + ((d >> 1) & 1)) + (long long)ny * (2 * k + (d >> 2)));
+                out[vf * ldo + ch] = x;
+            }
+        } else {
+            // in = fine gradient, out = coarse gradient
+            float s = 0.f;
+            for (int d = 0; d < 8; d++) {
+                const long long vf = (2 * i + (d & 1)) + (long long)nx * ((2 * j + ((d >> 1) & 1)) + (long long)ny * (2 * k + (d >> 2)));
+                s += __bfloat162float(in[vf * ldi + ch]);
+            }
+            out[vc * ldo + ch] = __float2bfloat16_rn(s);
+        }
+    }
+}
+
+// d *= (y > 0): the gradient through a ReLU from its output.
+__global__ void k_relu_bwd(__nv_bfloat16* __restrict__ d, int ldd, const __nv_bfloat16* __restrict__ y, int ldy, int c,
+                           long long V) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < V * c; q += (long long)gridDim.x * blockDim.x) {
+        const long long v = q / c;
+        const int ch = (int)(q % c);
+        if (!(__bfloat162float(y[v * ldy + ch]) > 0.f)) d[v * ldd + ch] = __float2bfloat16_rn(0.f);
+    }
+}
+
+// Masked mean-square error of the 3 output channels against the target
+// (FP32, [V][3]); planes k = 0 and nz-1 are excluded (their displacement is
+// imposed to be zero).  Writes the gradient (BF16) and adds the loss sum.
+__global__ void k_mse(const __nv_bfloat16* __restrict__ y, int ldy, const float* __restrict__ tgt,
+                      __nv_bfloat16* __restrict__ dy, int lddy, int nx, int ny, int nz, float scale,
+                      float* __restrict__ loss) {
+    __shared__ float red[256];
+    const long long V = (long long)nx * ny * nz;
+    float s = 0.f;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(v / ((long long)nx * ny));
+        const bool in = k > 0 && k < nz - 1;
+        for (int c = 0; c < 3; c++) {
+            const float e = in ? __bfloat162float(y[v * ldy + c]) - tgt[3 * v + c] : 0.f;
+            s += e * e;
+            dy[v * lddy + c] = __float2bfloat16_rn(2.f * scale * e);
+        }
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, red[0] * scale);
+}
+
+// Adam on FP32 master weights W[27][co][ci] and b[co]; then the BF16 operand
+// layouts: Wf[27][Npo][Kci] (forward: rows = outputs) and Wb[27][Npi][Kco]
+// (input gradient: taps flipped, rows = inputs).
+__global__ void k_adam(float* __restrict__ W, float* __restrict__ mW, float* __restrict__ vW,
+                       const float* __restrict__ gW, float* __restrict__ b, float* __restrict__ mb,
+                       float* __restrict__ vb, const float* __restrict__ gb, int co, int ci, float lr, float b1,
+                       float b2, float c1, float c2, float eps, __nv_bfloat16* __restrict__ Wf, int Npo, int Kci,
+                       __nv_bfloat16* __restrict__ Wb, int Npi, int Kco, float* __restrict__ bpad, int step) {
+    const long long n = 27LL * co * ci;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n + co; q += (long long)gridDim.x * blockDim.x) {
+        if (q < n) {
+            float w = W[q];
+            if (step) {
+                const float g = gW[q];
+                const float m = b1 * mW[q] + (1 - b1) * g, v = b2 * vW[q] + (1 - b2) * g * g;
+                mW[q] = m;
+                vW[q] = v;
+                w -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+                W[q] = w;
+            }
+            const int t = (int)(q / ((long long)co * ci)), o = (int)((q / ci) % co), i = (int)(q % ci);
+            const __nv_bfloat16 wb = __float2bfloat16_rn(w);
+            Wf[((size_t)t * Npo + o) * Kci + i] = wb;
+            Wb[((size_t)(26 - t) * Npi + i) * Kco + o] = wb;
+        } else {
+            const int o = (int)(q - n);
+            float x = b[o];
+            if (step) {
+                const float g = gb[o];
+                const float m = b1 * mb[o] + (1 - b1) * g, v = b2 * vb[o] + (1 - b2) * g * g;
+                mb[o] = m;
+                vb[o] = v;
+                x -= lr * (m / c1) / (sqrtf(v / c2) + eps);
+                b[o] = x;
+            }
+            bpad[o] = x;
+        }
+    }
+}
+
+// Input channels (B0x, B0y, B0z - 1) of the inner points, from the ghosted
+// AoS B0 of the reference layout (REAL T); ld channels, the rest zero.
+template <typename T>
+__global__ void k_input(const T* __restrict__ B0, int nx, int ny, int nz, __nv_bfloat16* __restrict__ x, int ld) {
+    const long long V = (long long)nx * ny * nz;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long long)nx * ny));
+        const long long g = (long long)(i + 1) + (long long)(nx + 2) * ((j + 1) + (long long)(ny + 2) * (k + 1));
+        for (int c = 0; c < ld; c++) {
+            float val = 0.f;
+            if (c < 3) val = (float)B0[3 * g + c] - (c == 2 ? 1.f : 0.f);
+            x[v * ld + c] = __float2bfloat16_rn(val);
+        }
+    }
+}
+
+static unsigned nb(long long n) {
+    long long b = (n + 255) / 256;
+    return (unsigned)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
+}
+
+}  // namespace gmnn
+
+using gmnn::ConvArgs;
+using gmnn::WgradArgs;
+
+extern "C" {
+
+int gm_nn_tc_gemm_check(const void* A, const void* B, float* D, int N, int K, int* status) {
+    if (!A || !B || !D || !status) return gm::fail(GM_EPARAM, "gm_nn_tc_gemm_check: null argument");
+    if (N < 16 || N > 256 || N % 16 || K < 16 || K > 256 || K % 16)
+        return gm::fail(GM_EPARAM, "gm_nn_tc_gemm_check: N and K must be multiples of 16 in [16, 256]");
+    const size_t smem = (size_t)(128 + N) * K * 2 + 16;
+    cudaError_t e = cudaFuncSetAttribute(gmnn::k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+    gmnn::k_tc_gemm<<<1, 128, smem>>>((const __nv_bfloat16*)A, (const __nv_bfloat16*)B, D, N, K, status);
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("k_tc_gemm: ") + cudaGetErrorString(e));
+    return GM_OK;
+}
+
+static int check_view_align(const void* p, int ld, const char* what) {
+    if (p && ((reinterpret_cast<uintptr_t>(p) & 15) || (ld % 8)))
+        return gm::fail(GM_EPARAM, std::string(what) + ": views must start on 16 bytes with a channel stride that is a multiple of 8");
+    return GM_OK;
+}
+
+int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c2, const void* W, const float* bias,
+               void* out, int ldo, int co, const void* mask, int ldm, int relu, int nx, int ny, int nz, int xper,
+               int yper, int Kc, int Np, int* status, void* stream) {
+    if (!in1 || !W || !out || !status) return gm::fail(GM_EPARAM, "gm_nn_conv: null argument");
+    if (Kc % 16 || Kc < 16 || Kc > 256 || Np % 16 || Np < 16 || Np > 256 || c1 + (in2 ? c2 : 0) > Kc || co > Np ||
+        c1 % 8 || (size_t)2 * (128 + Np) * Kc * 2 + 32 > 200 * 1024)
+        return gm::fail(GM_EPARAM, "gm_nn_conv: channel counts out of range");
+    int rc;
+    if ((rc = check_view_align(in1, ld1, "gm_nn_conv in1")) || (rc = check_view_align(in2, ld2, "gm_nn_conv in2")))
+        return rc;
+    ConvArgs a;
+    a.in1 = (const __nv_bfloat16*)in1; a.ld1 = ld1; a.c1 = c1;
+    a.in2 = (const __nv_bfloat16*)in2; a.ld2 = ld2; a.c2 = in2 ? c2 : 0;
+    a.W = (const __nv_bfloat16*)W; a.bias = bias;
+    a.out = (__nv_bfloat16*)out; a.ldo = ldo; a.co = co;
+    a.mask = (const __nv_bfloat16*)mask; a.ldm = ldm; a.relu = relu;
+    a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper; a.Kc = Kc; a.Np = Np; a.status = status;
+    const size_t smem = (size_t)2 * (128 + Np) * Kc * 2 + 32;
+    cudaError_t e = cudaFuncSetAttribute(gmnn::k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+    const long long V = (long long)nx * ny * nz;
+    gmnn::k_conv<<<(unsigned)((V + 127) / 128), 128, smem, (cudaStream_t)stream>>>(a);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, std::string("k_conv: ") + cudaGetErrorString(e));
+}
+
+int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1, int c1, const void* in2, int ld2,
+                     int c2, float* dW, int ci, int nx, int ny, int nz, int xper, int yper, int Kin, int vchunk,
+                     int* status, void* stream) {
+    if (!dout || !in1 || !dW || !status) return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: null argument");
+    if (Kin % 16 || Kin < 16 || Kin > 256 || c1 + (in2 ? c2 : 0) > Kin || ci > c1 + (in2 ? c2 : 0) || ci < 1 ||
+        co > 128 || co < 1 || vchunk % 64 || vchunk < 64 || c1 % 8)
+        return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: channel counts or chunk out of range");
+    int rc;
+    if ((rc = check_view_align(in1, ld1, "gm_nn_conv_wgrad in1")) || (rc = check_view_align(in2, ld2, "gm_nn_conv_wgrad in2")))
+        return rc;
+    WgradArgs a;
+    a.dout = (const __nv_bfloat16*)dout; a.ldd = ldd; a.co = co;
+    a.in1 = (const __nv_bfloat16*)in1; a.ld1 = ld1; a.c1 = c1;
+    a.in2 = (const __nv_bfloat16*)in2; a.ld2 = ld2; a.c2 = in2 ? c2 : 0;
+    a.dW = dW; a.ci = ci; a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper; a.Kin = Kin; a.vchunk = vchunk;
+    a.status = status;
+    const size_t smem = (size_t)2 * (128 + Kin) * 64 * 2 + 32;
+    cudaError_t e = cudaFuncSetAttribute(gmnn::k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+    const long long V = (long long)nx * ny * nz;
+    const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), 27);
+    gmnn::k_conv_wgrad<<<grid, 128, smem, (cudaStream_t)stream>>>(a);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, std::string("k_conv_wgrad: ") + cudaGetErrorString(e));
+}
+
+int gm_nn_bias_grad(const void* d, int ld, int c, long long V, float* db, void* stream) {
+    gmnn::k_bias_grad<<<dim3(gmnn::nb(V) > 64 ? 64 : gmnn::nb(V), c), 256, 0, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16*)d, ld, c, V, db);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_bias_grad");
+}
+
+int gm_nn_pool(const void* in, int ldi, void* out, int ldo, int c, int nx, int ny, int nz, int backward,
+               int accumulate, void* stream) {
+    if (nx % 2 || ny % 2 || nz % 2) return gm::fail(GM_EPARAM, "gm_nn_pool: grid sizes must be even");
+    const long long n = (long long)(nx / 2) * (ny / 2) * (nz / 2) * c;
+    gmnn::k_pool<<<gmnn::nb(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)in, ldi, (__nv_bfloat16*)out,
+                                                                 ldo, c, nx, ny, nz, backward, accumulate);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_pool");
+}
+
+int gm_nn_upsample(const void* in, int ldi, void* out, int ldo, int c, int nx, int ny, int nz, int backward,
+                   void* stream) {
+    if (nx % 2 || ny % 2 || nz % 2) return gm::fail(GM_EPARAM, "gm_nn_upsample: grid sizes must be even");
+    const long long n = (long long)(nx / 2) * (ny / 2) * (nz / 2) * c;
+    gmnn::k_upsample<<<gmnn::nb(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)in, ldi,
+                                                                     (__nv_bfloat16*)out, ldo, c, nx, ny, nz, backward);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_upsample");
+}
+
+int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, void* stream) {
+    const long long V = (long long)nx * ny * nz;
+    if (precision == 32)
+        gmnn::k_input<float><<<gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>((const float*)B0, nx, ny, nz,
+                                                                              (__nv_bfloat16*)x, ld);
+    else
+        gmnn::k_input<double><<<gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>((const double*)B0, nx, ny, nz,
+                                                                               (__nv_bfloat16*)x, ld);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_input");
+}
+
+int gm_nn_zero(void* p, size_t bytes, void* stream) {
+    const cudaError_t e = cudaMemsetAsync(p, 0, bytes, (cudaStream_t)stream);
+    return e == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+}
+
+int gm_nn_relu_bwd(void* d, int ldd, const void* y, int ldy, int c, long long V, void* stream) {
+    gmnn::k_relu_bwd<<<gmnn::nb(V * c), 256, 0, (cudaStream_t)stream>>>((__nv_bfloat16*)d, ldd,
+                                                                         (const __nv_bfloat16*)y, ldy, c, V);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_relu_bwd");
+}
+
+int gm_nn_mse(const void* y, int ldy, const float* tgt, void* dy, int lddy, int nx, int ny, int nz, float scale,
+              float* loss, void* stream) {
+    const long long V = (long long)nx * ny * nz;
+    gmnn::k_mse<<<gmnn::nb(V) > 256 ? 256 : gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16*)y, ldy, tgt, (__nv_bfloat16*)dy, lddy, nx, ny, nz, scale, loss);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_mse");
+}
+
+int gm_nn_adam(float* W, float* mW, float* vW, const float* gW, float* b, float* mb, float* vb, const float* gb, int co,
+               int ci, float lr, float b1, float b2, int t, float eps, void* Wf, int Npo, int Kci, void* Wb, int Npi,
+               int Kco, float* bpad, void* stream) {
+    const float c1 = t > 0 ? 1.f - powf(b1, (float)t) : 1.f, c2 = t > 0 ? 1.f - powf(b2, (float)t) : 1.f;
+    gmnn::k_adam<<<gmnn::nb(27LL * co * ci + co), 256, 0, (cudaStream_t)stream>>>(
+        W, mW, vW, gW, b, mb, vb, gb, co, ci, lr, b1, b2, c1, c2, eps, (__nv_bfloat16*)Wf, Npo, Kci,
+        (__nv_bfloat16*)Wb, Npi, Kco, bpad, t > 0 ? 1 : 0);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_adam");
+}
+
+}  // extern "C"

@@ -340,6 +340,64 @@ int gm_batch_stop(gm_batch* b, int c);
 int gm_batch_run(gm_batch* b, int nCycle, double residual, int pointwise, int checkEvery, gm_batch_case* out);
 int64_t gm_batch_launch_count(const gm_batch* b);
 
+/* ---- learned warm start (no counterpart in the reference) ---------------- */
+
+/* Check of the tensor-core MMA core: D[128 x N] = A[128 x K] . B[N x K]^T
+ * with BF16 operands (DEVICE arrays, row-major) and FP32 accumulation in
+ * tensor memory; N, K multiples of 16 in [16, 256].  *status (device int) is
+ * set to 1 if the completion wait gave up.  Synchronises the device. */
+int gm_nn_tc_gemm_check(const void* A, const void* B, float* D, int N, int K, int* status);
+
+/* The network's layers (glemur_gb300/warmstart.py drives them).  Activations
+ * are DEVICE arrays of BF16, channels-last (voxel v = x + nx (y + ny z)),
+ * passed as views: a pointer (16-byte aligned) and a channel stride ld (a
+ * multiple of 8).  Grids are periodic in x / y when xper / yper, zero-padded
+ * in z.  All calls enqueue on `stream` (a cudaStream_t) and do not
+ * synchronise; a tensor-core completion wait that gives up sets *status.
+ *
+ * gm_nn_conv: 3x3x3 convolution as an implicit GEMM on the tensor cores.
+ *   out[v][o] = sum_t sum_i in[v + off(t)][i] W[t][o][i] (+ bias[o]), ReLU if
+ *   relu, then times (mask[v][o] > 0) if mask; the input is the concatenation
+ *   of the views in1 (c1 channels, c1 a multiple of 8) and in2 (c2); W is
+ *   BF16 [27][Np][Kc] (Kc >= c1 + c2 and Np >= co multiples of 16, <= 256).
+ *   With W flipped in t and transposed it is the input gradient. */
+int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c2, const void* W, const float* bias,
+               void* out, int ldo, int co, const void* mask, int ldm, int relu, int nx, int ny, int nz, int xper,
+               int yper, int Kc, int Np, int* status, void* stream);
+/* dW[t][o][i] += sum_v dout[v][o] in[v + off(t)][i] (FP32, i < ci), on the
+ * tensor cores over voxel chunks of vchunk (a multiple of 64); Kin >= c1 + c2
+ * a multiple of 16 <= 256, co <= 128. */
+int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1, int c1, const void* in2, int ld2,
+                     int c2, float* dW, int ci, int nx, int ny, int nz, int xper, int yper, int Kin, int vchunk,
+                     int* status, void* stream);
+/* db[o] += sum_v d[v][o]. */
+int gm_nn_bias_grad(const void* d, int ld, int c, long long V, float* db, void* stream);
+/* 2x2x2 mean pooling of the fine grid (nx, ny, nz) and its adjoint
+ * (backward: the fine gradient from the coarse one, added when accumulate). */
+int gm_nn_pool(const void* in, int ldi, void* out, int ldo, int c, int nx, int ny, int nz, int backward,
+               int accumulate, void* stream);
+/* Nearest 2x upsampling to the fine grid (nx, ny, nz) and its adjoint. */
+int gm_nn_upsample(const void* in, int ldi, void* out, int ldo, int c, int nx, int ny, int nz, int backward,
+                   void* stream);
+/* d *= (y > 0). */
+int gm_nn_relu_bwd(void* d, int ldd, const void* y, int ldy, int c, long long V, void* stream);
+/* loss += scale sum (y - tgt)^2 over channels 0..2 and planes 1..nz-2;
+ * dy = 2 scale (y - tgt) there and 0 on the first and last planes; tgt FP32 [V][3]. */
+int gm_nn_mse(const void* y, int ldy, const float* tgt, void* dy, int lddy, int nx, int ny, int nz, float scale,
+              float* loss, void* stream);
+/* Adam step t (t = 0: no update) of FP32 W[27][co][ci], b[co] with their
+ * moments and gradients, then the BF16 operand layouts Wf[27][Npo][Kci]
+ * (forward) and Wb[27][Npi][Kco] (input gradient: taps flipped, transposed)
+ * and the padded bias. */
+int gm_nn_adam(float* W, float* mW, float* vW, const float* gW, float* b, float* mb, float* vb, const float* gb, int co,
+               int ci, float lr, float b1, float b2, int t, float eps, void* Wf, int Npo, int Kci, void* Wb, int Npi,
+               int Kco, float* bpad, void* stream);
+/* Network input from B0 on the device (reference layout, REAL of
+ * `precision`): channels (B0x, B0y, B0z - 1) of the inner points, ld channels. */
+int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, void* stream);
+/* Zero `bytes` bytes of device memory (cudaMemsetAsync). */
+int gm_nn_zero(void* p, size_t bytes, void* stream);
+
 /* Number of CUDA devices and selection of the device the calling thread
  * uses (the cudaGetDeviceCount / cudaSetDevice of src/main.cu:47-80). */
 int gm_device_count(int* n);

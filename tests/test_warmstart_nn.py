@@ -1,0 +1,152 @@
+"""The warm-start network: the CPU oracle of its forward and backward pass is
+pinned by finite differences, and the GPU kernels (tensor-core convolutions,
+pooling, upsampling, loss, Adam) are checked against that oracle on the same
+BF16-rounded weights and inputs."""
+import numpy as np
+import pytest
+
+from oracle import unet_oracle as uo
+from glemur_gb300.warmstart import LAYERS, n_params
+
+
+def rand_params(rng, scale=1.0):
+    return {n: (rng.normal(0, scale * np.sqrt(2.0 / (27 * ci)), (27, co, ci)), rng.normal(0, 0.05, co))
+            for n, ci, co, _ in LAYERS}
+
+
+def test_param_count():
+    assert 750_000 < n_params() < 850_000
+
+
+def test_oracle_gradients_by_finite_differences():
+    rng = np.random.default_rng(0)
+    P = rand_params(rng)
+    x = rng.normal(size=(8, 4, 4, 3))
+    tgt = rng.normal(size=(8, 4, 4, 3))
+    a = uo.forward(P, x)
+    L0, gy = uo.loss_grad(a["y"], tgt, 1.0)
+    G = uo.backward(P, x, a, gy)
+    h = 1e-6
+    for name in ("e0a", "e1b", "bb", "d1a", "d0a", "head"):
+        W, b = P[name]
+        for _ in range(3):
+            idx = tuple(rng.integers(s) for s in W.shape)
+            W[idx] += h
+            lp = uo.loss_grad(uo.forward(P, x)["y"], tgt, 1.0)[0]
+            W[idx] -= 2 * h
+            lm = uo.loss_grad(uo.forward(P, x)["y"], tgt, 1.0)[0]
+            W[idx] += h
+            fd = (lp - lm) / (2 * h)
+            assert fd == pytest.approx(G[name][0][idx], rel=1e-4, abs=1e-7), (name, idx)
+        o = rng.integers(b.shape[0])
+        b[o] += h
+        lp = uo.loss_grad(uo.forward(P, x)["y"], tgt, 1.0)[0]
+        b[o] -= 2 * h
+        lm = uo.loss_grad(uo.forward(P, x)["y"], tgt, 1.0)[0]
+        b[o] += h
+        assert (lp - lm) / (2 * h) == pytest.approx(G[name][1][o], rel=1e-4, abs=1e-7), (name, "bias")
+
+
+def bf16(a):
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def relerr(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def frob(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.gpu
+def test_gpu_network_matches_oracle():
+    import torch
+    from glemur_gb300.warmstart import UNet
+    nx, ny, nz = 8, 8, 16
+    net = UNet((nx, ny, nz), seed=3)
+    rng = np.random.default_rng(1)
+    for L in net.layers.values():
+        L.b.copy_(torch.from_numpy(rng.normal(0, 0.05, L.co).astype(np.float32)))
+    net.refresh_weights()
+    x = rng.normal(size=(nz, ny, nx, 3))
+    X0 = np.zeros((nx * ny * nz, 8), np.float32)
+    X0[:, :3] = x.reshape(-1, 3)
+    net.A["X0"].copy_(torch.from_numpy(X0).to(torch.bfloat16))
+    tgt = rng.normal(size=(nz, ny, nx, 3)).astype(np.float32)
+    tdev = torch.from_numpy(tgt.reshape(-1, 3)).cuda()
+    net.zero_grad()
+    y = net.forward()
+    scale = 1.0 / (nx * ny * nz * 3)
+    net.backward(tdev, scale)
+    torch.cuda.synchronize()
+    net.check_status()
+    # oracle on the BF16 weights and input the GPU used
+    P = {n: (bf16(W), b) for n, (W, b) in net.params_numpy().items()}
+    xb = bf16(x)
+    a = uo.forward(P, xb)
+    yg = y[:, :3].float().cpu().numpy().reshape(nz, ny, nx, 3)
+    assert relerr(yg, a["y"]) < 3e-2 and frob(yg, a["y"]) < 1.5e-2
+    loss, gy = uo.loss_grad(a["y"], tgt.astype(np.float64), scale)
+    assert float(net.loss_acc.item()) == pytest.approx(loss, rel=5e-2)
+    G = uo.backward(P, xb, a, gy)
+    g = net.grads_numpy()
+    # end to end: the GPU rounds every activation and gradient buffer to BF16
+    # (8-bit mantissa); through the 22 convolutions of the backward pass that
+    # leaves up to ~6 % (Frobenius) on the first layer's gradient
+    for name, _, _, _ in LAYERS:
+        for q, what in ((0, "W"), (1, "b")):
+            assert frob(g[name][q], G[name][q]) < 1e-1, (name, what, frob(g[name][q], G[name][q]))
+    # layer by layer: each weight / bias gradient against numpy on the GPU's
+    # own upstream gradient and input buffers (FP32 accumulation of BF16 products)
+    def buf(name, c0, c, lvl):
+        d = net.dims[lvl]
+        a_ = net.A[name][:, c0:c0 + c].float().cpu().numpy().astype(np.float64)
+        return a_.reshape(d[2], d[1], d[0], c)
+    pairs = {"head": (("dY", 0, 3, 0), ("D0b", 0, 24, 0)), "d0b": (("dD0b", 0, 24, 0), ("D0a", 0, 24, 0)),
+             "d0a": (("dD0a", 0, 24, 0), ("CAT0", 0, 72, 0)), "d1b": (("dD1b", 0, 48, 1), ("D1a", 0, 48, 1)),
+             "d1a": (("dD1a", 0, 48, 1), ("CAT1", 0, 144, 1)), "bb": (("dBb", 0, 96, 2), ("Ba", 0, 96, 2)),
+             "ba": (("dBa", 0, 96, 2), ("P2", 0, 48, 2)), "e1b": (("dCAT1", 96, 48, 1), ("E1a", 0, 48, 1)),
+             "e1a": (("dE1a", 0, 48, 1), ("P1", 0, 24, 1)), "e0b": (("dCAT0", 48, 24, 0), ("E0a", 0, 24, 0)),
+             "e0a": (("dE0a", 0, 24, 0), ("X0", 0, 3, 0))}
+    for name, (dspec, ispec) in pairs.items():
+        dpre, inp = buf(*dspec), buf(*ispec)
+        W = P[name][0]
+        _, dW, db = uo.conv_bwd(inp, W, dpre)
+        assert frob(g[name][0], dW) < 3e-3, (name, "W kernel", frob(g[name][0], dW))
+        assert frob(g[name][1], db) < 3e-3, (name, "b kernel", frob(g[name][1], db))
+    # forward convolutions and input gradients, layer by layer, from GPU buffers
+    fwd = {"e0b": ("E0a", 0, 24, 0, "CAT0", 48, 24), "d1a": ("CAT1", 0, 144, 1, "D1a", 0, 48),
+           "bb": ("Ba", 0, 96, 2, "Bb", 0, 96), "d0a": ("CAT0", 0, 72, 0, "D0a", 0, 24)}
+    for name, (iname, i0, ic, lvl, oname, o0, oc) in fwd.items():
+        ref = uo.relu(uo.conv(buf(iname, i0, ic, lvl), *P[name]))
+        assert frob(buf(oname, o0, oc, lvl), ref) < 1e-2, (name, "forward kernel")
+    # input gradient of d1a (the 144-channel concatenation), before the pool / ReLU updates
+    # of its skip part: the up part (channels 0..95) is untouched afterwards
+    dcat1 = uo.conv_bwd(buf("CAT1", 0, 144, 1), P["d1a"][0], buf("dD1a", 0, 48, 1))[0]
+    assert frob(buf("dCAT1", 0, 96, 1), dcat1[..., :96]) < 1e-2, "input-gradient kernel"
+
+
+@pytest.mark.gpu
+def test_gpu_adam_step_reduces_loss():
+    import torch
+    from glemur_gb300.warmstart import UNet
+    nx, ny, nz = 8, 8, 16
+    net = UNet((nx, ny, nz), seed=4)
+    rng = np.random.default_rng(2)
+    X0 = np.zeros((nx * ny * nz, 8), np.float32)
+    X0[:, :3] = rng.normal(size=(nx * ny * nz, 3))
+    net.A["X0"].copy_(torch.from_numpy(X0).to(torch.bfloat16))
+    tdev = torch.from_numpy(0.3 * rng.normal(size=(nx * ny * nz, 3)).astype(np.float32)).cuda()
+    scale = 1.0 / (nx * ny * nz * 3)
+    losses = []
+    for it in range(30):
+        net.zero_grad()
+        net.forward()
+        net.backward(tdev, scale)
+        losses.append(float(net.loss_acc.item()))
+        net.refresh_weights(lr=3e-3, step=True)
+    net.check_status()
+    assert losses[-1] < 0.5 * losses[0], losses
