@@ -8,6 +8,9 @@ the whole grid; the metric is cell-RK-stages/s = N x 6 x steps / time.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
   python bench.py --workload batch64 [--batch-residual R] [--batch-cycles C]
 
+--workload large times the 256x256x512 braid with k = +-1.2 and the
+pressure term with the p0(r) profile (the plain path of the large case).
+
 --workload batch64 runs the batched configuration instead: 64 seeded random
 braids of uneven sizes (seeds 1000..1063, drawn as configs.random_braid) in
 one persistent launch per RK stage, each case until its weighted force-free
@@ -41,20 +44,29 @@ BYTES_PER_CELL_STAGE = {32: 82, 64: 164}   # algorithmic: 20.5 REALs per cell an
 SHAPE = (128, 128, 256)
 
 
+WORKLOAD = "braid6"
+
+
 def workload_params(precision=32):
     from glemur_gb300 import configs
+    if WORKLOAD == "large":
+        return configs.braid6_large(256, 256, 512, precision=precision)
     p = configs.braid6(*SHAPE, precision=precision)
     return p
 
 
 def workload_config(p, extra=None):
+    name = (f"braid6 {p.nx}x{p.ny}x{p.nz}: six alternating twisted blobs, periodic x,y, line-tied z"
+            if WORKLOAD != "large" else
+            f"large {p.nx}x{p.ny}x{p.nz}: six-blob braid with k = +-1.2, pressure p0 = 0.1 (1 + 0.5 exp(-r^2/4))")
     c = {
-        "workload": f"braid6 {p.nx}x{p.ny}x{p.nz}: six alternating twisted blobs, periodic x,y, line-tied z",
+        "workload": name,
         "grid": [p.nx, p.ny, p.nz],
         "storage": "fp32" if p.precision == 32 else "fp64",
         "error_norm": "fp64" if p.errMode == 1 else "run precision",
         "step": "one attempted adaptive Cash-Karp RK step (6 stages + accept/reject)",
-        "l2": "working set ~0.5 GB > 129 MB L2 (inputs larger than L2, no flush)",
+        "l2": f"working set ~{p.nx * p.ny * p.nz * 117 * (p.precision // 8) / 1e9:.1f} GB > 129 MB L2 "
+              "(inputs larger than L2, no flush)",
         "parallelism": "replicas" if int(os.environ.get("WORLD_SIZE", "1")) > 1 else "single",
     }
     if extra:
@@ -137,7 +149,7 @@ def traffic_per_launch(p):
     if not f.exists():
         return None, None
     d = json.loads(f.read_text())
-    key = f"{p.nx}x{p.ny}x{p.nz}_fp{p.precision}"
+    key = f"{p.nx}x{p.ny}x{p.nz}_fp{p.precision}" + ("_pressure" if p.pressure else "")
     e = d.get(key)
     if not e:
         return None, None
@@ -404,12 +416,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--workload", default="braid6", choices=["braid6", "batch64"])
+    ap.add_argument("--workload", default="braid6", choices=["braid6", "batch64", "large"])
     ap.add_argument("--batch-residual", type=float, default=0.2)
     ap.add_argument("--batch-cycles", type=int, default=3000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    global WORKLOAD
+    WORKLOAD = args.workload
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch64":

@@ -1,0 +1,363 @@
+"""Training and evaluation of the learned warm start (glemur_gb300/warmstart.py).
+
+    python -m glemur_gb300.train_warmstart --train 256 --eval 32 --residual 0.15 \\
+        --minutes 6 --out weights.npz --report report.json
+
+1. Data: seeded random braids (configs.random_braid: 2-8 blobs, k ~ +-U[0.5,
+   1.2], a ~ U[1, 2], l ~ U[1.5, 3]) on a fixed 64x64x128 grid are relaxed by
+   the batched plain path (FP32) until the weighted force-free residual reaches
+   `--residual`; each converged case gives a pair (B0, (x - X) / spacing).
+   Cases whose grid folds first (dt <= dtMin) are left out.
+2. Training: the U-Net on those pairs with Adam (cosine learning-rate decay)
+   for a wall-clock budget, every step in this library's kernels.
+3. Evaluation on held-out seeds: for each case, the wall time from the
+   initial state to the residual target for the plain relaxation, and for the
+   warm start (network inference + grid build + validity check + relaxation),
+   the residual right after the warm start, whether it was accepted
+   (min Delta > 0) and min Delta over the run.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import BatchRelaxation, Relaxation, configs
+from .warmstart import UNet, n_params
+
+SHAPE = (64, 64, 128)
+TRAIN_SEED0 = 100000      # training seeds TRAIN_SEED0 + i
+EVAL_SEED0 = 900000       # held-out seeds EVAL_SEED0 + i
+
+
+def case(seed, shape=None):
+    return configs.random_braid(seed, shape=shape or SHAPE, precision=32)
+
+
+def displacement(p, xb, xb0):
+    """(x - X) / spacing at the inner points, float32 [V][3] in voxel order."""
+    sp = np.array([p.dx, p.dy, p.dz], dtype=np.float64)
+    d = (xb[1:-1, 1:-1, 1:-1].astype(np.float64) - xb0[1:-1, 1:-1, 1:-1].astype(np.float64)) / sp
+    return d.reshape(-1, 3).astype(np.float32)
+
+
+def relax_to_residual_batched(ps, residual, max_cycles, check_every=10):
+    """Relax cases together; returns (final grids, per-case outcomes)."""
+    b = BatchRelaxation(ps)
+    for c, p in enumerate(ps):
+        B0, xb = configs.init_state(p)
+        b.upload(c, xb, B0)
+    out = b.run(max_cycles, residual, pointwise=False, check_every=check_every)
+    grids = [b.download(c)["xb"] for c in range(len(ps))]
+    b.close()
+    return grids, out
+
+
+def make_data(seeds, residual, max_cycles, log=print):
+    """Training pairs from relaxed random braids (converged cases only)."""
+    import torch
+    data = []
+    t0 = time.perf_counter()
+    for i0 in range(0, len(seeds), 64):
+        ps = [case(s) for s in seeds[i0:i0 + 64]]
+        grids, out = relax_to_residual_batched(ps, residual, max_cycles)
+        for p, xb, o in zip(ps, grids, out):
+            if not o["converged"]:
+                continue
+            B0, xb0 = configs.init_state(p)
+            data.append((torch.from_numpy(B0).cuda(), torch.from_numpy(displacement(p, xb, xb0)).cuda()))
+        log(f"data: {len(data)} pairs from {i0 + len(ps)} braids, {time.perf_counter() - t0:.1f} s")
+    return data
+
+
+def train(net, data, minutes, lr=1e-3, batch=4, log=print):
+    """Adam with cosine decay over a wall-clock budget; returns the loss history."""
+    import torch
+    nx, ny, nz = net.shape
+    scale = 1.0 / (batch * nx * ny * nz * 3)
+    rng = np.random.default_rng(0)
+    hist = []
+    t0 = time.perf_counter()
+    budget = 60.0 * minutes
+    step = 0
+    while True:
+        order = rng.permutation(len(data))
+        for q in range(0, len(order) - batch + 1, batch):
+            el = time.perf_counter() - t0
+            if el > budget:
+                return hist
+            frac = el / budget
+            lr_t = 0.1 * lr + 0.9 * lr * 0.5 * (1 + np.cos(np.pi * frac))
+            net.zero_grad()
+            for k in order[q:q + batch]:
+                B0, tgt = data[k]
+                net.set_input_b0(B0, 32)
+                net.forward()
+                net.backward(tgt, scale)
+            net.refresh_weights(lr=lr_t, step=True)
+            step += 1
+            if step % 25 == 0:
+                hist.append((step, time.perf_counter() - t0, float(net.loss_acc.item())))
+                log(f"train: step {step} {hist[-1][1]:.0f} s loss {hist[-1][2]:.4e} lr {lr_t:.2e}")
+                net.check_status()
+
+
+def smooth_displacement(d, passes, xper=True, yper=True):
+    """`passes` 3x3x3 box-filter passes over a displacement [nz, ny, nx, 3]
+    (periodic in x / y, zero beyond the z range): removes the network's
+    grid-scale noise, which would otherwise show up as current."""
+    for _ in range(passes):
+        acc = np.zeros_like(d)
+        for dk in (-1, 0, 1):
+            if dk == 0:
+                dz = d
+            else:
+                dz = np.zeros_like(d)
+                if dk > 0:
+                    dz[:-dk] = d[dk:]
+                else:
+                    dz[-dk:] = d[:dk]
+            for dj in (-1, 0, 1):
+                for di in (-1, 0, 1):
+                    acc += np.roll(dz, (-dj, -di), axis=(1, 2))
+        d = acc / 27.0
+    return d
+
+
+def warm_grid(net, p, B0, smooth=0):
+    """The predicted grid in the reference layout (ghosted AoS): the identity
+    grid plus the network's displacement at the inner points (optionally
+    smoothed; zero on the first and last z-planes), periodic ghosts as shifted
+    images."""
+    import torch
+    nx, ny, nz = p.nx, p.ny, p.nz
+    net.set_input_b0(torch.from_numpy(B0).cuda(), 32)
+    y = net.forward()[:, :3].float().cpu().numpy().reshape(nz, ny, nx, 3)
+    if smooth:
+        y = smooth_displacement(y.astype(np.float64), smooth, bool(p.xPeri), bool(p.yPeri))
+    _, xb = configs.init_state(p)
+    xb = xb.astype(np.float64)
+    sp = np.array([p.dx, p.dy, p.dz])
+    d = y * sp
+    d[0] = 0.0
+    d[-1] = 0.0
+    xb[1:-1, 1:-1, 1:-1] += d
+    if p.xPeri:
+        xb[:, :, 0] = xb[:, :, nx]
+        xb[:, :, 0, 0] -= p.Lx + p.dx
+        xb[:, :, nx + 1] = xb[:, :, 1]
+        xb[:, :, nx + 1, 0] += p.Lx + p.dx
+    if p.yPeri:
+        xb[:, 0] = xb[:, ny]
+        xb[:, 0, :, 1] -= p.Ly + p.dy
+        xb[:, ny + 1] = xb[:, 1]
+        xb[:, ny + 1, :, 1] += p.Ly + p.dy
+    return xb.astype(np.float32)
+
+
+def time_to_residual(g, p, xb, B0, residual, max_attempts, check_every=50):
+    """Upload, then relax until the weighted residual is at most `residual`.
+    Returns (seconds, attempts, residual at start, min Delta seen, reached)."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.upload(xb, B0)
+    r = g.refresh()
+    r0, mind = r["residual"], r["minDetJac"]
+    att = 0
+    reached = r0 <= residual
+    while not reached and att < max_attempts:
+        g.steps_async(check_every)
+        s = g.state()
+        r = g.refresh()
+        att = s["nAttempted"]
+        mind = min(mind, r["minDetJac"])
+        if r["residual"] <= residual:
+            reached = True
+        elif s["status"] & 0x17:
+            break
+    return time.perf_counter() - t0, att, r0, mind, reached
+
+
+def evaluate(net, seeds, residual, max_attempts, log=print, smooth=0):
+    import torch
+    rows = []
+    for s in seeds:
+        p = case(s)
+        B0, xb0 = configs.init_state(p)
+        g = Relaxation(p)
+        g.upload(xb0, B0)
+        g.steps_async(2)       # capture the step graph outside the timed runs
+        g.state()
+        tp, ap, rp0, mdp, okp = time_to_residual(g, p, xb0, B0, residual, max_attempts)
+        d_true = displacement(p, g.download()["xb"], xb0)
+        # the warm start's own cost: inference, grid build, validity check
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xw = warm_grid(net, p, B0, smooth)
+        g.upload(xw, B0)
+        accepted = g.refresh()["minDetJac"] > 0
+        if not accepted:
+            xw = xb0
+        t_net = time.perf_counter() - t0
+        d_pred = displacement(p, xw, xb0)
+        rms_true = float(np.sqrt((d_true.astype(np.float64) ** 2).mean()))
+        rms_err = float(np.sqrt(((d_pred.astype(np.float64) - d_true) ** 2).mean()))
+        tw, aw, rw0, mdw, okw = time_to_residual(g, p, xw, B0, residual, max_attempts)
+        tw += t_net
+        g.close()
+        rows.append(dict(seed=s, plain_s=tp, plain_attempts=ap, plain_reached=okp, plain_res0=rp0, plain_minDet=mdp,
+                         warm_s=tw, warm_attempts=aw, warm_reached=okw, warm_res0=rw0, warm_minDet=mdw,
+                         accepted=bool(accepted), net_s=t_net, rms_disp=rms_true, rms_err=rms_err))
+        log(f"eval seed {s}: plain {tp:.2f} s ({ap} att, reached {okp}), warm {tw:.2f} s ({aw} att, res0 "
+            f"{rw0:.3f}, accepted {accepted}, reached {okw}), displacement rms {rms_true:.3f} err {rms_err:.3f}")
+    return rows
+
+
+def coarse_b0(p, B0, f):
+    """B0 averaged over f x f x f blocks of inner points, in a ghosted array
+    of the coarse grid (ghost values unused by the network input)."""
+    nx, ny, nz = p.nx // f, p.ny // f, p.nz // f
+    inner = B0[1:-1, 1:-1, 1:-1].astype(np.float64).reshape(nz, f, ny, f, nx, f, 3).mean(axis=(1, 3, 5))
+    out = np.zeros((nz + 2, ny + 2, nx + 2, 3), np.float32)
+    out[1:-1, 1:-1, 1:-1] = inner
+    return out
+
+
+def upsample_displacement(d, f, fine, per=(True, True)):
+    """Trilinear interpolation of a coarse displacement field [cz, cy, cx, 3]
+    (coarse voxel I centred on fine index f I + (f - 1) / 2) to the fine inner
+    points; periodic in x and y, clamped in z."""
+    nx, ny, nz = fine
+    out = d
+    for axis, n, periodic in ((2, nx, per[0]), (1, ny, per[1]), (0, nz, False)):
+        c = out.shape[axis]
+        pos = (np.arange(n) - (f - 1) / 2.0) / f
+        i0 = np.floor(pos).astype(int)
+        w = pos - i0
+        if periodic:
+            a, b = i0 % c, (i0 + 1) % c
+        else:
+            a, b = np.clip(i0, 0, c - 1), np.clip(i0 + 1, 0, c - 1)
+        shape = [1, 1, 1, 1]
+        shape[axis] = n
+        w = w.reshape(shape)
+        out = np.take(out, a, axis=axis) * (1 - w) + np.take(out, b, axis=axis) * w
+    return out
+
+
+def evaluate_large(weights, residual, max_attempts, factor=2, log=print):
+    """The large case (256x256x512, k = +-1.2, pressure with the p0 profile):
+    the network runs on a factor-x coarsened B0 and its displacement is
+    trilinearly upsampled; plain against warm start to the residual target."""
+    import torch
+    p = configs.braid6_large(256, 256, 512, precision=32)
+    B0, xb0 = configs.init_state(p)
+    g = Relaxation(p)
+    g.upload(xb0, B0)
+    g.steps_async(2)
+    g.state()
+    tp, ap, rp0, mdp, okp = time_to_residual(g, p, xb0, B0, residual, max_attempts)
+    cshape = (p.nx // factor, p.ny // factor, p.nz // factor)
+    net = UNet(cshape, seed=0)
+    net.load_state_dict(weights)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Bc = coarse_b0(p, B0, factor)
+    net.set_input_b0(torch.from_numpy(Bc).cuda(), 32)
+    y = net.forward()[:, :3].float().cpu().numpy().reshape(cshape[2], cshape[1], cshape[0], 3)
+    # coarse grid units -> physical -> fine inner points
+    sp_c = np.array([p.dx, p.dy, p.dz]) * factor
+    d = upsample_displacement(y * sp_c, factor, (p.nx, p.ny, p.nz))
+    d[0] = 0.0
+    d[-1] = 0.0
+    xw = xb0.astype(np.float64)
+    xw[1:-1, 1:-1, 1:-1] += d
+    nx, ny = p.nx, p.ny
+    xw[:, :, 0] = xw[:, :, nx]; xw[:, :, 0, 0] -= p.Lx + p.dx
+    xw[:, :, nx + 1] = xw[:, :, 1]; xw[:, :, nx + 1, 0] += p.Lx + p.dx
+    xw[:, 0] = xw[:, ny]; xw[:, 0, :, 1] -= p.Ly + p.dy
+    xw[:, ny + 1] = xw[:, 1]; xw[:, ny + 1, :, 1] += p.Ly + p.dy
+    xw = xw.astype(np.float32)
+    g.upload(xw, B0)
+    accepted = g.refresh()["minDetJac"] > 0
+    if not accepted:
+        xw = xb0
+    t_net = time.perf_counter() - t0
+    tw, aw, rw0, mdw, okw = time_to_residual(g, p, xw, B0, residual, max_attempts)
+    tw += t_net
+    g.close()
+    row = dict(shape=(p.nx, p.ny, p.nz), factor=factor, plain_s=tp, plain_attempts=ap, plain_reached=okp,
+               plain_res0=rp0, plain_minDet=mdp, warm_s=tw, warm_attempts=aw, warm_reached=okw, warm_res0=rw0,
+               warm_minDet=mdw, accepted=bool(accepted), net_s=t_net)
+    log(f"large: {row}")
+    return row
+
+
+def summarize(rows):
+    both = [r for r in rows if r["plain_reached"] and r["warm_reached"]]
+    sp = [r["plain_s"] / r["warm_s"] for r in both]
+    return dict(cases=len(rows), both_reached=len(both), accepted=sum(r["accepted"] for r in rows),
+                speedup_median=float(np.median(sp)) if sp else None,
+                speedup_total=float(sum(r["plain_s"] for r in both) / sum(r["warm_s"] for r in both)) if both else None,
+                plain_res0_median=float(np.median([r["plain_res0"] for r in rows])),
+                warm_res0_median=float(np.median([r["warm_res0"] for r in rows])),
+                min_delta_warm=float(min(r["warm_minDet"] for r in rows)),
+                rms_disp_median=float(np.median([r["rms_disp"] for r in rows])),
+                rms_err_median=float(np.median([r["rms_err"] for r in rows])))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=256)
+    ap.add_argument("--eval", type=int, default=32)
+    ap.add_argument("--residual", type=float, default=0.15)
+    ap.add_argument("--max-cycles", type=int, default=8000)
+    ap.add_argument("--minutes", type=float, default=6.0)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default="")
+    ap.add_argument("--report", default="")
+    ap.add_argument("--weights", default="", help="evaluate these weights instead of training")
+    ap.add_argument("--shape", default="64,64,128", help="grid (nx,ny,nz), each divisible by 4")
+    ap.add_argument("--large", action="store_true", help="also evaluate the 256x256x512 pressure case")
+    ap.add_argument("--smooth", default="0", help="comma-separated box-filter passes to evaluate")
+    a = ap.parse_args(argv)
+    global SHAPE
+    SHAPE = tuple(int(v) for v in a.shape.split(","))
+    log = lambda m: print(m, flush=True)
+    net = UNet(SHAPE, seed=7)
+    log(f"U-Net: {n_params()} parameters")
+    report = dict(shape=SHAPE, residual=a.residual, params=n_params())
+    if a.weights:
+        net.load_state_dict(dict(np.load(a.weights)))
+    else:
+        t0 = time.perf_counter()
+        data = make_data([TRAIN_SEED0 + i for i in range(a.train)], a.residual, a.max_cycles, log)
+        report.update(train_pairs=len(data), data_s=time.perf_counter() - t0,
+                      target_rms=float(np.sqrt(np.mean([float((t.double() ** 2).mean()) for _, t in data]))))
+        log(f"target rms {report['target_rms']:.3f} grid spacings")
+        hist = train(net, data, a.minutes, lr=a.lr, log=log)
+        report.update(train_steps=hist[-1][0] if hist else 0, loss_first=hist[0][2] if hist else None,
+                      loss_last=hist[-1][2] if hist else None)
+        if a.out:
+            np.savez(a.out, **net.state_dict())
+    variants = [int(v) for v in a.smooth.split(",")]
+    for sm in variants:
+        rows = evaluate(net, [EVAL_SEED0 + i for i in range(a.eval)], a.residual, a.max_cycles, log, smooth=sm)
+        report[f"smooth{sm}"] = dict(summary=summarize(rows), rows=rows)
+        log(f"smooth {sm}: " + json.dumps(report[f"smooth{sm}"]["summary"]))
+    best = min(variants, key=lambda v: -(report[f"smooth{v}"]["summary"]["speedup_total"] or 0))
+    report.update(best_smooth=best, summary=report[f"smooth{best}"]["summary"])
+    if a.large:
+        report["large"] = evaluate_large(net.state_dict(), a.residual, 4 * a.max_cycles, log=log)
+    log(json.dumps(report["summary"]))
+    if a.report:
+        with open(a.report, "w") as f:
+            json.dump(report, f, indent=1)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
