@@ -416,15 +416,16 @@ __global__ void k_relu_bwd(__nv_bfloat16* __restrict__ d, int ldd, const __nv_bf
 // imposed to be zero).  Writes the gradient (BF16) and adds the loss sum.
 __global__ void k_mse(const __nv_bfloat16* __restrict__ y, int ldy, const float* __restrict__ tgt,
                       __nv_bfloat16* __restrict__ dy, int lddy, int nx, int ny, int nz, float scale,
-                      float* __restrict__ loss) {
+                      float* __restrict__ loss, int sx, int sy) {
     __shared__ float red[256];
     const long long V = (long long)nx * ny * nz;
     float s = 0.f;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(v / ((long long)nx * ny));
+        const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long long)nx * ny));
         const bool in = k > 0 && k < nz - 1;
+        const long long vt = (long long)((i + sx) % nx) + (long long)nx * (((j + sy) % ny) + (long long)ny * k);
         for (int c = 0; c < 3; c++) {
-            const float e = in ? __bfloat162float(y[v * ldy + c]) - tgt[3 * v + c] : 0.f;
+            const float e = in ? __bfloat162float(y[v * ldy + c]) - tgt[3 * vt + c] : 0.f;
             s += e * e;
             dy[v * lddy + c] = __float2bfloat16_rn(2.f * scale * e);
         }
@@ -480,12 +481,16 @@ __global__ void k_adam(float* __restrict__ W, float* __restrict__ mW, float* __r
 
 // Input channels (B0x, B0y, B0z - 1) of the inner points, from the ghosted
 // AoS B0 of the reference layout (REAL T); ld channels, the rest zero.
+// The field is read at (i + sx, j + sy) (periodic): a whole-cell translation
+// of the sample, used to augment training data on the periodic axes.
 template <typename T>
-__global__ void k_input(const T* __restrict__ B0, int nx, int ny, int nz, __nv_bfloat16* __restrict__ x, int ld) {
+__global__ void k_input(const T* __restrict__ B0, int nx, int ny, int nz, __nv_bfloat16* __restrict__ x, int ld,
+                        int sx, int sy) {
     const long long V = (long long)nx * ny * nz;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long long)nx * ny));
-        const long long g = (long long)(i + 1) + (long long)(nx + 2) * ((j + 1) + (long long)(ny + 2) * (k + 1));
+        const int is = (i + sx) % nx, js = (j + sy) % ny;
+        const long long g = (long long)(is + 1) + (long long)(nx + 2) * ((js + 1) + (long long)(ny + 2) * (k + 1));
         for (int c = 0; c < ld; c++) {
             float val = 0.f;
             if (c < 3) val = (float)B0[3 * g + c] - (c == 2 ? 1.f : 0.f);
@@ -601,14 +606,16 @@ int gm_nn_upsample(const void* in, int ldi, void* out, int ldo, int c, int nx, i
     return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_upsample");
 }
 
-int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, void* stream) {
+int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, int sx, int sy,
+                void* stream) {
+    if (sx < 0 || sx >= nx || sy < 0 || sy >= ny) return gm::fail(GM_EPARAM, "gm_nn_input: shift out of range");
     const long long V = (long long)nx * ny * nz;
     if (precision == 32)
         gmnn::k_input<float><<<gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>((const float*)B0, nx, ny, nz,
-                                                                              (__nv_bfloat16*)x, ld);
+                                                                              (__nv_bfloat16*)x, ld, sx, sy);
     else
         gmnn::k_input<double><<<gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>((const double*)B0, nx, ny, nz,
-                                                                               (__nv_bfloat16*)x, ld);
+                                                                               (__nv_bfloat16*)x, ld, sx, sy);
     return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_input");
 }
 
@@ -624,10 +631,11 @@ int gm_nn_relu_bwd(void* d, int ldd, const void* y, int ldy, int c, long long V,
 }
 
 int gm_nn_mse(const void* y, int ldy, const float* tgt, void* dy, int lddy, int nx, int ny, int nz, float scale,
-              float* loss, void* stream) {
+              float* loss, int sx, int sy, void* stream) {
+    if (sx < 0 || sx >= nx || sy < 0 || sy >= ny) return gm::fail(GM_EPARAM, "gm_nn_mse: shift out of range");
     const long long V = (long long)nx * ny * nz;
     gmnn::k_mse<<<gmnn::nb(V) > 256 ? 256 : gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>(
-        (const __nv_bfloat16*)y, ldy, tgt, (__nv_bfloat16*)dy, lddy, nx, ny, nz, scale, loss);
+        (const __nv_bfloat16*)y, ldy, tgt, (__nv_bfloat16*)dy, lddy, nx, ny, nz, scale, loss, sx, sy);
     return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_mse");
 }
 

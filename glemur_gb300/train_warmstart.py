@@ -25,7 +25,7 @@ import time
 import numpy as np
 
 from . import BatchRelaxation, Relaxation, configs
-from .warmstart import UNet, n_params
+from .warmstart import UNet, load_weights, n_params, save_weights
 
 SHAPE = (64, 64, 128)
 TRAIN_SEED0 = 100000      # training seeds TRAIN_SEED0 + i
@@ -93,9 +93,11 @@ def train(net, data, minutes, lr=1e-3, batch=4, log=print):
             net.zero_grad()
             for k in order[q:q + batch]:
                 B0, tgt = data[k]
-                net.set_input_b0(B0, 32)
+                # whole-cell translations along the periodic axes: exact copies of the problem
+                sh = (int(rng.integers(nx)), int(rng.integers(ny)))
+                net.set_input_b0(B0, 32, sh)
                 net.forward()
-                net.backward(tgt, scale)
+                net.backward(tgt, scale, sh)
             net.refresh_weights(lr=lr_t, step=True)
             step += 1
             if step % 25 == 0:
@@ -126,7 +128,7 @@ def smooth_displacement(d, passes, xper=True, yper=True):
     return d
 
 
-def warm_grid(net, p, B0, smooth=0):
+def warm_grid(net, p, B0, smooth=2):
     """The predicted grid in the reference layout (ghosted AoS): the identity
     grid plus the network's displacement at the inner points (optionally
     smoothed; zero on the first and last z-planes), periodic ghosts as shifted
@@ -181,7 +183,7 @@ def time_to_residual(g, p, xb, B0, residual, max_attempts, check_every=50):
     return time.perf_counter() - t0, att, r0, mind, reached
 
 
-def evaluate(net, seeds, residual, max_attempts, log=print, smooth=0):
+def evaluate(net, seeds, residual, max_attempts, log=print, smooth=2):
     import torch
     rows = []
     for s in seeds:
@@ -268,6 +270,7 @@ def evaluate_large(weights, residual, max_attempts, factor=2, log=print):
     Bc = coarse_b0(p, B0, factor)
     net.set_input_b0(torch.from_numpy(Bc).cuda(), 32)
     y = net.forward()[:, :3].float().cpu().numpy().reshape(cshape[2], cshape[1], cshape[0], 3)
+    y = smooth_displacement(y.astype(np.float64), 2)
     # coarse grid units -> physical -> fine inner points
     sp_c = np.array([p.dx, p.dy, p.dz]) * factor
     d = upsample_displacement(y * sp_c, factor, (p.nx, p.ny, p.nz))
@@ -322,7 +325,7 @@ def main(argv=None):
     ap.add_argument("--weights", default="", help="evaluate these weights instead of training")
     ap.add_argument("--shape", default="64,64,128", help="grid (nx,ny,nz), each divisible by 4")
     ap.add_argument("--large", action="store_true", help="also evaluate the 256x256x512 pressure case")
-    ap.add_argument("--smooth", default="0", help="comma-separated box-filter passes to evaluate")
+    ap.add_argument("--smooth", default="2", help="comma-separated box-filter passes to evaluate")
     a = ap.parse_args(argv)
     global SHAPE
     SHAPE = tuple(int(v) for v in a.shape.split(","))
@@ -331,7 +334,7 @@ def main(argv=None):
     log(f"U-Net: {n_params()} parameters")
     report = dict(shape=SHAPE, residual=a.residual, params=n_params())
     if a.weights:
-        net.load_state_dict(dict(np.load(a.weights)))
+        net.load_state_dict(load_weights(a.weights))
     else:
         t0 = time.perf_counter()
         data = make_data([TRAIN_SEED0 + i for i in range(a.train)], a.residual, a.max_cycles, log)
@@ -342,7 +345,7 @@ def main(argv=None):
         report.update(train_steps=hist[-1][0] if hist else 0, loss_first=hist[0][2] if hist else None,
                       loss_last=hist[-1][2] if hist else None)
         if a.out:
-            np.savez(a.out, **net.state_dict())
+            save_weights(net.state_dict(), a.out)
     variants = [int(v) for v in a.smooth.split(",")]
     for sm in variants:
         rows = evaluate(net, [EVAL_SEED0 + i for i in range(a.eval)], a.residual, a.max_cycles, log, smooth=sm)

@@ -21,8 +21,12 @@ import math
 
 import numpy as np
 
+from pathlib import Path
+
 from . import _abi
 from ._abi import check
+
+WEIGHTS = Path(__file__).resolve().parent / "weights" / "unet_64x64x128.npz"
 
 # name, input channels of the weights, output channels, ReLU
 LAYERS = [("e0a", 3, 24, True), ("e0b", 24, 24, True), ("e1a", 24, 48, True), ("e1b", 48, 48, True),
@@ -42,6 +46,24 @@ def r8(n):
 
 def n_params():
     return sum(27 * ci * co + co for _, ci, co, _ in LAYERS)
+
+
+def bf16_bits(a):
+    """float32 -> BF16 bit patterns (round to nearest even)."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def save_weights(state, path):
+    """Weights as BF16 bit patterns, the precision the network computes with."""
+    np.savez(path, **{k: bf16_bits(v) for k, v in state.items()})
+
+
+def load_weights(path=None):
+    """Weights saved by save_weights (BF16 bits, widened to float32) or as float32."""
+    d = np.load(path or WEIGHTS)
+    return {k: (d[k].astype(np.uint32) << 16).view(np.float32) if d[k].dtype == np.uint16 else d[k].astype(np.float32)
+            for k in d.files}
 
 
 class _Layer:
@@ -138,11 +160,12 @@ class UNet:
               "gm_nn_relu_bwd")
 
     # -- the network ----------------------------------------------------------
-    def set_input_b0(self, B0_dev, precision):
-        """B0: device array of the reference layout (ghosted AoS, REAL)."""
+    def set_input_b0(self, B0_dev, precision, shift=(0, 0)):
+        """B0: device array of the reference layout (ghosted AoS, REAL), read
+        translated by `shift` whole cells in x and y (periodic)."""
         nx, ny, nz = self.shape
         check(self.lib.gm_nn_input(C.c_void_p(B0_dev.data_ptr()), precision, nx, ny, nz,
-                                   self.v("X0")[0], 8, C.c_void_p(self.stream)), "gm_nn_input")
+                                   self.v("X0")[0], 8, shift[0], shift[1], C.c_void_p(self.stream)), "gm_nn_input")
 
     def forward(self):
         Ls, v = self.layers, self.v
@@ -169,14 +192,15 @@ class UNet:
                 check(self.lib.gm_nn_zero(C.c_void_p(t.data_ptr()), t.numel() * 4, C.c_void_p(self.stream)), "zero")
         check(self.lib.gm_nn_zero(C.c_void_p(self.loss_acc.data_ptr()), 4, C.c_void_p(self.stream)), "zero")
 
-    def backward(self, target, scale):
+    def backward(self, target, scale, shift=(0, 0)):
         """Loss scale * sum (y - target)^2 (planes 1..nz-2, 3 channels) and the
-        accumulation of every weight gradient; target: float32 [V][3] on the device."""
+        accumulation of every weight gradient; target: float32 [V][3] on the
+        device, read translated by `shift` as the input was."""
         Ls, v = self.layers, self.v
         nx, ny, nz = self.shape
         check(self.lib.gm_nn_mse(v("Y")[0], 8, C.cast(target.data_ptr(), C.POINTER(C.c_float)), v("dY")[0], 8,
                                  nx, ny, nz, C.c_float(scale), C.cast(self.loss_acc.data_ptr(), C.POINTER(C.c_float)),
-                                 C.c_void_p(self.stream)), "gm_nn_mse")
+                                 shift[0], shift[1], C.c_void_p(self.stream)), "gm_nn_mse")
         L = Ls["head"]
         self._wgrad(L, v("dY"), v("D0b"), 0)
         self._conv(L, v("dY"), v("dD0b"), 24, 0, False, mask=v("D0b"), backward=True, src_c=8)

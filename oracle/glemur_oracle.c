@@ -675,9 +675,26 @@ static void grad_p(orc_state* s) {
                             g[1] -= d2[a][b][l] * jac1[b][a] * jac1[l][1];
                             g[2] -= d2[a][b][l] * jac1[b][a] * jac1[l][2];
                         }
-                for (l = 0; l < 3; l++) {
-                    g[l] *= p->beta * det1;
-                    s->gradP[3 * II(p, i, j, k) + l] = g[l];
+                if (p->p0Amp != 0) {
+                    /* This library's extension (no reference counterpart):
+                     * p = p0(X) / Delta with p0(X) = beta (1 + p0Amp exp(-(X^2 + Y^2) / p0Width^2))
+                     * on the initial grid, so grad_x p = p0 grad_x(1/Delta) + (1/Delta) grad_x p0,
+                     * where grad_x(1/Delta) = det1 * g (the sum above) and
+                     * d p0 / d x_c = sum_a d p0 / d X_a  d X_a / d x_c = sum_a dp0_a jac1[a][c]. */
+                    const R X = p->dx * (R)i + p->Ox, Y = p->dy * (R)j + p->Oy;
+                    const R w2 = (R)((double)p->p0Width * (double)p->p0Width);
+                    const R e = p->p0Amp * (R)exp((double)(-(X * X + Y * Y) / w2));
+                    const R p0 = p->beta * (1 + e);
+                    const R dp0x = p->beta * e * (-2 * X / w2), dp0y = p->beta * e * (-2 * Y / w2);
+                    for (l = 0; l < 3; l++) {
+                        g[l] = (p0 * g[l] + dp0x * jac1[0][l] + dp0y * jac1[1][l]) * det1;
+                        s->gradP[3 * II(p, i, j, k) + l] = g[l];
+                    }
+                } else {
+                    for (l = 0; l < 3; l++) {
+                        g[l] *= p->beta * det1;
+                        s->gradP[3 * II(p, i, j, k) + l] = g[l];
+                    }
                 }
             }
     }

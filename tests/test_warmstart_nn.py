@@ -150,3 +150,30 @@ def test_gpu_adam_step_reduces_loss():
         net.refresh_weights(lr=3e-3, step=True)
     net.check_status()
     assert losses[-1] < 0.5 * losses[0], losses
+
+
+@pytest.mark.gpu
+def test_gpu_input_and_loss_translation():
+    """The augmentation: input and loss target read translated by whole cells."""
+    import torch
+    from glemur_gb300.warmstart import UNet
+    nx, ny, nz = 8, 12, 16
+    net = UNet((nx, ny, nz), seed=0)
+    rng = np.random.default_rng(9)
+    B0 = rng.normal(size=(nz + 2, ny + 2, nx + 2, 3)).astype(np.float32)
+    sh = (3, 5)
+    net.set_input_b0(torch.from_numpy(B0).cuda(), 32, sh)
+    x = net.A["X0"][:, :3].float().cpu().numpy().reshape(nz, ny, nx, 3)
+    ref = np.roll(B0[1:-1, 1:-1, 1:-1], (-sh[1], -sh[0]), axis=(1, 2)).astype(np.float64)
+    ref[..., 2] -= 1.0
+    assert np.abs(x - ref).max() < 1e-2 * np.abs(ref).max()
+    tgt = rng.normal(size=(nz, ny, nx, 3)).astype(np.float32)
+    net.zero_grad()
+    net.forward()
+    net.backward(torch.from_numpy(tgt.reshape(-1, 3)).cuda(), 1.0, sh)
+    torch.cuda.synchronize()
+    y = net.A["Y"][:, :3].float().cpu().numpy().reshape(nz, ny, nx, 3).astype(np.float64)
+    e = y - np.roll(tgt, (-sh[1], -sh[0]), axis=(1, 2))
+    e[0] = 0
+    e[-1] = 0
+    assert float(net.loss_acc.item()) == pytest.approx(float((e * e).sum()), rel=1e-3)
