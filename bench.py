@@ -9,7 +9,9 @@ the whole grid; the metric is cell-RK-stages/s = N x 6 x steps / time.
   python bench.py --workload batch64 [--batch-residual R] [--batch-cycles C]
 
 --workload large times the 256x256x512 braid with k = +-1.2 and the
-pressure term with the p0(r) profile (the plain path of the large case).
+pressure term with the p0(r) profile (the plain path of the large case);
+--large-shape nx,ny,nz runs the same braid on another grid (a smaller case
+for a profiler capture).
 
 --workload batch64 runs the batched configuration instead: 64 seeded random
 braids of uneven sizes (seeds 1000..1063, drawn as configs.random_braid) in
@@ -45,12 +47,13 @@ SHAPE = (128, 128, 256)
 
 
 WORKLOAD = "braid6"
+LARGE_SHAPE = (256, 256, 512)
 
 
 def workload_params(precision=32):
     from glemur_gb300 import configs
     if WORKLOAD == "large":
-        return configs.braid6_large(256, 256, 512, precision=precision)
+        return configs.braid6_large(*LARGE_SHAPE, precision=precision)
     p = configs.braid6(*SHAPE, precision=precision)
     return p
 
@@ -151,9 +154,15 @@ def traffic_per_launch(p):
     d = json.loads(f.read_text())
     key = f"{p.nx}x{p.ny}x{p.nz}_fp{p.precision}" + ("_pressure" if p.pressure else "")
     e = d.get(key)
+    if e:
+        return float(e["bytes_per_launch"]), e.get("source")
+    # a per-point figure measured on a smaller grid of the same kernel scales
+    # with the inner points (the traffic is streaming: each plane once)
+    e = d.get(f"per_point_fp{p.precision}" + ("_pressure" if p.pressure else ""))
     if not e:
         return None, None
-    return float(e["bytes_per_launch"]), e.get("source")
+    n = p.nx * p.ny * p.nz
+    return float(e["bytes_per_point"]) * n, f"{e.get('source')}, scaled to {n} inner points"
 
 
 def cpu_baseline(p, seconds=20.0):
@@ -417,13 +426,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--workload", default="braid6", choices=["braid6", "batch64", "large"])
+    ap.add_argument("--large-shape", default="256,256,512", help="grid of --workload large")
     ap.add_argument("--batch-residual", type=float, default=0.2)
     ap.add_argument("--batch-cycles", type=int, default=3000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    global WORKLOAD
+    global WORKLOAD, LARGE_SHAPE
     WORKLOAD = args.workload
+    LARGE_SHAPE = tuple(int(v) for v in args.large_shape.split(","))
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch64":
