@@ -58,8 +58,8 @@ int check_params(const gm_params* p) {
     if (p->precision != 32 && p->precision != 64) return gm::fail(GM_EPARAM, "precision must be 32 or 64");
     if (p->nx < 3 || p->ny < 3 || p->nz < 3) return gm::fail(GM_EPARAM, "nx, ny, nz must be >= 3");
     if ((long long)p->nx * p->ny * p->nz > (1ll << 31)) return gm::fail(GM_EPARAM, "grid too large");
-    if (strncmp(p->jMethod, "Stokes ", 7) != 0)
-        return gm::fail(GM_EPARAM, "jMethod: only the Stokes current (the reference default) is implemented");
+    if (strncmp(p->jMethod, "Stokes ", 7) != 0 && strncmp(p->jMethod, "Classic ", 8) != 0)
+        return gm::fail(GM_EPARAM, "jMethod: the Stokes and Classic currents are implemented");
     if (p->pressure && strncmp(p->pMethod, "Classic ", 8) != 0) return gm::fail(GM_EPARAM, "pMethod must be Classic");
     if (p->inertia) return gm::fail(GM_EPARAM, "inertia = T is not implemented");
     if (p->jxbAver) return gm::fail(GM_EPARAM, "jxbAver = T is not implemented");
@@ -174,6 +174,7 @@ struct Impl : ImplBase {
         kp.zUpdate = p->zUpdate != 0;
         kp.errMode = p->errMode;
         kp.refDt = p->errMode == 0;
+        kp.jClassic = strncmp(p->jMethod, "Classic ", 8) == 0;
         kp.beta = (T)p->beta;
         kp.p0Amp = (T)p->p0Amp;
         kp.p0W2 = (T)(p->p0Width * p->p0Width);
@@ -272,7 +273,9 @@ struct Impl : ImplBase {
         smem_stage = gmk::stage_smem_bytes<T>(TY, gmk::MODE_STAGE, p->pressure);
         smem_diag = gmk::stage_smem_bytes<T>(TY, gmk::MODE_DIAG, p->pressure);
         nparts = (int)(grid.x * grid.y * grid.z);
-        use_tma = p->stageKernel == 0;
+        // the TMA kernel computes the Stokes current only; the Classic current
+        // runs in the generic kernel
+        use_tma = p->stageKernel == 0 && strncmp(p->jMethod, "Classic ", 8) != 0;
         if (use_tma) {
             if ((rc = init_tma(nsm))) return rc;
         }
@@ -698,6 +701,8 @@ struct Batch : BatchBase {
             p.stageKernel = 0;
             int rc = check_params(&p);
             if (rc) return rc;
+            if (strncmp(p.jMethod, "Stokes ", 7) != 0)
+                return gm::fail(GM_EPARAM, "gm_batch_create: batched cases use the Stokes current");
             cs.emplace_back(new Impl<T>());
             if ((rc = cs.back()->init(&p))) return rc;
             cs.back()->stream = stream;

@@ -201,6 +201,82 @@ __device__ __forceinline__ void stokes(const T xn[6][3], const T bn[6][3], T J[3
     for (int l = 0; l < 3; l++) J[l] = (NA1[l][0] * II[0] + NA1[l][1] * II[1] + NA1[l][2] * II[2]) * (T)2;
 }
 
+// Finite-difference current: JClassic, src/current.cu:10-218.  J = curl B
+// for B = jac.B0 / Delta, differentiated by the chain rule on the initial
+// grid: d B_m / d X_a = sum_b (d2x[m][a][b] B0_b / Delta + jac[m][b]
+// dB0_b/dX_a / Delta + jac[m][b] B0_b d(1/Delta)/dX_a), and
+// d / d x_c = sum_a jac^-1[a][c] d / d X_a.  Reads the positions of the
+// point, its face and edge neighbours (the position ring), Delta at the point
+// and its face neighbours (the B ring, ghost values included) and B0 there
+// (global memory); B itself is not used.
+template <typename T, class TileT>
+__device__ __forceinline__ void j_classic(const KP<T>& p, const TileT& t, const T* __restrict__ B0, int i, int j,
+                                          int k, T Jv[3]) {
+    T jac[3][3], jac1[3][3], dB0[3][3], dDet1[3], B0l[3];
+#define XV(di, dj, dk, l) t.x(k + (dk), l, j + (dj), i + (di))
+#define B0V(di, dj, dk, l) __ldg(&B0[(long long)(l) * p.cs + gidx(p.px, p.py, i + (di), j + (dj), k + (dk))])
+#define DV(di, dj, dk) t.b(k + (dk), 3, j + (dj), i + (di))
+    const T det1 = rcp_rn(DV(0, 0, 0));
+#pragma unroll
+    for (int l = 0; l < 3; l++) {
+        jac[l][0] = (XV(1, 0, 0, l) - XV(-1, 0, 0, l)) * p.dx1 / 2;
+        jac[l][1] = (XV(0, 1, 0, l) - XV(0, -1, 0, l)) * p.dy1 / 2;
+        jac[l][2] = (XV(0, 0, 1, l) - XV(0, 0, -1, l)) * p.dz1 / 2;
+        B0l[l] = B0V(0, 0, 0, l);
+        dB0[l][0] = (B0V(1, 0, 0, l) - B0V(-1, 0, 0, l)) * p.dx1 / 2;
+        dB0[l][1] = (B0V(0, 1, 0, l) - B0V(0, -1, 0, l)) * p.dy1 / 2;
+        dB0[l][2] = (B0V(0, 0, 1, l) - B0V(0, 0, -1, l)) * p.dz1 / 2;
+    }
+    jac1[0][0] = (jac[1][1] * jac[2][2] - jac[1][2] * jac[2][1]) * det1;
+    jac1[0][1] = (jac[0][2] * jac[2][1] - jac[0][1] * jac[2][2]) * det1;
+    jac1[0][2] = (jac[0][1] * jac[1][2] - jac[0][2] * jac[1][1]) * det1;
+    jac1[1][0] = (jac[1][2] * jac[2][0] - jac[1][0] * jac[2][2]) * det1;
+    jac1[1][1] = (jac[0][0] * jac[2][2] - jac[0][2] * jac[2][0]) * det1;
+    jac1[1][2] = (jac[0][2] * jac[1][0] - jac[0][0] * jac[1][2]) * det1;
+    jac1[2][0] = (jac[1][0] * jac[2][1] - jac[1][1] * jac[2][0]) * det1;
+    jac1[2][1] = (jac[0][1] * jac[2][0] - jac[0][0] * jac[2][1]) * det1;
+    jac1[2][2] = (jac[0][0] * jac[1][1] - jac[0][1] * jac[1][0]) * det1;
+    dDet1[0] = (rcp_rn(DV(1, 0, 0)) - rcp_rn(DV(-1, 0, 0))) * p.dx1 / 2;
+    dDet1[1] = (rcp_rn(DV(0, 1, 0)) - rcp_rn(DV(0, -1, 0))) * p.dy1 / 2;
+    dDet1[2] = (rcp_rn(DV(0, 0, 1)) - rcp_rn(DV(0, 0, -1))) * p.dz1 / 2;
+    Jv[0] = 0; Jv[1] = 0; Jv[2] = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        // second derivatives d2x[m][a][b] of the three components for this a
+        T d2[3][3];
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            const T xc2 = 2 * XV(0, 0, 0, m);
+            if (a == 0) {
+                d2[m][0] = (XV(1, 0, 0, m) - xc2 + XV(-1, 0, 0, m)) * p.dx1 * p.dx1;
+                d2[m][1] = (XV(1, 1, 0, m) - XV(1, -1, 0, m) - XV(-1, 1, 0, m) + XV(-1, -1, 0, m)) * p.dx1 * p.dy1 / 4;
+                d2[m][2] = (XV(1, 0, 1, m) - XV(1, 0, -1, m) - XV(-1, 0, 1, m) + XV(-1, 0, -1, m)) * p.dx1 * p.dz1 / 4;
+            } else if (a == 1) {
+                d2[m][0] = (XV(1, 1, 0, m) - XV(1, -1, 0, m) - XV(-1, 1, 0, m) + XV(-1, -1, 0, m)) * p.dx1 * p.dy1 / 4;
+                d2[m][1] = (XV(0, 1, 0, m) - xc2 + XV(0, -1, 0, m)) * p.dy1 * p.dy1;
+                d2[m][2] = (XV(0, 1, 1, m) - XV(0, -1, 1, m) - XV(0, 1, -1, m) + XV(0, -1, -1, m)) * p.dy1 * p.dz1 / 4;
+            } else {
+                d2[m][0] = (XV(1, 0, 1, m) - XV(1, 0, -1, m) - XV(-1, 0, 1, m) + XV(-1, 0, -1, m)) * p.dx1 * p.dz1 / 4;
+                d2[m][1] = (XV(0, 1, 1, m) - XV(0, -1, 1, m) - XV(0, 1, -1, m) + XV(0, -1, -1, m)) * p.dy1 * p.dz1 / 4;
+                d2[m][2] = (XV(0, 0, 1, m) - xc2 + XV(0, 0, -1, m)) * p.dz1 * p.dz1;
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            T dB[3];
+#pragma unroll
+            for (int m = 0; m < 3; m++)
+                dB[m] = d2[m][b] * B0l[b] * det1 + jac[m][b] * dB0[b][a] * det1 + jac[m][b] * B0l[b] * dDet1[a];
+            Jv[0] += jac1[a][1] * dB[2] - jac1[a][2] * dB[1];
+            Jv[1] += jac1[a][2] * dB[0] - jac1[a][0] * dB[2];
+            Jv[2] += jac1[a][0] * dB[1] - jac1[a][1] * dB[0];
+        }
+    }
+#undef XV
+#undef B0V
+#undef DV
+}
+
 // Pressure gradient grad(p) for p = p0(X)/Delta: gradPClassic,
 // src/gradP.cu:91-155 (uniform p0 = beta), plus (1/Delta) J^-T grad_X p0 for
 // a non-uniform p0(X) (no counterpart in the reference).
@@ -292,7 +368,7 @@ __device__ __forceinline__ bool finite3d(double a, double b, double c) { return 
 template <typename T, bool PRESS, int MODE, bool LAST>
 __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    constexpr int NB = (PRESS || MODE == MODE_DIAG) ? 4 : 3;
+    constexpr int NB = 4;     // B and Delta (Delta: pressure, the Classic current, diagnostics)
     const KP<T>& p = a.p;
     DevState* st = a.st;
     if (MODE == MODE_STAGE && st->done) return;
@@ -386,18 +462,23 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
         if (kc >= k0 && kc < kend) {
             const int i = i0 + tx, j = j0 + ty;
             if (i < p.nx && j < p.ny) {
-                T xn[6][3], bn[6][3], Bc[3], Jv[3];
-                const int di[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, dk[6] = {0, 0, 0, 0, -1, 1};
-#pragma unroll
-                for (int q = 0; q < 6; q++)
-#pragma unroll
-                    for (int l = 0; l < 3; l++) {
-                        xn[q][l] = t.x(kc + dk[q], l, j + dj[q], i + di[q]);
-                        bn[q][l] = t.b(kc + dk[q], l, j + dj[q], i + di[q]);
-                    }
+                T Bc[3], Jv[3];
 #pragma unroll
                 for (int l = 0; l < 3; l++) Bc[l] = t.b(kc, l, j, i);
-                stokes<T>(xn, bn, Jv);
+                if (p.jClassic) {
+                    j_classic<T>(p, t, a.B0, i, j, kc, Jv);
+                } else {
+                    T xn[6][3], bn[6][3];
+                    const int di[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, dk[6] = {0, 0, 0, 0, -1, 1};
+#pragma unroll
+                    for (int q = 0; q < 6; q++)
+#pragma unroll
+                        for (int l = 0; l < 3; l++) {
+                            xn[q][l] = t.x(kc + dk[q], l, j + dj[q], i + di[q]);
+                            bn[q][l] = t.b(kc + dk[q], l, j + dj[q], i + di[q]);
+                        }
+                    stokes<T>(xn, bn, Jv);
+                }
                 const long long lin = (long long)i + (long long)p.nx * ((long long)j + (long long)p.ny * kc);
                 const long long klin = (long long)i + (long long)p.kpx * ((long long)j + (long long)p.ny * kc);
                 const long long KC = p.kcs;
@@ -885,7 +966,8 @@ __global__ void k_eps_star(const KP<T> p, const T* __restrict__ B, const T* __re
 
 template <typename T>
 size_t stage_smem_bytes(int TY, int mode, int pressure) {
-    const int NB = (pressure || mode == MODE_DIAG) ? 4 : 3;
+    (void)pressure;
+    const int NB = 4;
     size_t b = sizeof(T) * ((size_t)XRING * 3 * (TY + 4) * (TX + 4) + (size_t)BRING * NB * (TY + 2) * (TX + 2));
     if (mode == MODE_DIAG) b = b > (size_t)R_COUNT * TX * TY * sizeof(double) ? b : (size_t)R_COUNT * TX * TY * sizeof(double);
     return b;

@@ -61,6 +61,7 @@ typedef struct {
     int nTs;
     int errMode;
     R p0Amp, p0Width;
+    int jClassic;              /* jMethod = "Classic" (else "Stokes")            */
 } P;
 
 typedef struct orc_state {
@@ -100,6 +101,7 @@ static void to_P(const gm_params* g, P* p) {
     p->nTs = g->nTs > 0 ? g->nTs : 1;
     p->errMode = g->errMode;
     p->p0Amp = (R)g->p0Amp; p->p0Width = (R)g->p0Width;
+    p->jClassic = strncmp(g->jMethod, "Classic ", 8) == 0;
 }
 
 /* ghosted (i, j, k in 0..n+1) and inner (0..n-1) linear point indices */
@@ -626,6 +628,81 @@ static void j_stokes(orc_state* s) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Finite-difference current, JClassic src/current.cu:10-218                */
+/* ------------------------------------------------------------------------ */
+
+/* J = curl B with B = jac.B0 / Delta, differentiated by the chain rule on the
+ * initial grid: d B_k / d X_a = sum_b (d2x[k][a][b] B0_b det1
+ * + jac[k][b] dB0[b][a] det1 + jac[k][b] B0_b d det1 / d X_a) and
+ * d / d x_c = sum_a jac1[a][c] d / d X_a (current.cu:142-216).  B itself is
+ * not read: the inputs are x (with its edge neighbours), B0 and detJac at
+ * the point and its six face neighbours (ghost values included). */
+static void j_classic(orc_state* s) {
+    const P* p = &s->p;
+    int k;
+#pragma omp parallel for schedule(static)
+    for (k = 0; k < p->nz; k++) {
+        int i, j, l, a, b;
+        for (j = 0; j < p->ny; j++)
+            for (i = 0; i < p->nx; i++) {
+                R jac[3][3], jac1[3][3], d2[3][3][3], dB0[3][3], dDet1[3], det1, B0l[3], Jv[3];
+                const R* x = s->xb;
+#define XV(di, dj, dk, l_) x[3 * GI(p, i + 1 + (di), j + 1 + (dj), k + 1 + (dk)) + (l_)]
+#define B0V(di, dj, dk, l_) s->B0[3 * GI(p, i + 1 + (di), j + 1 + (dj), k + 1 + (dk)) + (l_)]
+#define DV(di, dj, dk) s->detJac[GI(p, i + 1 + (di), j + 1 + (dj), k + 1 + (dk))]
+                for (l = 0; l < 3; l++) {
+                    jac[l][0] = (XV(1, 0, 0, l) - XV(-1, 0, 0, l)) * p->dx1 / 2;
+                    jac[l][1] = (XV(0, 1, 0, l) - XV(0, -1, 0, l)) * p->dy1 / 2;
+                    jac[l][2] = (XV(0, 0, 1, l) - XV(0, 0, -1, l)) * p->dz1 / 2;
+                    B0l[l] = B0V(0, 0, 0, l);
+                }
+                det1 = 1 / DV(0, 0, 0);
+                jac1[0][0] = (jac[1][1] * jac[2][2] - jac[1][2] * jac[2][1]) * det1;
+                jac1[0][1] = (jac[0][2] * jac[2][1] - jac[0][1] * jac[2][2]) * det1;
+                jac1[0][2] = (jac[0][1] * jac[1][2] - jac[0][2] * jac[1][1]) * det1;
+                jac1[1][0] = (jac[1][2] * jac[2][0] - jac[1][0] * jac[2][2]) * det1;
+                jac1[1][1] = (jac[0][0] * jac[2][2] - jac[0][2] * jac[2][0]) * det1;
+                jac1[1][2] = (jac[0][2] * jac[1][0] - jac[0][0] * jac[1][2]) * det1;
+                jac1[2][0] = (jac[1][0] * jac[2][1] - jac[1][1] * jac[2][0]) * det1;
+                jac1[2][1] = (jac[0][1] * jac[2][0] - jac[0][0] * jac[2][1]) * det1;
+                jac1[2][2] = (jac[0][0] * jac[1][1] - jac[0][1] * jac[1][0]) * det1;
+                for (l = 0; l < 3; l++) {
+                    d2[l][0][0] = (XV(1, 0, 0, l) - 2 * XV(0, 0, 0, l) + XV(-1, 0, 0, l)) * p->dx1 * p->dx1;
+                    d2[l][1][1] = (XV(0, 1, 0, l) - 2 * XV(0, 0, 0, l) + XV(0, -1, 0, l)) * p->dy1 * p->dy1;
+                    d2[l][2][2] = (XV(0, 0, 1, l) - 2 * XV(0, 0, 0, l) + XV(0, 0, -1, l)) * p->dz1 * p->dz1;
+                    d2[l][0][1] = (XV(1, 1, 0, l) - XV(1, -1, 0, l) - XV(-1, 1, 0, l) + XV(-1, -1, 0, l)) * p->dx1 * p->dy1 / 4;
+                    d2[l][0][2] = (XV(1, 0, 1, l) - XV(1, 0, -1, l) - XV(-1, 0, 1, l) + XV(-1, 0, -1, l)) * p->dx1 * p->dz1 / 4;
+                    d2[l][1][2] = (XV(0, 1, 1, l) - XV(0, -1, 1, l) - XV(0, 1, -1, l) + XV(0, -1, -1, l)) * p->dy1 * p->dz1 / 4;
+                    d2[l][1][0] = d2[l][0][1];
+                    d2[l][2][0] = d2[l][0][2];
+                    d2[l][2][1] = d2[l][1][2];
+                    dB0[l][0] = (B0V(1, 0, 0, l) - B0V(-1, 0, 0, l)) * p->dx1 / 2;
+                    dB0[l][1] = (B0V(0, 1, 0, l) - B0V(0, -1, 0, l)) * p->dy1 / 2;
+                    dB0[l][2] = (B0V(0, 0, 1, l) - B0V(0, 0, -1, l)) * p->dz1 / 2;
+                }
+                dDet1[0] = (1 / DV(1, 0, 0) - 1 / DV(-1, 0, 0)) * p->dx1 / 2;
+                dDet1[1] = (1 / DV(0, 1, 0) - 1 / DV(0, -1, 0)) * p->dy1 / 2;
+                dDet1[2] = (1 / DV(0, 0, 1) - 1 / DV(0, 0, -1)) * p->dz1 / 2;
+#undef XV
+#undef B0V
+#undef DV
+                Jv[0] = 0; Jv[1] = 0; Jv[2] = 0;
+                for (a = 0; a < 3; a++)
+                    for (b = 0; b < 3; b++) {
+                        /* d B_m / d X_a, term b, for m = 0, 1, 2 */
+                        R dB[3];
+                        for (l = 0; l < 3; l++)
+                            dB[l] = d2[l][a][b] * B0l[b] * det1 + jac[l][b] * dB0[b][a] * det1 + jac[l][b] * B0l[b] * dDet1[a];
+                        Jv[0] += jac1[a][1] * dB[2] - jac1[a][2] * dB[1];
+                        Jv[1] += jac1[a][2] * dB[0] - jac1[a][0] * dB[2];
+                        Jv[2] += jac1[a][0] * dB[1] - jac1[a][1] * dB[0];
+                    }
+                for (l = 0; l < 3; l++) s->J[3 * II(p, i, j, k) + l] = Jv[l];
+            }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Pressure gradient, gradPClassic src/gradP.cu:10-156                      */
 /* ------------------------------------------------------------------------ */
 
@@ -790,7 +867,8 @@ static void x_new_star(orc_state* s) {
 void orc_refresh_fields(orc_state* s) {
     b_jac_b0(s);
     set_b_bound(s);
-    j_stokes(s);
+    if (s->p.jClassic) j_classic(s);
+    else j_stokes(s);
 }
 
 /* One RK stage n, src/main.cu:260-307. */

@@ -189,6 +189,7 @@ struct Ref {
     int timeIndex = 0, nAttempted = 0;
     size_t NG = 0, N = 0;
     bool open = false;
+    bool classic = false;   // jMethod = "Classic": JClassic instead of JStokes
 };
 Ref S;
 
@@ -201,6 +202,7 @@ const char* kname(const char* base, int prec) {
     else if (b == "updateBbound") s = "_Z12updateBbound7VarsDevi";
     else if (b == "setPeriFace") s = "_Z11setPeriFaceP" + r + "i";
     else if (b == "JStokes") s = "_Z7JStokes7VarsDeviii";
+    else if (b == "JClassic") s = "_Z8JClassic7VarsDeviii";
     else if (b == "gradPClassic") s = "_Z12gradPClassic7VarsDeviii";
     else if (b == "kk") s = "_Z2kk7VarsDeviiii" + r;
     else if (b == "setGridPeriFace") s = "_Z15setGridPeriFaceP" + r + "i";
@@ -268,7 +270,10 @@ int fields() {
     rc = set_peri(S.fPeri, S.d.B);
     if (rc) return rc;
     SYNC();
-    LK(S.fJ, dgrid(), dblock(), (unsigned)((3 * dX * dY * dZ * 2 + 3 * b0 * b1 * b2) * S.rs), a);
+    // current(), src/current.cu:1685-1720: dynamic shared memory per method
+    const unsigned jsm = S.classic ? (unsigned)(dX * dY * dZ * (3 * 2 + 1) * S.rs)
+                                   : (unsigned)((3 * dX * dY * dZ * 2 + 3 * b0 * b1 * b2) * S.rs);
+    LK(S.fJ, dgrid(), dblock(), jsm, a);
     SYNC();
     return 0;
 }
@@ -401,7 +406,8 @@ int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* 
     if (!load_driver()) return -3;
     ref_close();
     if (g->inertia || g->jxbAver) { g_err = "inertia/jxbAver runs are not driven by this launcher"; return -1; }
-    if (strncmp(g->jMethod, "Stokes ", 7) != 0) { g_err = "only jMethod = Stokes"; return -1; }
+    S.classic = strncmp(g->jMethod, "Classic ", 8) == 0;
+    if (strncmp(g->jMethod, "Stokes ", 7) != 0 && !S.classic) { g_err = "only jMethod = Stokes or Classic"; return -1; }
     S.prec = g->precision;
     S.rs = S.prec == 64 ? 8 : 4;
     S.gp = *g;
@@ -413,7 +419,7 @@ int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* 
     CK(D.ModuleLoad(&S.mod, cubin));
     int rc = 0;
     if ((rc = get_fn(&S.fBJ, "B_JacB0")) || (rc = get_fn(&S.fBound, "updateBbound")) ||
-        (rc = get_fn(&S.fPeri, "setPeriFace")) || (rc = get_fn(&S.fJ, "JStokes")) ||
+        (rc = get_fn(&S.fPeri, "setPeriFace")) || (rc = get_fn(&S.fJ, S.classic ? "JClassic" : "JStokes")) ||
         (rc = get_fn(&S.fGradP, "gradPClassic")) || (rc = get_fn(&S.fKK, "kk")) ||
         (rc = get_fn(&S.fGridPeri, "setGridPeriFace")) || (rc = get_fn(&S.fXNS, "xNewStar")) ||
         (rc = get_fn(&S.fMaxBlock, "maxBlock")))

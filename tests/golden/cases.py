@@ -10,6 +10,12 @@ reference's boundary handling:
 * zperi_f64  -- periodic y and z, line-tied x.
 * press_f64  -- the pressure term (src/gradP.cu) with uniform p0 = beta.
 * analytic_f64 -- the reference's analytic field (src/init.cu:71-78).
+* classic_tied_f64 / classic_tied_f32 -- the finite-difference current
+  (jMethod = "Classic", src/current.cu:10-218) with every face line-tied.
+  (With a periodic face the reference's ghost detJac there is not defined on
+  every row -- updateBbound's periodic branch, boundaries.cu:278,406 -- and
+  the Classic current reads it, so periodic Classic runs are checked against
+  the oracle only.)
 """
 from __future__ import annotations
 
@@ -39,6 +45,10 @@ def make(name: str):
         p.pressure = 1
         p.beta = 0.05
         return configs.derive(p)
+    if name in ("classic_tied_f64", "classic_tied_f32"):
+        p = _braid((17, 12, 17), 64 if name.endswith("64") else 32, peri=(0, 0, 0))
+        p.set_str("jMethod", "Classic")
+        return configs.derive(p)
     if name == "analytic_f64":
         p = configs.defaults(64)
         p.nx, p.ny, p.nz = 16, 16, 16
@@ -56,5 +66,6 @@ def make(name: str):
     raise KeyError(name)
 
 
-NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64"]
+NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64", "classic_tied_f64",
+         "classic_tied_f32"]
 N_ACCEPTED = 10

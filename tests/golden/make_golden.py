@@ -14,7 +14,7 @@ their outputs as tests/golden/<case>.npz:
   xN, BN, JN, DN    state after N_ACCEPTED accepted steps (inner points)
 
 Needs a GPU; run on the GPU machine after the build:
-  python tests/golden/make_golden.py
+  python tests/golden/make_golden.py [OUT_DIR [CASE ...]]
 """
 from __future__ import annotations
 
@@ -67,7 +67,7 @@ def generate(name: str, out_dir: Path) -> Path:
 def main(argv):
     out = Path(argv[1]) if len(argv) > 1 else HERE
     out.mkdir(parents=True, exist_ok=True)
-    for name in cases.NAMES:
+    for name in (argv[2:] or cases.NAMES):
         path = generate(name, out)
         print("wrote", path, path.stat().st_size)
 

@@ -180,7 +180,7 @@ def test_invalid_and_unbuilt_methods(tmp_path):
     d = tmp_path / "bad"
     make_run(d, 5)
     txt = (d / "params.in").read_text()
-    (d / "params.in").write_text(txt.replace('jMethod = "Stokes"', 'jMethod = "Classic"'))
+    (d / "params.in").write_text(txt.replace('jMethod = "Stokes"', 'jMethod = "StokesTri"'))
     r = subprocess.run([str(EXE)], cwd=d, capture_output=True, text=True, timeout=120)
     assert r.returncode != 0 and "not built" in r.stdout
     (d / "params.in").write_text(txt.replace('jMethod = "Stokes"', 'jMethod = "Nonsense"'))

@@ -53,9 +53,22 @@ def test_stages_match_oracle(name):
     stage_by_stage(cases.make(name), Oracle)
 
 
-@pytest.mark.parametrize("name", ["braid_f64", "braid_f32", "tied_f64", "press_f64"])
+@pytest.mark.parametrize("name", ["braid_f64", "braid_f32", "tied_f64", "press_f64", "classic_tied_f64",
+                                  "classic_tied_f32"])
 def test_stages_match_reference_kernels(name):
     stage_by_stage(cases.make(name), RefLauncher)
+
+
+@pytest.mark.parametrize("precision,peri", [(64, (1, 1, 0)), (64, (0, 1, 1)), (32, (1, 1, 0))])
+def test_classic_current_periodic_stages_match_oracle(precision, peri):
+    """The Classic current with periodic faces, against the oracle only: it
+    reads Delta on the ghost planes, which the reference leaves undefined on
+    some rows of a periodic face (updateBbound's periodic branch)."""
+    p = configs.braid2(16, 14, 18, precision=precision)
+    p.xPeri, p.yPeri, p.zPeri = peri
+    p.errMode = 0
+    p.set_str("jMethod", "Classic")
+    stage_by_stage(configs.derive(p), Oracle)
 
 
 # FP32: the error norm sum (c - c*) k cancels to ~1e-4 |k|, so float rounding
