@@ -178,6 +178,7 @@ struct Impl : ImplBase {
         kp.beta = (T)p->beta;
         kp.p0Amp = (T)p->p0Amp;
         kp.p0W2 = (T)(p->p0Width * p->p0Width);
+        kp.inv_p0W2 = kp.p0W2 != (T)0 ? (T)1 / kp.p0W2 : (T)0;
         kp.maxError = (double)(T)p->maxError;
         kp.dtMin = (double)(T)p->dtMin;
         kp.ar = p->ar; kp.az = p->az; kp.phi1 = p->phi1;

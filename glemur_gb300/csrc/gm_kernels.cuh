@@ -68,6 +68,7 @@ struct KP {
     int xPeri, yPeri, zPeri, zUpdate, errMode, refDt;
     int jClassic;            // jMethod = "Classic": the finite-difference current (generic kernel only)
     T beta, p0Amp, p0W2;     // pressure: p0(X) = beta (1 + p0Amp exp(-(X^2+Y^2)/p0W2))
+    T inv_p0W2;              // 1 / p0W2
     double maxError, dtMin;  // run-precision values widened to double
     T db[6][6];              // b[n+1][m] - b[n][m] of the Cash-Karp tableau
     T c[6], cst[6];          // 5th- and 4th-order weights

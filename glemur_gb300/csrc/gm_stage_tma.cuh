@@ -155,7 +155,8 @@ __device__ __forceinline__ void ld_b(const double* d, double v[3]) {
 // slack):
 //   XR position-plane slots (the tile + 2-point halo, three components),
 //   2 slots of B0s planes (same box),
-//   2 slots of k-planes (the n arrays k_0..k_{n-1} over the tile),
+//   2 slots of k-planes (the n arrays k_0..k_{n-1} over the tile; 1 slot in
+//   the last stage with pressure, so that three CTAs fit on an SM),
 //   2 B planes (float4 per point: B and a pad),
 //   XR + 4 mbarriers, warp maxima, the abort flag and the work-item slot.
 // Every slot is a multiple of 128 bytes, the alignment TMA destinations need.
@@ -166,12 +167,16 @@ struct StageSmem {
     static constexpr int NK = NS;                                 // k arrays read by stage NS
     static constexpr int KBOX = 3 * TY2 * TX;                     // elements of one k-array plane
     static constexpr int KSLOT = NK * KBOX;
+    // k-plane slots: two (the next plane streams in while this one is read),
+    // one in the last stage with pressure (its plane is loaded during the B
+    // phase of the same iteration, behind a second barrier)
+    static constexpr int KS = (PRESS && NS == 5) ? 1 : 2;
     static constexpr int PLANE_B = 4 * BY2 * BX2;
     static constexpr size_t OFF_B0 = sizeof(T) * (size_t)XR * SLOT;
     static constexpr size_t OFF_K = OFF_B0 + sizeof(T) * 2 * (size_t)SLOT;
-    static constexpr size_t OFF_B = OFF_K + sizeof(T) * 2 * (size_t)KSLOT;
+    static constexpr size_t OFF_B = OFF_K + sizeof(T) * KS * (size_t)KSLOT;
     static constexpr size_t OFF_BAR = OFF_B + sizeof(T) * 2 * (size_t)PLANE_B;
-    static constexpr int NBAR = XR + 4;                          // x slots, 2 B0s slots, 2 k slots
+    static constexpr int NBAR = XR + 2 + KS;                     // x slots, 2 B0s slots, k slots
     static constexpr size_t OFF_WMAX = OFF_BAR + 8 * NBAR;
     static constexpr size_t OFF_CTL = OFF_WMAX + 16 * TY2;
     static constexpr size_t BYTES = 128 + OFF_CTL + 64;
@@ -315,12 +320,15 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
         mbar_expect_tx(b, kPlaneBytes);
         tma_load_4d(b0r + (q & 1) * SLOT, tmb0, b, i0, j0, q + 2, 0);
     };
+    constexpr int KS = L::KS;
+    auto kbar = [&](int q) { return XR + 2 + (KS == 2 ? (q & 1) : 0); };
+    auto kslot = [&](int q) { return kr + (KS == 2 ? (q & 1) : 0) * L::KSLOT; };
     auto issue_k = [&](int q) {
-        uint64_t* b = &bars[XR + 2 + (q & 1)];
+        uint64_t* b = &bars[kbar(q)];
         mbar_expect_tx(b, kKBytes);
 #pragma unroll
         for (int m = 0; m < n; m++)
-            tma_load_4d(kr + (q & 1) * L::KSLOT + m * L::KBOX, &A.tm[5 + m], b, i0, j0, q, 0);
+            tma_load_4d(kslot(q) + m * L::KBOX, &A.tm[5 + m], b, i0, j0, q, 0);
     };
     // ring positions relative to plane kk, from one modulo per iteration
     auto xring = [&](int m, int back) { int s = m - back; s += s < 0 ? XR : 0; return xs + s * SLOT; };
@@ -361,8 +369,8 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             bool ok = true;
             while (ok && ctl->x_done < need) { ok = wait_bar(xslot(ctl->x_done + 1)); ctl->x_done++; }
             while (ok && ctl->b_done < kk - 1) { ok = wait_bar(XR + ((ctl->b_done + 1) & 1)); ctl->b_done++; }
-            if (n > 0)
-                while (ok && ctl->k_done < kk - 2) { ok = wait_bar(XR + 2 + ((ctl->k_done + 1) & 1)); ctl->k_done++; }
+            if (n > 0 && KS == 2)
+                while (ok && ctl->k_done < kk - 2) { ok = wait_bar(kbar(ctl->k_done + 1)); ctl->k_done++; }
             if (!ok) {
                 *s_abort = 1;
                 atomicOr(&st->status, (unsigned)GM_ST_TIMEOUT);
@@ -376,7 +384,10 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             const int qx = kk + 1;
             if (qx <= kend + 1 && qx > ctl->x_iss) { issue_x(qx); ctl->x_iss = qx; }
             if (kk <= kend && kk > ctl->b_iss) { issue_b0(kk); ctl->b_iss = kk; }
-            if (n > 0 && kk - 1 >= k0 && kk - 1 < kend && kk - 1 > ctl->k_iss) { issue_k(kk - 1); ctl->k_iss = kk - 1; }
+            // k planes: the next J phase's (two slots), or this one's (one slot:
+            // the previous J phase, its last reader, is behind the barrier)
+            const int qk = KS == 2 ? kk - 1 : kk - 2;
+            if (n > 0 && qk >= k0 && qk < kend && qk > ctl->k_iss) { issue_k(qk); ctl->k_iss = qk; }
         }
         const int mx = (kk + 20) % XR;      // ring slot of position plane kk
         // (3) B on plane kb = kk - 1 into B plane kb & 1
@@ -413,6 +424,20 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
         for (int l = 0; l < 3; l++) { Bm[l] = Bz[l]; Bz[l] = Bp[l]; Bp[l] = Bv[l]; }
         // (4) J, k_n and the stage position on plane kc = kk - 2
         const int kc = kk - 2;
+        if (KS == 1 && kc >= k0) {
+            // one k slot: the producer waits for this plane's k copies (issued
+            // at the top of this iteration), then a barrier publishes them
+            if (producer) {
+                bool ok = true;
+                while (ok && ctl->k_done < kc) { ok = wait_bar(kbar(ctl->k_done + 1)); ctl->k_done++; }
+                if (!ok) {
+                    *s_abort = 1;
+                    atomicOr(&st->status, (unsigned)GM_ST_TIMEOUT);
+                }
+            }
+            __syncthreads();
+            if (*s_abort) break;
+        }
         if (kc >= k0 && own) {
             const T* bc = bs + (kc & 1) * PLANE_B;
             // in-plane neighbours' B: -x, +x, -y, +y
@@ -466,7 +491,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             for (int l = 0; l < 3; l++) xa[l] = x0[ox1 + l * PLANE_C];
             const bool images = img_xy || (zPeri && (kc < 2 || kc >= nz - 2));
             const int g = gxy1 + pxy * (kc + 2);
-            const T* kp = kr + (kc & 1) * L::KSLOT + tyx;    // k_m component l at kp[(3m + l) * TX * TY2]
+            const T* kp = kslot(kc) + tyx;    // k_m component l at kp[(3m + l) * TX * TY2]
             if (!LAST) {
                 // x_{n+1} = x_n + sum_{m<=n} (b[n+1][m] - b[n][m]) k_m (rungeKutta.cu:216-227)
 #pragma unroll
@@ -554,7 +579,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
         for (int q = ctl->x_done + 1; q <= ctl->x_iss; q++) wait_bar(xslot(q));
         for (int q = ctl->b_done + 1; q <= ctl->b_iss; q++) wait_bar(XR + (q & 1));
         if (n > 0)
-            for (int q = ctl->k_done + 1; q <= ctl->k_iss; q++) wait_bar(XR + 2 + (q & 1));
+            for (int q = ctl->k_done + 1; q <= ctl->k_iss; q++) wait_bar(kbar(q));
     }
     if (bad) atomicOr(&st->status, (unsigned)GM_ST_NAN);
     if (LAST) {
