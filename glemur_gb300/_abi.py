@@ -99,7 +99,8 @@ class GmState(C.Structure):
 
 class GmReduction(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("B2", "BMax", "JMax", "JxB_B2Max", "residual", "residualPw", "minDetJac",
-                                           "wedgeMin", "convex", "errB_1ez", "errXb_XbAn", "epsilonStar")]
+                                           "wedgeMin", "convex", "errB_1ez", "errXb_XbAn", "epsilonStar", "U2",
+                                           "UMax")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -138,6 +139,8 @@ SIGNATURES = {
     "gm_download": (C.c_int, [VP, VP, VP, VP, VP]),
     "gm_download_k": (C.c_int, [VP, C.c_int, VP]),
     "gm_download_x": (C.c_int, [VP, C.c_int, VP]),
+    "gm_upload_u": (C.c_int, [VP, VP]),
+    "gm_download_u": (C.c_int, [VP, C.c_int, VP]),
     "gm_reduce_noalloc": (C.c_int, [P(GmParams), VP, VP, VP, VP, VP]),
     "gm_batch_create": (C.c_int, [P(GmParams), C.c_int, P(VP)]),
     "gm_batch_destroy": (C.c_int, [VP]),
@@ -170,8 +173,10 @@ SIGNATURES = {
     "gm_set_device": (C.c_int, [C.c_int]),
     "gm_io_write_cuda_info": (C.c_int, [C.c_char_p, C.c_int, C.c_long]),
     "gm_io_write_b0": (C.c_int, [P(GmParams), C.c_char_p, VP]),
-    "gm_io_write_dump": (C.c_int, [P(GmParams), C.c_char_p, C.c_double, C.c_double, VP, VP, VP, VP, VP, VP, VP]),
-    "gm_io_read_state": (C.c_int, [P(GmParams), C.c_char_p, C.c_char_p, VP, VP, P(C.c_double), P(C.c_double)]),
+    "gm_io_write_dump": (C.c_int, [P(GmParams), C.c_char_p, C.c_double, C.c_double, VP, VP, VP, VP, VP, VP, VP,
+                                   VP]),
+    "gm_io_read_state": (C.c_int, [P(GmParams), C.c_char_p, C.c_char_p, VP, VP, P(C.c_double), P(C.c_double),
+                                   VP]),
     "gm_io_ts_line": (C.c_int, [P(GmParams), P(GmReduction), C.c_double, C.c_double, C.c_double, C.c_int,
                                 C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int]),
     "gm_launch_count": (C.c_int64, [VP]),

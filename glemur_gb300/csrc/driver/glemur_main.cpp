@@ -65,7 +65,7 @@ template <typename T>
 int run(gm_params& p, long activeDevice) {
     const size_t G = (size_t)(p.nx + 2) * (p.ny + 2) * (p.nz + 2);
     const size_t N = (size_t)p.nx * p.ny * p.nz;
-    std::vector<T> B0(3 * G), xb(3 * G), B(3 * G), J(3 * N), D(G), cv(N), cx(N), wm(N);
+    std::vector<T> B0(3 * G), xb(3 * G), B(3 * G), J(3 * N), D(G), cv(N), cx(N), wm(N), u(3 * N);
     (void)activeDevice;
     gm_handle* h = nullptr;
     if (gm_create(&p, &h)) return fail("could not set up the device state");
@@ -85,10 +85,12 @@ int run(gm_params& p, long activeDevice) {
         if (gm_io_ts_line(&p, nullptr, B2r, 0, dt, 0, 0, 1, 1, line, sizeof line) < 0) return fail("time series");
         if (ts.append("w+", line)) return -1;
     } else {
-        if (gm_io_read_state(&p, "data/save.vtk", "data/B0.vtk", xb.data(), B0.data(), &t, &dt))
+        if (gm_io_read_state(&p, "data/save.vtk", "data/B0.vtk", xb.data(), B0.data(), &t, &dt,
+                             p.inertia ? u.data() : nullptr))
             return fail("could not read the restart state");
     }
     if (gm_upload(h, xb.data(), B0.data(), t, dt)) return fail("could not copy the state to the device");
+    if (p.inertia && p.fRestart && gm_upload_u(h, u.data())) return fail("could not copy the velocity to the device");
 
     gm_state s;
     memset(&s, 0, sizeof s);
@@ -113,18 +115,19 @@ int run(gm_params& p, long activeDevice) {
         if (s.event & (GM_EV_DUMP | GM_EV_SAVE | GM_EV_LAST)) {
             // prepareDump (diagnostics.cu:138-212), then dumpState with the adapted dt
             if (gm_download(h, xb.data(), B.data(), J.data(), D.data())) return fail("download");
+            if (p.inertia && gm_download_u(h, 5, u.data())) return fail("download");
             if (p.dumpCellVol || p.dumpConvexity || p.dumpWedgeMin)
                 if (gm_grid_fields(h, cv.data(), cx.data(), wm.data())) return fail("grid fields");
             if (s.event & GM_EV_DUMP) {
                 char name[64];
                 snprintf(name, sizeof name, "data/dump%d.vtk", dump_number<T>(s.t, s.dt, p.dtDump));
                 if (gm_io_write_dump(&p, name, s.t, s.dt, xb.data(), B.data(), J.data(), D.data(), cv.data(),
-                                     cx.data(), wm.data()))
+                                     cx.data(), wm.data(), u.data()))
                     return fail("dump");
             }
             if (s.event & (GM_EV_SAVE | GM_EV_LAST))
                 if (gm_io_write_dump(&p, "data/save.vtk", s.t, s.dt, xb.data(), B.data(), J.data(), D.data(),
-                                     cv.data(), cx.data(), wm.data()))
+                                     cv.data(), cx.data(), wm.data(), u.data()))
                     return fail("save");
         }
     }
@@ -195,10 +198,7 @@ int main(int argc, char* argv[]) {
         return -1;
     }
     printf("initial B: %s\n", p.bInit);
-    if (p.inertia) {
-        printf("error: the inertial equation (inertia = T) is not built in this implementation\n");
-        return -1;
-    }
+    if (p.inertia) printf("initial U: %s\n", p.uInit);
     if (p.pressure) printf("include pressure gradient with beta = %f\n", p.beta);
     printf("tiles = 32 x 8 columns, one launch per Runge-Kutta stage, step loop on the device\n");
     const int rc = precision == 32 ? run<float>(p, activeDevice) : run<double>(p, activeDevice);

@@ -61,7 +61,6 @@ int check_params(const gm_params* p) {
     if (strncmp(p->jMethod, "Stokes ", 7) != 0 && strncmp(p->jMethod, "Classic ", 8) != 0)
         return gm::fail(GM_EPARAM, "jMethod: the Stokes and Classic currents are implemented");
     if (p->pressure && strncmp(p->pMethod, "Classic ", 8) != 0) return gm::fail(GM_EPARAM, "pMethod must be Classic");
-    if (p->inertia) return gm::fail(GM_EPARAM, "inertia = T is not implemented");
     if (p->jxbAver) return gm::fail(GM_EPARAM, "jxbAver = T is not implemented");
     if (p->initShearA != 0 || p->initShearB != 0)
         return gm::fail(GM_EPARAM, "initial-distortion ghost corrections (initShearA/B != 0) are not implemented");
@@ -86,6 +85,8 @@ struct ImplBase {
     virtual int download(void* xb, void* B, void* J, void* D) = 0;
     virtual int download_k(int m, void* k) = 0;
     virtual int download_x(int which, void* xb) = 0;
+    virtual int upload_u(const void* u) = 0;
+    virtual int download_u(int which, void* u) = 0;
     virtual int step(gm_step_result* r) = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
@@ -101,6 +102,11 @@ struct Impl : ImplBase {
     T* X[2] = {nullptr, nullptr};
     T* XS[2] = {nullptr, nullptr};
     T* K[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // inertia: velocity (pitched inner SoA, as K): U[cur] at the step start,
+    // US stage ping-pong, KU the velocity increments
+    T* U[2] = {nullptr, nullptr};
+    T* US[2] = {nullptr, nullptr};
+    T* KU[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     T* B0 = nullptr;
     T* B0s = nullptr;           // B0 scaled for the algebraic B formula
     T* outB = nullptr;
@@ -134,7 +140,8 @@ struct Impl : ImplBase {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
         void* ptrs[] = {X[0], X[1], XS[0], XS[1], K[0], K[1], K[2], K[3], K[4], B0, B0s, outB, outJ,
-                        outD, stage_buf, eps, eps_col, st, log, part, red};
+                        outD, stage_buf, eps, eps_col, st, log, part, red, U[0], U[1], US[0], US[1],
+                        KU[0], KU[1], KU[2], KU[3], KU[4]};
         for (void* q : ptrs)
             if (q) cudaFree(q);
         if (h_st) cudaFreeHost(h_st);
@@ -175,6 +182,8 @@ struct Impl : ImplBase {
         kp.errMode = p->errMode;
         kp.refDt = p->errMode == 0;
         kp.jClassic = strncmp(p->jMethod, "Classic ", 8) == 0;
+        kp.inertia = p->inertia != 0;
+        kp.nu = (T)p->nu;
         kp.beta = (T)p->beta;
         kp.p0Amp = (T)p->p0Amp;
         kp.p0W2 = (T)(p->p0Width * p->p0Width);
@@ -216,6 +225,14 @@ struct Impl : ImplBase {
         }
         for (int m = 0; m < 5; m++)
             if ((rc = alloc((void**)&K[m], 3 * (size_t)kp.kcs * sizeof(T)))) return rc;
+        if (kp.inertia) {
+            for (int q = 0; q < 2; q++) {
+                if ((rc = alloc((void**)&U[q], 3 * (size_t)kp.kcs * sizeof(T)))) return rc;
+                if ((rc = alloc((void**)&US[q], 3 * (size_t)kp.kcs * sizeof(T)))) return rc;
+            }
+            for (int m = 0; m < 5; m++)
+                if ((rc = alloc((void**)&KU[m], 3 * (size_t)kp.kcs * sizeof(T)))) return rc;
+        }
         if ((rc = alloc((void**)&B0, NP * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&B0s, NP * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outB, 3 * NG * sizeof(T)))) return rc;
@@ -274,9 +291,10 @@ struct Impl : ImplBase {
         smem_stage = gmk::stage_smem_bytes<T>(TY, gmk::MODE_STAGE, p->pressure);
         smem_diag = gmk::stage_smem_bytes<T>(TY, gmk::MODE_DIAG, p->pressure);
         nparts = (int)(grid.x * grid.y * grid.z);
-        // the TMA kernel computes the Stokes current only; the Classic current
-        // runs in the generic kernel
-        use_tma = p->stageKernel == 0 && strncmp(p->jMethod, "Classic ", 8) != 0;
+        // the TMA kernel computes the Stokes current of the frictional
+        // equation only; the Classic current and the inertial equation run in
+        // the generic kernel
+        use_tma = p->stageKernel == 0 && strncmp(p->jMethod, "Classic ", 8) != 0 && !p->inertia;
         if (use_tma) {
             if ((rc = init_tma(nsm))) return rc;
         }
@@ -343,6 +361,9 @@ struct Impl : ImplBase {
         a.X[0] = X[0]; a.X[1] = X[1];
         a.XS[0] = XS[0]; a.XS[1] = XS[1];
         for (int m = 0; m < 5; m++) a.K[m] = K[m];
+        a.U[0] = U[0]; a.U[1] = U[1];
+        a.US[0] = US[0]; a.US[1] = US[1];
+        for (int m = 0; m < 5; m++) a.KU[m] = KU[m];
         a.B0 = B0;
         a.B0s = B0s;
         a.st = st;
@@ -368,6 +389,12 @@ struct Impl : ImplBase {
             CUDA_TRY(gmk::launch_images<T>(kp, b, stream));
         }
         launches += 10;
+        if (kp.inertia) {
+            // uInit = "nil": zero velocity (the reference allocates uu with
+            // malloc and leaves it unset, memory.cu:33-35, init.cu:362-364)
+            for (T* b : {U[0], U[1], US[0], US[1]})
+                CUDA_TRY(cudaMemsetAsync(b, 0, 3 * (size_t)kp.kcs * sizeof(T), stream));
+        }
         DevState s;
         memset(&s, 0, sizeof s);
         s.t = gp.errMode == 0 ? (double)(T)t : t;
@@ -592,6 +619,8 @@ struct Impl : ImplBase {
             r->errB_1ez = sqrt(v[gmk::R_SUM_E1]) / sqrt((double)N);
             r->errXb_XbAn = sqrt(v[gmk::R_SUM_E2]) / sqrt((double)N);
             r->epsilonStar = v[gmk::R_COUNT];
+            r->U2 = v[gmk::R_SUM_U2] * gp.dx * gp.dy * gp.dz;
+            r->UMax = v[gmk::R_MAX_U];
         }
         return GM_OK;
     }
@@ -630,9 +659,43 @@ struct Impl : ImplBase {
 
     int download_k(int m, void* k) override {
         if (m < 0 || m > 4 || !k) return gm::fail(GM_EPARAM, "gm_download_k: m must be 0..4");
-        CUDA_TRY(gmk::launch_pack_k<T>(kp, K[m], stage_buf, stream));
+        if (!kp.inertia) {
+            CUDA_TRY(gmk::launch_pack_k<T>(kp, K[m], stage_buf, stream));
+            launches++;
+            CUDA_TRY(cudaMemcpyAsync(k, stage_buf, 3 * N * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        } else {
+            // six values per point, the reference's kk record: k_x then k_u
+            CUDA_TRY(gmk::launch_pack_k6<T>(kp, K[m], KU[m], stage_buf, stream));
+            launches++;
+            CUDA_TRY(cudaMemcpyAsync(k, stage_buf, 6 * N * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        }
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    int upload_u(const void* u) override {
+        if (!kp.inertia) return gm::fail(GM_EPARAM, "gm_upload_u: the run has no velocity (inertia = F)");
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_upload_u before gm_upload");
+        if (!u) return gm::fail(GM_EPARAM, "gm_upload_u: null array");
+        int rc = read_state();
+        if (rc) return rc;
+        CUDA_TRY(cudaMemcpyAsync(stage_buf, u, 3 * N * sizeof(T), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(gmk::launch_unpack_k<T>(kp, stage_buf, U[h_st->cur], stream));
         launches++;
-        CUDA_TRY(cudaMemcpyAsync(k, stage_buf, 3 * N * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return GM_OK;
+    }
+
+    int download_u(int which, void* u) override {
+        if (!kp.inertia) return gm::fail(GM_EPARAM, "gm_download_u: the run has no velocity (inertia = F)");
+        if (which < 0 || which > 6 || !u) return gm::fail(GM_EPARAM, "gm_download_u: which must be 0..6");
+        int rc = read_state();
+        if (rc) return rc;
+        const int cur = h_st->cur;
+        const T* src = which <= 4 ? US[which & 1] : (which == 5 ? U[cur] : U[cur ^ 1]);
+        CUDA_TRY(gmk::launch_pack_k<T>(kp, src, stage_buf, stream));
+        launches++;
+        CUDA_TRY(cudaMemcpyAsync(u, stage_buf, 3 * N * sizeof(T), cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
         return GM_OK;
     }
@@ -702,8 +765,8 @@ struct Batch : BatchBase {
             p.stageKernel = 0;
             int rc = check_params(&p);
             if (rc) return rc;
-            if (strncmp(p.jMethod, "Stokes ", 7) != 0)
-                return gm::fail(GM_EPARAM, "gm_batch_create: batched cases use the Stokes current");
+            if (strncmp(p.jMethod, "Stokes ", 7) != 0 || p.inertia)
+                return gm::fail(GM_EPARAM, "gm_batch_create: batched cases use the frictional equation and the Stokes current");
             cs.emplace_back(new Impl<T>());
             if ((rc = cs.back()->init(&p))) return rc;
             cs.back()->stream = stream;
@@ -970,6 +1033,16 @@ int gm_refresh(gm_handle* h, gm_reduction* r) {
 int gm_download(gm_handle* h, void* xb, void* B, void* J, void* detJac) {
     if (!h) return gm::fail(GM_EPARAM, "null handle");
     return h->impl->download(xb, B, J, detJac);
+}
+
+int gm_upload_u(gm_handle* h, const void* u) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->upload_u(u);
+}
+
+int gm_download_u(gm_handle* h, int which, void* u) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->download_u(which, u);
 }
 
 int gm_download_k(gm_handle* h, int m, void* k) {

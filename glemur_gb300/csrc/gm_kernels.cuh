@@ -67,6 +67,8 @@ struct KP {
     T Lx, Ly, Lz, Ox, Oy, Oz;
     int xPeri, yPeri, zPeri, zUpdate, errMode, refDt;
     int jClassic;            // jMethod = "Classic": the finite-difference current (generic kernel only)
+    int inertia;             // the velocity equation (generic kernel only)
+    T nu;                    // velocity damping
     T beta, p0Amp, p0W2;     // pressure: p0(X) = beta (1 + p0Amp exp(-(X^2+Y^2)/p0W2))
     T inv_p0W2;              // 1 / p0W2
     double maxError, dtMin;  // run-precision values widened to double
@@ -88,11 +90,12 @@ enum { MODE_STAGE = 0, MODE_DIAG = 1 };
 
 // Reduction partial of one CTA (diagnostic mode).
 enum {
-    R_SUM_CROSS = 0, R_SUM_JB, R_SUM_PW, R_SUM_B2W, R_SUM_E1, R_SUM_E2,
-    R_MAX_JXBB2, R_MAX_B, R_MAX_J,
+    R_SUM_CROSS = 0, R_SUM_JB, R_SUM_PW, R_SUM_B2W, R_SUM_E1, R_SUM_E2, R_SUM_U2,
+    R_MAX_JXBB2, R_MAX_B, R_MAX_J, R_MAX_U,
     R_MIN_DET, R_MIN_WEDGE, R_MIN_CONVEX,
     R_COUNT
 };
+constexpr int R_LAST_SUM = R_SUM_U2, R_LAST_MAX = R_MAX_U;   // sums, then maxima, then minima
 
 template <typename T>
 struct StageArgs {
@@ -100,6 +103,9 @@ struct StageArgs {
     T* X[2];                 // start / new grid (roles swap on accept)
     T* XS[2];                // stage positions, ping-pong
     T* K[5];                 // k_0..k_4
+    T* U[2];                 // inertia: velocity at the step start / of the new step (roles follow X)
+    T* US[2];                // inertia: stage velocities, ping-pong
+    T* KU[5];                // inertia: velocity increments k_u,0..k_u,4
     const T* B0;
     const T* B0s;            // B0 scaled by (4 dy dz, 4 dx dz, 4 dx dy), padded layout
     DevState* st;
@@ -138,6 +144,10 @@ template <typename T>
 cudaError_t launch_scale_b0(const KP<T>& p, const T* B0, T* B0s, cudaStream_t s);
 template <typename T>
 cudaError_t launch_pack_k(const KP<T>& p, const T* k, T* aos, cudaStream_t s);
+template <typename T>
+cudaError_t launch_pack_k6(const KP<T>& p, const T* kx, const T* ku, T* aos, cudaStream_t s);
+template <typename T>
+cudaError_t launch_unpack_k(const KP<T>& p, const T* aos, T* k, cudaStream_t s);
 template <typename T>
 cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t s);
 // grid-quality fields (inner layout) of a padded grid

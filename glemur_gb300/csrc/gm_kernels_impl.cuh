@@ -397,8 +397,8 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
     double dmax = 0;      // running max of the error norm (stage 5)
     bool bad = false;     // NaN/Inf seen
     // diagnostic partials
-    double r_sum[6] = {0, 0, 0, 0, 0, 0};
-    double r_max[3] = {0, 0, 0};
+    double r_sum[7] = {0, 0, 0, 0, 0, 0, 0};
+    double r_max[4] = {0, 0, 0, 0};
     double r_min[3] = {DBL_MAX, DBL_MAX, 1.0};
 
     for (int kk = k0 - 2; kk <= kend + 1; kk++) {
@@ -488,16 +488,35 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                 const long long KC = p.kcs;
                 if (MODE == MODE_STAGE) {
                     T kn[3];
-                    cross3(Jv, Bc, kn);
-                    const T eps = p.ex[i] * p.ey[j] * p.ez[kc];
-                    const T f = dtT * eps;
+                    T g[3] = {0, 0, 0};
+                    if (PRESS) grad_p<T>(p, t, i, j, kc, t.b(kc, 3, j, i), g);
+                    // inertia: the stage velocity u_n and its increment
+                    T uc[3] = {0, 0, 0}, ku[3] = {0, 0, 0};
+                    if (!p.inertia) {
+                        cross3(Jv, Bc, kn);
+                        const T eps = p.ex[i] * p.ey[j] * p.ez[kc];
+                        const T f = dtT * eps;
 #pragma unroll
-                    for (int l = 0; l < 3; l++) kn[l] *= f;
-                    if (PRESS) {
-                        T g[3];
-                        grad_p<T>(p, t, i, j, kc, t.b(kc, 3, j, i), g);
+                        for (int l = 0; l < 3; l++) kn[l] *= f;
+                        if (PRESS) {
 #pragma unroll
-                        for (int l = 0; l < 3; l++) kn[l] += -dtT * g[l];
+                            for (int l = 0; l < 3; l++) kn[l] += -dtT * g[l];
+                        }
+                    } else {
+                        // rungeKutta.cu:195-212: k_x = dt u, k_u = dt Delta (J x B)
+                        // - dt nu u Delta - dt grad p (no epsilon profile)
+                        const T* Un = (n == 0) ? a.U[cur] : a.US[(n - 1) & 1];
+                        const T D = t.b(kc, 3, j, i);
+                        cross3(Jv, Bc, ku);
+#pragma unroll
+                        for (int l = 0; l < 3; l++) {
+                            uc[l] = Un[l * KC + klin];
+                            kn[l] = dtT * uc[l];
+                            ku[l] *= dtT * D;
+                            ku[l] -= dtT * p.nu * uc[l] * D;
+                            if (PRESS) ku[l] += -dtT * g[l];
+                        }
+                        if (!finite3d((double)ku[0], (double)ku[1], (double)ku[2])) bad = true;
                     }
                     if (!finite3d((double)kn[0], (double)kn[1], (double)kn[2])) bad = true;
                     T xa[3];
@@ -521,6 +540,21 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                         Kn[KC + klin] = kn[1];
                         Kn[2 * KC + klin] = kn[2];
                         store_pos<T>(p, a.XS[n & 1], i, j, kc, xa);
+                        if (p.inertia) {
+                            // u_{n+1} = u_n + sum_{m<=n} (b[n+1][m] - b[n][m]) k_u,m
+                            T ua[3] = {uc[0], uc[1], uc[2]};
+                            for (int m = 0; m < n; m++) {
+                                const T w = p.db[n][m];
+#pragma unroll
+                                for (int l = 0; l < 3; l++) ua[l] += w * __ldg(&a.KU[m][l * KC + klin]);
+                            }
+#pragma unroll
+                            for (int l = 0; l < 3; l++) {
+                                ua[l] += p.db[n][n] * ku[l];
+                                a.KU[n][l * KC + klin] = ku[l];
+                                a.US[n & 1][l * KC + klin] = ua[l];
+                            }
+                        }
                     } else {
                         // stage 5: x_6, then x_new, x* and the error norm (rungeKutta.cu:251-339)
                         T km[6][3];
@@ -564,6 +598,24 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                         }
                         store_pos<T>(p, a.X[cur], i, j, kc, xa);
                         store_pos<T>(p, a.X[cur ^ 1], i, j, kc, xnew);
+                        if (p.inertia) {
+                            // u_6 and u_new = u_6 + sum c k_u (rungeKutta.cu:311-322)
+#pragma unroll
+                            for (int l = 0; l < 3; l++) {
+                                T kum[6];
+#pragma unroll
+                                for (int m = 0; m < 5; m++) kum[m] = __ldg(&a.KU[m][l * KC + klin]);
+                                kum[5] = ku[l];
+                                T u6 = uc[l];
+#pragma unroll
+                                for (int m = 0; m < 6; m++) u6 += p.db[5][m] * kum[m];
+                                T un = u6;
+#pragma unroll
+                                for (int m = 0; m < 6; m++) un += p.c[m] * kum[m];
+                                a.U[cur][l * KC + klin] = u6;
+                                a.U[cur ^ 1][l * KC + klin] = un;
+                            }
+                        }
                     }
                 } else {
                     // refresh and reductions (diagnostics.cu:12-134)
@@ -604,6 +656,15 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                     r_max[0] = fmax(r_max[0], (double)q1);
                     r_max[1] = fmax(r_max[1], bnm);
                     r_max[2] = fmax(r_max[2], jnm);
+                    if (p.inertia) {
+                        // kinetic energy sum |u|^2 Delta with the boundary weights
+                        // (maths.cu:684-710) and max |u| (mag, maths.cu)
+                        const T* Uc = a.U[cur];
+                        const double u0 = Uc[klin], u1 = Uc[KC + klin], u2 = Uc[2 * KC + klin];
+                        const T uu2 = (T)u0 * (T)u0 + (T)u1 * (T)u1 + (T)u2 * (T)u2;
+                        r_sum[6] += (double)(uu2 * D) / (double)(1 << bound);
+                        r_max[3] = fmax(r_max[3], sqrt(u0 * u0 + u1 * u1 + u2 * u2));
+                    }
                     r_min[0] = fmin(r_min[0], (double)D);
                     // wedge products and convexity (maths.cu:497-643)
                     T wmin = 0;
@@ -656,8 +717,8 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
         // deterministic CTA partials: fixed-order reduction through shared memory
         __syncthreads();
         double* red = reinterpret_cast<double*>(smraw);
-        const double vals[R_COUNT] = {r_sum[0], r_sum[1], r_sum[2], r_sum[3], r_sum[4], r_sum[5],
-                                      r_max[0], r_max[1], r_max[2], r_min[0], r_min[1], r_min[2]};
+        const double vals[R_COUNT] = {r_sum[0], r_sum[1], r_sum[2], r_sum[3], r_sum[4], r_sum[5], r_sum[6],
+                                      r_max[0], r_max[1], r_max[2], r_max[3], r_min[0], r_min[1], r_min[2]};
         for (int r = 0; r < R_COUNT; r++) red[r * nthr + tid] = vals[r];
         __syncthreads();
         if (tid < R_COUNT) {
@@ -665,8 +726,8 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
             double acc = red[r * nthr];
             for (int q = 1; q < nthr; q++) {
                 const double v = red[r * nthr + q];
-                if (r <= R_SUM_E2) acc += v;
-                else if (r <= R_MAX_J) acc = fmax(acc, v);
+                if (r <= R_LAST_SUM) acc += v;
+                else if (r <= R_LAST_MAX) acc = fmax(acc, v);
                 else acc = fmin(acc, v);
             }
             const int blin = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
@@ -750,12 +811,12 @@ __global__ void k_finalize(const double* __restrict__ part, int nparts, double* 
     __shared__ double red[R_COUNT][256];
     const int tid = threadIdx.x;
     for (int r = 0; r < R_COUNT; r++) {
-        double acc = r <= R_SUM_E2 ? 0.0 : (r <= R_MAX_J ? 0.0 : DBL_MAX);
+        double acc = r <= R_LAST_SUM ? 0.0 : (r <= R_LAST_MAX ? 0.0 : DBL_MAX);
         if (r == R_MIN_CONVEX) acc = 1.0;
         for (int q = tid; q < nparts; q += blockDim.x) {
             const double v = part[(long long)q * R_COUNT + r];
-            if (r <= R_SUM_E2) acc += v;
-            else if (r <= R_MAX_J) acc = fmax(acc, v);
+            if (r <= R_LAST_SUM) acc += v;
+            else if (r <= R_LAST_MAX) acc = fmax(acc, v);
             else acc = fmin(acc, v);
         }
         red[r][tid] = acc;
@@ -766,8 +827,8 @@ __global__ void k_finalize(const double* __restrict__ part, int nparts, double* 
         double acc = red[r][0];
         for (int q = 1; q < (int)blockDim.x; q++) {
             const double v = red[r][q];
-            if (r <= R_SUM_E2) acc += v;
-            else if (r <= R_MAX_J) acc = fmax(acc, v);
+            if (r <= R_LAST_SUM) acc += v;
+            else if (r <= R_LAST_MAX) acc = fmax(acc, v);
             else acc = fmin(acc, v);
         }
         out[r] = acc;
@@ -853,6 +914,33 @@ __global__ void k_pack_k(const KP<T> p, const T* __restrict__ k, T* __restrict__
         aos[3 * q] = k[g];
         aos[3 * q + 1] = k[p.kcs + g];
         aos[3 * q + 2] = k[2 * p.kcs + g];
+    }
+}
+
+// Two k-layout arrays (x and velocity increments) into the reference's
+// six-value kk record per inner point.
+template <typename T>
+__global__ void k_pack_k6(const KP<T> p, const T* __restrict__ kx, const T* __restrict__ ku, T* __restrict__ aos) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < p.N; q += (long long)gridDim.x * blockDim.x) {
+        const long long i = q % p.nx, r = q / p.nx;
+        const long long g = i + (long long)p.kpx * r;
+#pragma unroll
+        for (int l = 0; l < 3; l++) {
+            aos[6 * q + l] = kx[l * p.kcs + g];
+            aos[6 * q + 3 + l] = ku[l * p.kcs + g];
+        }
+    }
+}
+
+// Inner-point AoS (the reference's uu layout) into the pitched k layout.
+template <typename T>
+__global__ void k_unpack_k(const KP<T> p, const T* __restrict__ aos, T* __restrict__ k) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < p.N; q += (long long)gridDim.x * blockDim.x) {
+        const long long i = q % p.nx, r = q / p.nx;
+        const long long g = i + (long long)p.kpx * r;
+        k[g] = aos[3 * q];
+        k[p.kcs + g] = aos[3 * q + 1];
+        k[2 * p.kcs + g] = aos[3 * q + 2];
     }
 }
 
@@ -1076,6 +1164,18 @@ cudaError_t launch_pack_k(const KP<T>& p, const T* k, T* aos, cudaStream_t s) {
 }
 
 template <typename T>
+cudaError_t launch_pack_k6(const KP<T>& p, const T* kx, const T* ku, T* aos, cudaStream_t s) {
+    k_pack_k6<T><<<nblk(p.N), 256, 0, s>>>(p, kx, ku, aos);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_unpack_k(const KP<T>& p, const T* aos, T* k, cudaStream_t s) {
+    k_unpack_k<T><<<nblk(p.N), 256, 0, s>>>(p, aos, k);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_export_ghosts(const KP<T>& p, T* outB, T* outD, cudaStream_t s) {
     const int nx2 = p.nx + 2, ny2 = p.ny + 2, nz2 = p.nz + 2;
     if (p.zPeri) k_export_peri<T><<<nblk((long long)nx2 * ny2), 256, 0, s>>>(p, outB, outD, 2);
@@ -1110,6 +1210,8 @@ cudaError_t launch_eps_star(const KP<T>& p, const T* B, const T* J, const T* X, 
     template cudaError_t launch_images<T>(const KP<T>&, T*, cudaStream_t);                                        \
     template cudaError_t launch_scale_b0<T>(const KP<T>&, const T*, T*, cudaStream_t);                            \
     template cudaError_t launch_pack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \
+    template cudaError_t launch_pack_k6<T>(const KP<T>&, const T*, const T*, T*, cudaStream_t);                  \
+    template cudaError_t launch_unpack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                          \
     template cudaError_t launch_export_ghosts<T>(const KP<T>&, T*, T*, cudaStream_t);                            \
     template cudaError_t launch_grid_fields<T>(const KP<T>&, const T*, T*, T*, T*, cudaStream_t);                 \
     template cudaError_t launch_eps_star<T>(const KP<T>&, const T*, const T*, const T*, T*, double*, cudaStream_t);

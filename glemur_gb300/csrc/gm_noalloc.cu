@@ -116,6 +116,8 @@ __global__ void k_plane_final(const double* __restrict__ part, int nz, double N,
     out->convex = nan("");
     out->errB_1ez = sqrt(s[S_E1]) / sqrt(N);
     out->errXb_XbAn = nan("");
+    out->U2 = nan("");            // needs the velocity
+    out->UMax = nan("");
 }
 
 }  // namespace

@@ -103,10 +103,9 @@ int write_b0(const gm_params* p, const char* path, const T* B0) {
 
 template <typename T>
 int write_dump(const gm_params* p, const char* path, double t, double dt, const T* xb, const T* B, const T* J,
-               const T* D, const T* cellVol, const T* convexity, const T* wedgeMin) {
-    if (p->inertia) return gm::fail(GM_EPARAM, "gm_io_write_dump: inertia (ufield) is not supported");
+               const T* D, const T* cellVol, const T* convexity, const T* wedgeMin, const T* u) {
     if ((p->dumpJ && !J) || (p->dumpDetJac && !D) || (p->dumpCellVol && !cellVol) ||
-        (p->dumpConvexity && !convexity) || (p->dumpWedgeMin && !wedgeMin) || !xb || !B)
+        (p->dumpConvexity && !convexity) || (p->dumpWedgeMin && !wedgeMin) || !xb || !B || (p->inertia && !u))
         return gm::fail(GM_EPARAM, "gm_io_write_dump: a field selected by the dump flags is NULL");
     FILE* f = fopen(path, "wb");
     if (!f) return gm::fail(GM_EIO, std::string("error: could not open file '") + path + "'");
@@ -146,6 +145,14 @@ int write_dump(const gm_params* p, const char* path, double t, double dt, const 
     for (size_t q = 0; q < 3 * (size_t)G; q++) w.real(B[q]);
     auto ghost = [&](int i, int j, int k) { return i == 0 || i == nx + 1 || j == 0 || j == ny + 1 || k == 0 || k == nz + 1; };
     auto inner = [&](int i, int j, int k) { return (size_t)(i - 1) + (size_t)nx * ((j - 1) + (size_t)ny * (k - 1)); };
+    if (p->inertia) {
+        // velocity, zero on the ghost layer (io.cu:269-291)
+        w.text("VECTORS ufield %s\n", rs);
+        for (int k = 0; k < nz + 2; k++)
+            for (int j = 0; j < ny + 2; j++)
+                for (int i = 0; i < nx + 2; i++)
+                    for (int l = 0; l < 3; l++) w.real(ghost(i, j, k) ? 0.0 : (double)u[3 * inner(i, j, k) + l]);
+    }
     if (p->dumpJ) {
         w.text("VECTORS jfield %s\n", rs);
         for (int k = 0; k < nz + 2; k++)
@@ -188,7 +195,8 @@ bool read_line(FILE* f, std::string& line) {
 // no effect).  A field the reference does not name (maxError) is skipped by
 // its declared size.
 template <typename T>
-int read_state(const gm_params* p, const char* save_path, const char* b0_path, T* xb, T* B0, double* t, double* dt) {
+int read_state(const gm_params* p, const char* save_path, const char* b0_path, T* xb, T* B0, double* t, double* dt,
+               T* u) {
     FILE* f = fopen(save_path, "rb");
     if (!f) return gm::fail(GM_EIO, std::string("error: could not open file '") + save_path + "'");
     std::string line;
@@ -224,6 +232,27 @@ int read_state(const gm_params* p, const char* save_path, const char* b0_path, T
     std::vector<unsigned char> raw(3 * G * sizeof(T));
     if (fread(raw.data(), 1, raw.size(), f) != raw.size()) return bad("truncated grid data");
     for (size_t q = 0; q < 3 * G; q++) get_be(raw.data() + q * sizeof(T), &xb[q]);
+    if (p->inertia) {
+        // the velocity follows B (io.cu:466-481).  The reference reads one
+        // text line, then 3G values from the "VECTORS bfield" line on, then one
+        // more text line: that lands on the velocity block only when the last
+        // bytes of the B block hold no newline byte.  Here each text line and
+        // data block is read in turn.
+        if (!read_line(f, line) || line.compare(0, 10, "POINT_DATA") != 0) return bad("no POINT_DATA line");
+        if (!read_line(f, line) || line.compare(0, 14, "VECTORS bfield") != 0) return bad("no bfield");
+        if (fread(raw.data(), 1, raw.size(), f) != raw.size()) return bad("truncated bfield");
+        if (!read_line(f, line) || line.compare(0, 14, "VECTORS ufield") != 0) return bad("no ufield");
+        if (fread(raw.data(), 1, raw.size(), f) != raw.size()) return bad("truncated ufield");
+        const int nx = p->nx, ny = p->ny, nz = p->nz;
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++)
+                    for (int l = 0; l < 3; l++) {
+                        const size_t g = (size_t)(i + 1) + (size_t)(nx + 2) * ((j + 1) + (size_t)(ny + 2) * (k + 1));
+                        get_be(raw.data() + (3 * g + l) * sizeof(T),
+                               &u[l + 3 * ((size_t)i + (size_t)nx * (j + (size_t)ny * k))]);
+                    }
+    }
     fclose(f);
     f = fopen(b0_path, "rb");
     if (!f) return gm::fail(GM_EIO, std::string("error: could not open file '") + b0_path + "'");
@@ -276,8 +305,8 @@ int ts_line(const gm_params* p, const gm_reduction* r, double B2res, double t, d
     col(p->redB2f, "B2f", (double)((T)R.B2 - (T)B2res));
     col(p->redConvex, "convex", R.convex);
     col(p->redWedgeMin, "wedgeMin", R.wedgeMin);
-    col(p->redU2 && in, "U2", 0.0);
-    col(p->redUMax && in, "UMax", 0.0);
+    col(p->redU2 && in, "U2", R.U2);
+    col(p->redUMax && in, "UMax", R.UMax);
     s += "\n";
     if ((int)s.size() + 1 > size) return gm::fail(GM_EPARAM, "gm_io_ts_line: buffer too small");
     memcpy(buf, s.c_str(), s.size() + 1);
@@ -382,23 +411,23 @@ int gm_io_write_b0(const gm_params* p, const char* path, const void* B0) {
 
 int gm_io_write_dump(const gm_params* p, const char* path, double t, double dt, const void* xb, const void* B,
                      const void* J, const void* detJac, const void* cellVol, const void* convexity,
-                     const void* wedgeMin) {
+                     const void* wedgeMin, const void* u) {
     if (!p || !path) return gm::fail(GM_EPARAM, "gm_io_write_dump: null argument");
     if (p->precision == 32)
         return write_dump<float>(p, path, t, dt, (const float*)xb, (const float*)B, (const float*)J,
                                  (const float*)detJac, (const float*)cellVol, (const float*)convexity,
-                                 (const float*)wedgeMin);
+                                 (const float*)wedgeMin, (const float*)u);
     return write_dump<double>(p, path, t, dt, (const double*)xb, (const double*)B, (const double*)J,
                               (const double*)detJac, (const double*)cellVol, (const double*)convexity,
-                              (const double*)wedgeMin);
+                              (const double*)wedgeMin, (const double*)u);
 }
 
 int gm_io_read_state(const gm_params* p, const char* save_path, const char* b0_path, void* xb, void* B0,
-                     double* t, double* dt) {
-    if (!p || !save_path || !b0_path || !xb || !B0 || !t || !dt)
+                     double* t, double* dt, void* u) {
+    if (!p || !save_path || !b0_path || !xb || !B0 || !t || !dt || (p->inertia && !u))
         return gm::fail(GM_EPARAM, "gm_io_read_state: null argument");
-    return p->precision == 32 ? read_state<float>(p, save_path, b0_path, (float*)xb, (float*)B0, t, dt)
-                              : read_state<double>(p, save_path, b0_path, (double*)xb, (double*)B0, t, dt);
+    return p->precision == 32 ? read_state<float>(p, save_path, b0_path, (float*)xb, (float*)B0, t, dt, (float*)u)
+                              : read_state<double>(p, save_path, b0_path, (double*)xb, (double*)B0, t, dt, (double*)u);
 }
 
 int gm_io_ts_line(const gm_params* p, const gm_reduction* r, double B2res, double t, double dt, int it,

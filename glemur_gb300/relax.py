@@ -125,7 +125,8 @@ class Relaxation:
         return xb
 
     def k(self, m: int) -> np.ndarray:
-        k = np.empty(self.I + (3,), self.dtype)
+        """k_m, [nz, ny, nx, 3] (or 6 with inertia: position then velocity increment)."""
+        k = np.empty(self.I + (6 if self.p.inertia else 3,), self.dtype)
         check(self.lib.gm_download_k(self.h, m, ptr(k)), "gm_download_k")
         return k
 
@@ -133,6 +134,18 @@ class Relaxation:
         x = np.empty(self.G + (3,), self.dtype)
         check(self.lib.gm_download_x(self.h, which, ptr(x)), "gm_download_x")
         return x
+
+    def upload_u(self, u: np.ndarray):
+        """Velocity of an inertia run at the inner points, [nz, ny, nx, 3]."""
+        u = np.ascontiguousarray(u, dtype=self.dtype)
+        assert u.shape == self.I + (3,)
+        check(self.lib.gm_upload_u(self.h, ptr(u)), "gm_upload_u")
+
+    def u(self, which: int = 5) -> np.ndarray:
+        """Velocity: which = 0..4 stage velocity u_{which+1}; 5 the current one; 6 u_new."""
+        u = np.empty(self.I + (3,), self.dtype)
+        check(self.lib.gm_download_u(self.h, which, ptr(u)), "gm_download_u")
+        return u
 
     @property
     def launches(self) -> int:

@@ -173,6 +173,9 @@ typedef struct gm_reduction {
     double errXb_XbAn;   /* rms |x - x_analytic| (maths.cu:332-377)             */
     double epsilonStar;  /* force-free parameter eps* along the central column
                             (maths.cu:203-290, diagnostics.cu:32-47)            */
+    double U2;           /* inertia: sum |u|^2 detJac with the boundary weights of B2
+                            * dx dy dz (maths.cu:684-710, diagnostics.cu:114-122); 0 without */
+    double UMax;         /* inertia: max |u| (diagnostics.cu:124-130); 0 without        */
 } gm_reduction;
 
 typedef struct gm_handle gm_handle;
@@ -263,8 +266,10 @@ int gm_download(gm_handle* h, void* xb, void* B, void* J, void* detJac);
  * the 8 corner wedge products (gridWedgeMin, maths.cu:494-569). */
 int gm_grid_fields(gm_handle* h, void* cellVol, void* convexity, void* wedgeMin);
 
-/* Stage increments k_0..k_4 of the last step (inner AoS, 3*nx*ny*nz each, in
- * the reference kk layout src/rungeKutta.cu:236) -- for stage parity tests. */
+/* Stage increments k_0..k_4 of the last step (inner AoS in the reference kk
+ * layout src/rungeKutta.cu:236: 3*nx*ny*nz values each, or 6*nx*ny*nz with
+ * inertia, the position increment then the velocity increment per point)
+ * -- for stage parity tests. */
 int gm_download_k(gm_handle* h, int m, void* k);
 
 /* Grid buffers of the last step in the reference layout (ghosted AoS):
@@ -272,6 +277,17 @@ int gm_download_k(gm_handle* h, int m, void* k);
  * (the xb_tmp of src/rungeKutta.cu:234); 5: x_6, the start grid of a
  * rejected retry; 6: x_new of the combine (src/rungeKutta.cu:345). */
 int gm_download_x(gm_handle* h, int which, void* xb);
+
+/* Velocity of an inertia run (inertia = T), inner points, AoS 3*nx*ny*nz in
+ * the layout of the reference's uu (src/global.h:143, rungeKutta.cu:147-150).
+ * gm_upload zeroes it (uInit = "nil", src/init.cu:362-364); gm_upload_u, after
+ * gm_upload, sets the velocity of the step start (the restart path,
+ * src/io.cu:466-481).  gm_download_u: which = 0..4: stage velocity u_{which+1}
+ * (uu_tmp of src/rungeKutta.cu:238-241); 5: the current velocity (u_6, the
+ * start of a rejected retry, or the accepted u_new); 6: u_new of the last
+ * combine (uu_new, src/rungeKutta.cu:345-350).  GM_EPARAM without inertia. */
+int gm_upload_u(gm_handle* h, const void* u);
+int gm_download_u(gm_handle* h, int which, void* u);
 
 /* Largest nz that gm_reduce_noalloc accepts: the number of per-plane partial
  * sums its fixed scratch array holds. */
@@ -287,7 +303,8 @@ int gm_download_x(gm_handle* h, int which, void* xb);
  *   B, J, detJac: DEVICE arrays of REAL in the layouts gm_download returns
  *                 (B ghosted AoS, J inner AoS, detJac ghosted scalar).
  *   out:          DEVICE pointer to one gm_reduction; wedgeMin, convex and
- *                 errXb_XbAn need the grid and are set to NaN.
+ *                 errXb_XbAn need the grid and U2, UMax the velocity: they
+ *                 are set to NaN; epsilonStar is not written.
  *   stream:       cudaStream_t to run on (NULL: the legacy default stream).
  * The per-plane partial sums live in one fixed device array of
  * GM_NOALLOC_MAX_PLANES x 16 doubles (512 KiB, held by every GPU that loads
@@ -417,18 +434,23 @@ int gm_io_write_cuda_info(const char* path, int precision, long activeDevice);
 /* data/B0.vtk: STRUCTURED_POINTS, ghosts included (io.cu:167-205). */
 int gm_io_write_b0(const gm_params* p, const char* path, const void* B0);
 /* data/dump<n>.vtk or data/save.vtk: STRUCTURED_GRID with the 9 parameter
- * fields, POINTS xb, VECTORS bfield and, as p->dump* select, VECTORS jfield
- * (zero ghosts), SCALARS detJac / cellVol / convexity / wedgeMin
- * (io.cu:209-386, 503-538).  J, cellVol, convexity, wedgeMin are inner
- * layout; the others ghosted. */
+ * fields, POINTS xb, VECTORS bfield, with inertia VECTORS ufield (zero
+ * ghosts) and, as p->dump* select, VECTORS jfield (zero ghosts), SCALARS
+ * detJac / cellVol / convexity / wedgeMin (io.cu:209-386, 503-538).  J, u,
+ * cellVol, convexity, wedgeMin are inner layout; the others ghosted.  u may be
+ * NULL when p->inertia is 0. */
 int gm_io_write_dump(const gm_params* p, const char* path, double t, double dt, const void* xb, const void* B,
                      const void* J, const void* detJac, const void* cellVol, const void* convexity,
-                     const void* wedgeMin);
-/* Restart: t, dt and xb from a save file, B0 from a B0 file (io.cu:390-499).
- * Grid sizes come from p, as in the reference, which passes its parameters to
- * readState by value. */
+                     const void* wedgeMin, const void* u);
+/* Restart: t, dt and xb (and, with inertia, the velocity u, inner AoS) from a
+ * save file, B0 from a B0 file (io.cu:390-499).  Grid sizes come from p, as in
+ * the reference, which passes its parameters to readState by value.  The
+ * reference skips the B block before the velocity with a read that starts at
+ * the "VECTORS bfield" line (io.cu:468-473) and finds the velocity only when
+ * the end of the B block holds no newline byte; here the file is read block
+ * by block. */
 int gm_io_read_state(const gm_params* p, const char* save_path, const char* b0_path, void* xb, void* B0,
-                     double* t, double* dt);
+                     double* t, double* dt, void* u);
 /* One time-series line (io.cu:542-678) into buf: the header line when
  * header != 0 (toFile != 0 labels the error column "maxDelta" as the file
  * does, else "maxError" as stdout does), else the row for (it, t, dt,

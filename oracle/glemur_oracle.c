@@ -62,12 +62,16 @@ typedef struct {
     int errMode;
     R p0Amp, p0Width;
     int jClassic;              /* jMethod = "Classic" (else "Stokes")            */
+    int inertia;               /* the velocity equation (rungeKutta.cu:195-212)  */
+    R nu;                      /* velocity damping                               */
 } P;
 
 typedef struct orc_state {
     P p;
     size_t NG, N;              /* ghosted and inner point counts               */
     R *B0, *B, *xb, *xb_tmp, *xb_new, *J, *kk, *detJac, *gradP;
+    R *uu, *uu_tmp, *uu_new;   /* velocity (inertia): inner points, AoS          */
+    int nVar;                  /* variables per point in kk: 3, or 6 with inertia */
     R t, dt;
     int timeIndex;
     R b[7][6], c[6], cs[6];
@@ -102,6 +106,8 @@ static void to_P(const gm_params* g, P* p) {
     p->errMode = g->errMode;
     p->p0Amp = (R)g->p0Amp; p->p0Width = (R)g->p0Width;
     p->jClassic = strncmp(g->jMethod, "Classic ", 8) == 0;
+    p->inertia = g->inertia != 0;
+    p->nu = (R)g->nu;
 }
 
 /* ghosted (i, j, k in 0..n+1) and inner (0..n-1) linear point indices */
@@ -223,6 +229,8 @@ int orc_init_state(const gm_params* g, R* B0, R* xb) {
 /* State handling                                                            */
 /* ------------------------------------------------------------------------ */
 
+void orc_destroy(orc_state* s);
+
 orc_state* orc_create(const gm_params* g, const R* B0, const R* xb, double t, double dt) {
     orc_state* s = (orc_state*)calloc(1, sizeof(orc_state));
     if (!s) return NULL;
@@ -235,11 +243,18 @@ orc_state* orc_create(const gm_params* g, const R* B0, const R* xb, double t, do
     s->xb_tmp = (R*)calloc(3 * s->NG, sizeof(R));
     s->xb_new = (R*)calloc(3 * s->NG, sizeof(R));
     s->J = (R*)calloc(3 * s->N, sizeof(R));
-    s->kk = (R*)calloc(18 * s->N, sizeof(R));
+    s->nVar = g->inertia ? 6 : 3;
+    s->kk = (R*)calloc(6 * (size_t)s->nVar * s->N, sizeof(R));
     s->detJac = (R*)calloc(s->NG, sizeof(R));
     s->gradP = (R*)calloc(3 * s->N, sizeof(R));
-    if (!s->B0 || !s->B || !s->xb || !s->xb_tmp || !s->xb_new || !s->J || !s->kk || !s->detJac || !s->gradP) {
-        free(s);
+    /* uInit = "nil": zero velocity (memory.cu:33-35 allocates uu with malloc
+     * and init.cu:362-364 leaves it unset; zero-filled here) */
+    s->uu = (R*)calloc(3 * s->N, sizeof(R));
+    s->uu_tmp = (R*)calloc(3 * s->N, sizeof(R));
+    s->uu_new = (R*)calloc(3 * s->N, sizeof(R));
+    if (!s->B0 || !s->B || !s->xb || !s->xb_tmp || !s->xb_new || !s->J || !s->kk || !s->detJac || !s->gradP ||
+        !s->uu || !s->uu_tmp || !s->uu_new) {
+        orc_destroy(s);
         return NULL;
     }
     memcpy(s->B0, B0, 3 * s->NG * sizeof(R));
@@ -258,6 +273,7 @@ void orc_destroy(orc_state* s) {
     if (!s) return;
     free(s->B0); free(s->B); free(s->xb); free(s->xb_tmp); free(s->xb_new);
     free(s->J); free(s->kk); free(s->detJac); free(s->gradP);
+    free(s->uu); free(s->uu_tmp); free(s->uu_new);
     free(s);
 }
 
@@ -268,7 +284,14 @@ void orc_get(const orc_state* s, R* xb, R* B, R* J, R* detJac) {
     if (detJac) memcpy(detJac, s->detJac, s->NG * sizeof(R));
 }
 
-void orc_get_k(const orc_state* s, int m, R* k) { memcpy(k, &s->kk[3 * s->N * (size_t)m], 3 * s->N * sizeof(R)); }
+/* k_m in the reference's kk layout: nVar values per inner point (x part, then
+ * the velocity part with inertia) */
+void orc_get_k(const orc_state* s, int m, R* k) {
+    memcpy(k, &s->kk[(size_t)s->nVar * s->N * (size_t)m], (size_t)s->nVar * s->N * sizeof(R));
+}
+/* velocity at the inner points (AoS): the current one, or u_new of the last combine */
+void orc_get_u(const orc_state* s, int which, R* u) { memcpy(u, which ? s->uu_new : s->uu, 3 * s->N * sizeof(R)); }
+void orc_set_u(orc_state* s, const R* u) { memcpy(s->uu, u, 3 * s->N * sizeof(R)); }
 void orc_get_xnew(const orc_state* s, R* xn) { memcpy(xn, s->xb_new, 3 * s->NG * sizeof(R)); }
 
 void orc_get_scalars(const orc_state* s, double* out) {
@@ -799,20 +822,42 @@ static void kk_stage(orc_state* s, int n, R dt) {
         for (j = 0; j < p->ny; j++)
             for (i = 0; i < p->nx; i++) {
                 size_t g = GI(p, i + 1, j + 1, k + 1), q = II(p, i, j, k);
-                R kn[3], xs[3], epsilon;
-                cross3(&s->J[3 * q], &s->B[3 * g], kn);
-                epsilon = eps_profile(p, i, j, k);
-                for (l = 0; l < 3; l++) {
-                    kn[l] *= dt * epsilon;
-                    if (p->pressure) kn[l] += -dt * s->gradP[3 * q + l];
+                const int nV = s->nVar;
+                R kn[6], xs[3], epsilon;
+                if (!p->inertia) {
+                    cross3(&s->J[3 * q], &s->B[3 * g], kn);
+                    epsilon = eps_profile(p, i, j, k);
+                    for (l = 0; l < 3; l++) {
+                        kn[l] *= dt * epsilon;
+                        if (p->pressure) kn[l] += -dt * s->gradP[3 * q + l];
+                    }
+                } else {
+                    /* rungeKutta.cu:195-212: k_x = dt u, k_u = dt Delta (J x B)
+                     * - dt nu u Delta - dt grad p (no epsilon profile) */
+                    const R D = s->detJac[g];
+                    cross3(&s->J[3 * q], &s->B[3 * g], &kn[3]);
+                    for (l = 0; l < 3; l++) {
+                        const R u = s->uu[3 * q + l];
+                        kn[l] = dt * u;
+                        kn[3 + l] *= dt * D;
+                        kn[3 + l] -= dt * p->nu * u * D;
+                        if (p->pressure) kn[3 + l] += -dt * s->gradP[3 * q + l];
+                    }
                 }
-                for (l = 0; l < 3; l++) s->kk[3 * (N * (size_t)n + q) + l] = kn[l];
+                for (l = 0; l < nV; l++) s->kk[(size_t)nV * (N * (size_t)n + q) + l] = kn[l];
                 for (l = 0; l < 3; l++) {
                     xs[l] = s->xb[3 * g + l];
                     for (m = 0; m < n + 1; m++)
-                        xs[l] += (s->b[n + 1][m] - s->b[n][m]) * s->kk[3 * (N * (size_t)m + q) + l];
+                        xs[l] += (s->b[n + 1][m] - s->b[n][m]) * s->kk[(size_t)nV * (N * (size_t)m + q) + l];
                     s->xb_tmp[3 * g + l] = xs[l];
                 }
+                if (p->inertia)
+                    for (l = 0; l < 3; l++) {
+                        R us = s->uu[3 * q + l];
+                        for (m = 0; m < n + 1; m++)
+                            us += (s->b[n + 1][m] - s->b[n][m]) * s->kk[(size_t)nV * (N * (size_t)m + q) + 3 + l];
+                        s->uu_tmp[3 * q + l] = us;
+                    }
             }
     }
 }
@@ -830,20 +875,21 @@ static void x_new_star(orc_state* s) {
         for (j = 0; j < p->ny; j++)
             for (i = 0; i < p->nx; i++) {
                 size_t g = GI(p, i + 1, j + 1, k + 1), q = II(p, i, j, k);
+                const size_t nV = (size_t)s->nVar;
                 for (l = 0; l < 3; l++) {
                     R xn = s->xb[3 * g + l], xs = s->xb[3 * g + l], dl;
                     if (l < 2 || p->zUpdate) {
                         if (p->errMode == 0) {
                             for (n = 0; n < 6; n++) {
-                                xn += s->c[n] * s->kk[3 * (N * (size_t)n + q) + l];
-                                xs += s->cs[n] * s->kk[3 * (N * (size_t)n + q) + l];
+                                xn += s->c[n] * s->kk[nV * (N * (size_t)n + q) + l];
+                                xs += s->cs[n] * s->kk[nV * (N * (size_t)n + q) + l];
                             }
                             dl = (R)fabs((double)(xn - xs));
                         } else {
                             double e = 0;
                             for (n = 0; n < 6; n++) {
-                                xn += s->c[n] * s->kk[3 * (N * (size_t)n + q) + l];
-                                e += ((double)s->c[n] - (double)s->cs[n]) * (double)s->kk[3 * (N * (size_t)n + q) + l];
+                                xn += s->c[n] * s->kk[nV * (N * (size_t)n + q) + l];
+                                e += ((double)s->c[n] - (double)s->cs[n]) * (double)s->kk[nV * (N * (size_t)n + q) + l];
                             }
                             dl = (R)fabs(e);
                         }
@@ -853,6 +899,13 @@ static void x_new_star(orc_state* s) {
                     s->xb_new[3 * g + l] = xn;
                     if (dl > lmax) lmax = dl;   /* maxValue semantics: NaN never wins */
                 }
+                /* u_new = u + sum c k_u (rungeKutta.cu:311-322); the error is x's only */
+                if (p->inertia)
+                    for (l = 0; l < 3; l++) {
+                        R un = s->uu[3 * q + l];
+                        for (n = 0; n < 6; n++) un += s->c[n] * s->kk[nV * (N * (size_t)n + q) + 3 + l];
+                        s->uu_new[3 * q + l] = un;
+                    }
             }
         if (lmax > gmax) gmax = lmax;
     }
@@ -878,6 +931,7 @@ void orc_stage(orc_state* s, int n) {
     kk_stage(s, n, s->dt);
     set_grid_peri(&s->p, s->xb_tmp);
     memcpy(s->xb, s->xb_tmp, 3 * s->NG * sizeof(R));
+    if (s->p.inertia) memcpy(s->uu, s->uu_tmp, 3 * s->N * sizeof(R));   /* main.cu:296-305 */
 }
 
 /* xNewStar + setGridPeri(xb_new), src/main.cu:309-315. */
@@ -899,6 +953,7 @@ int orc_step(orc_state* s, int nCycle) {
     if (s->maxDelta < p->maxError) {
         s->t += s->dt;
         memcpy(s->xb, s->xb_new, 3 * s->NG * sizeof(R));
+        if (p->inertia) memcpy(s->uu, s->uu_new, 3 * s->N * sizeof(R));   /* main.cu:331-339 */
         orc_refresh_fields(s);
         if (s->maxDelta > 0) s->dt = (R)((double)s->dt * pow(0.9 * (double)p->maxError / (double)s->maxDelta, (double)(R)0.2));
         s->timeIndex++;
@@ -965,8 +1020,9 @@ void orc_reduce(const orc_state* s, gm_reduction* r) {
     const P* p = &s->p;
     int k;
     double B2 = 0, res = 0, resn = 0, resd = 0, Bmax = 0, Jmax = 0, jxbmax = 0, mind = 1e300, wmin = 1e300, e1 = 0, e2 = 0;
+    double U2 = 0, Umax = 0;
     int convex = 1;
-#pragma omp parallel for schedule(static) reduction(+ : B2, res, resn, resd, e1, e2) reduction(max : Bmax, Jmax, jxbmax) reduction(min : mind, wmin, convex)
+#pragma omp parallel for schedule(static) reduction(+ : B2, res, resn, resd, e1, e2, U2) reduction(max : Bmax, Jmax, jxbmax, Umax) reduction(min : mind, wmin, convex)
     for (k = 0; k < p->nz; k++) {
         int i, j;
         for (j = 0; j < p->ny; j++)
@@ -1001,6 +1057,13 @@ void orc_reduce(const orc_state* s, gm_reduction* r) {
                 }
                 bound = (i == 0) + (j == 0) + (k == 0) + (i == p->nx - 1) + (j == p->ny - 1) + (k == p->nz - 1);
                 B2 += (double)b2 * (double)s->detJac[g] / (double)(1 << bound);
+                if (p->inertia) {
+                    /* U2_det (maths.cu:684-710) and mag (diagnostics.cu:124-130) */
+                    const R* u = &s->uu[3 * q];
+                    const double un = sqrt((double)u[0] * u[0] + (double)u[1] * u[1] + (double)u[2] * u[2]);
+                    U2 += (double)(dot3(u, u) * s->detJac[g]) / (double)(1 << bound);
+                    if (un > Umax) Umax = un;
+                }
                 wm = wedge_min_at(s, i, j, k, &cv);
                 if ((double)wm < wmin) wmin = wm;
                 if (cv < convex) convex = cv;
@@ -1045,6 +1108,8 @@ void orc_reduce(const orc_state* s, gm_reduction* r) {
         }
     }
     r->B2 = B2 * (double)p->dx * (double)p->dy * (double)p->dz;
+    r->U2 = U2 * (double)p->dx * (double)p->dy * (double)p->dz;
+    r->UMax = Umax;
     r->BMax = Bmax;
     r->JMax = Jmax;
     r->JxB_B2Max = jxbmax;

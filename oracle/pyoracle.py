@@ -33,6 +33,8 @@ def _lib(bits: int) -> C.CDLL:
     lib.orc_init_state.restype = C.c_int
     lib.orc_get.argtypes = [vp, vp, vp, vp, vp]
     lib.orc_get_k.argtypes = [vp, C.c_int, vp]
+    lib.orc_get_u.argtypes = [vp, C.c_int, vp]
+    lib.orc_set_u.argtypes = [vp, vp]
     lib.orc_get_xnew.argtypes = [vp, vp]
     lib.orc_get_scalars.argtypes = [vp, vp]
     lib.orc_set_time.argtypes = [vp, C.c_double, C.c_double, C.c_int]
@@ -130,7 +132,7 @@ class Oracle:
         return dict(xb=xb, B=B, J=J, detJac=dj)
 
     def k(self, m):
-        k = np.zeros(self.I + (3,), self.dtype)
+        k = np.zeros(self.I + (6 if self.p.inertia else 3,), self.dtype)
         self.lib.orc_get_k(self.h, m, _p(k))
         return k
 
@@ -138,6 +140,16 @@ class Oracle:
         x = np.zeros(self.G + (3,), self.dtype)
         self.lib.orc_get_xnew(self.h, _p(x))
         return x
+
+    def u(self, new=False):
+        """Velocity (inertia) at the inner points: the current one, or u_new of the last combine."""
+        u = np.zeros(self.I + (3,), self.dtype)
+        self.lib.orc_get_u(self.h, 1 if new else 0, _p(u))
+        return u
+
+    def set_u(self, u):
+        u = np.ascontiguousarray(u, dtype=self.dtype)
+        self.lib.orc_set_u(self.h, _p(u))
 
     def reduce(self):
         from glemur_gb300._abi import GmReduction
@@ -165,6 +177,7 @@ class RefLauncher:
         lib.ref_time_steps.argtypes = [C.c_int, vp, vp]
         lib.ref_get.argtypes = [vp, vp, vp, vp]
         lib.ref_get_k.argtypes = [C.c_int, vp]
+        lib.ref_get_u.argtypes = [C.c_int, vp]
         lib.ref_get_xnew.argtypes = [vp]
         lib.ref_scalars.argtypes = [vp]
         lib.ref_last_error.restype = C.c_char_p
@@ -228,9 +241,14 @@ class RefLauncher:
         return dict(xb=xb, B=B, J=J, detJac=dj)
 
     def k(self, m):
-        k = np.zeros(self.I + (3,), self.dtype)
+        k = np.zeros(self.I + (6 if self.p.inertia else 3,), self.dtype)
         self._chk(self.lib.ref_get_k(m, _p(k)), "ref_get_k")
         return k
+
+    def u(self, new=False):
+        u = np.zeros(self.I + (3,), self.dtype)
+        self._chk(self.lib.ref_get_u(1 if new else 0, _p(u)), "ref_get_u")
+        return u
 
     def xnew(self):
         x = np.zeros(self.G + (3,), self.dtype)

@@ -305,6 +305,7 @@ int stage(int n) {
     if (rc) return rc;
     SYNC();
     CK(D.MemcpyDtoD(S.d.xb, S.d.xb_tmp, gbytes()));
+    if (S.gp.inertia) CK(D.MemcpyDtoD(S.d.uu, S.d.uu_tmp, 3 * S.N * S.rs));   // main.cu:296-305
     SYNC();
     return 0;
 }
@@ -362,6 +363,7 @@ int step(int nCycle, int* accepted) {
     if (S.maxDelta < S.gp.maxError) {
         S.t = to_real(S.t + S.dt);
         CK(D.MemcpyDtoD(S.d.xb, S.d.xb_new, gbytes()));
+        if (S.gp.inertia) CK(D.MemcpyDtoD(S.d.uu, S.d.uu_new, 3 * S.N * S.rs));   // main.cu:331-339
         SYNC();
         rc = fields();
         if (rc) return rc;
@@ -405,7 +407,7 @@ void ref_close(void) {
 int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* xb, double t, double dt) {
     if (!load_driver()) return -3;
     ref_close();
-    if (g->inertia || g->jxbAver) { g_err = "inertia/jxbAver runs are not driven by this launcher"; return -1; }
+    if (g->jxbAver) { g_err = "jxbAver runs are not driven by this launcher"; return -1; }
     S.classic = strncmp(g->jMethod, "Classic ", 8) == 0;
     if (strncmp(g->jMethod, "Stokes ", 7) != 0 && !S.classic) { g_err = "only jMethod = Stokes or Classic"; return -1; }
     S.prec = g->precision;
@@ -466,9 +468,10 @@ int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* 
             }
         }
     }
-    // block and grid shapes, src/main.cu:130-157 (inertia = false)
+    // block and grid shapes, src/main.cu:130-157
     int E = S.prec == 32 ? 1 : 0;
     S.block[0] = 5 + E; S.block[1] = 6 + E; S.block[2] = 6 + E;
+    if (g->inertia) { S.block[1] = 5 + E; S.block[2] = 4 + E; }
     S.grid[0] = (g->nx - 1) / S.block[0] + 1;
     S.grid[1] = (g->ny - 1) / S.block[1] + 1;
     S.grid[2] = (g->nz - 1) / S.block[2] + 1;
@@ -489,6 +492,13 @@ int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* 
         (rc = alloc(&S.d.detJac, S.NG * S.rs)) || (rc = alloc(&S.dmax, nblk * S.rs)) ||
         (rc = alloc(&S.dtmp, (nblk / 64 + 2) * S.rs)))
         return rc;
+    if (g->inertia) {
+        // kk holds 6 variables per point; uu starts at zero (uInit = "nil")
+        if ((rc = alloc(&S.d.uu, vi)) || (rc = alloc(&S.d.uu_tmp, vi)) || (rc = alloc(&S.d.uu_new, vi))) return rc;
+        D.MemFree(S.d.kk);
+        S.d.kk = 0;
+        if ((rc = alloc(&S.d.kk, 12 * vi))) return rc;
+    }
     // initial copies, src/main.cu:181-215
     CK(D.MemcpyHtoD(S.d.B0, B0, v));
     CK(D.MemcpyHtoD(S.d.xb, xb, v));
@@ -563,7 +573,16 @@ int ref_get(void* xb, void* B, void* J, void* detJac) {
 
 int ref_get_k(int m, void* k) {
     SYNC();
-    CK(D.MemcpyDtoH(k, S.d.kk + (CUdeviceptr)(3 * S.N * S.rs * (size_t)m), 3 * S.N * S.rs));
+    const size_t nv = S.gp.inertia ? 6 : 3;
+    CK(D.MemcpyDtoH(k, S.d.kk + (CUdeviceptr)(nv * S.N * S.rs * (size_t)m), nv * S.N * S.rs));
+    return 0;
+}
+
+// velocity (inertia): 0 the current uu, 1 uu_new of the last combine
+int ref_get_u(int which, void* u) {
+    SYNC();
+    if (!S.gp.inertia) { g_err = "no velocity without inertia"; return -1; }
+    CK(D.MemcpyDtoH(u, which ? S.d.uu_new : S.d.uu, 3 * S.N * S.rs));
     return 0;
 }
 

@@ -16,6 +16,8 @@ reference's boundary handling:
   every row -- updateBbound's periodic branch, boundaries.cu:278,406 -- and
   the Classic current reads it, so periodic Classic runs are checked against
   the oracle only.)
+* inertia_f64 / inertia_f32 -- the velocity equation (inertia = T,
+  src/rungeKutta.cu:195-212, 311-322) with damping nu = 1.
 """
 from __future__ import annotations
 
@@ -49,6 +51,11 @@ def make(name: str):
         p = _braid((17, 12, 17), 64 if name.endswith("64") else 32, peri=(0, 0, 0))
         p.set_str("jMethod", "Classic")
         return configs.derive(p)
+    if name in ("inertia_f64", "inertia_f32"):
+        p = _braid((17, 17, 18), 64 if name.endswith("64") else 32)
+        p.inertia = 1
+        p.nu = 1.0
+        return configs.derive(p)
     if name == "analytic_f64":
         p = configs.defaults(64)
         p.nx, p.ny, p.nz = 16, 16, 16
@@ -67,5 +74,5 @@ def make(name: str):
 
 
 NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64", "classic_tied_f64",
-         "classic_tied_f32"]
+         "classic_tied_f32", "inertia_f64", "inertia_f32"]
 N_ACCEPTED = 10

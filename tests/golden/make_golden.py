@@ -12,6 +12,8 @@ their outputs as tests/golden/<case>.npz:
   B1, J1, D1        B, J, detJac after the first step's refresh (inner points)
   log      (maxDelta, dt, accepted) per attempt until N_ACCEPTED accepted steps
   xN, BN, JN, DN    state after N_ACCEPTED accepted steps (inner points)
+  u1, unew1, uN     with inertia: the velocity after stage 0, u_new of the
+                    first step and the velocity after N_ACCEPTED steps
 
 Needs a GPU; run on the GPU machine after the build:
   python tests/golden/make_golden.py [OUT_DIR [CASE ...]]
@@ -45,18 +47,24 @@ def generate(name: str, out_dir: Path) -> Path:
     r.stage(0)
     rec["k0"] = r.k(0)
     rec["x1"] = inner(r.get()["xb"])
+    if p.inertia:
+        rec["u1"] = r.u()
     r.close()
     r = RefLauncher(p, B0, xb)
     r.step()
     s = r.scalars()
     rec["maxDelta1"] = np.array(s["maxDelta"])
     rec["xnew1"] = inner(r.xnew())
+    if p.inertia:
+        rec["unew1"] = r.u(new=True)
     f = r.get()
     rec["B1"], rec["J1"], rec["D1"] = inner(f["B"]), f["J"], inner(f["detJac"])
     n, lg = r.run(cases.N_ACCEPTED, max_attempts=500)
     rec["log"] = np.concatenate([[[s["maxDelta"], s["dt"], 1.0 if s["timeIndex"] == 1 else 0.0]], lg])
     f = r.get()
     rec["xN"], rec["BN"], rec["JN"], rec["DN"] = inner(f["xb"]), inner(f["B"]), f["J"], inner(f["detJac"])
+    if p.inertia:
+        rec["uN"] = r.u()
     rec["scalarsN"] = np.array([r.scalars()[k] for k in ("t", "dt", "maxDelta", "timeIndex", "nAttempted")])
     r.close()
     path = out_dir / f"{name}.npz"

@@ -20,7 +20,8 @@ ROOT = Path(__file__).resolve().parent.parent
 EXE = ROOT / "glemur_gb300" / "_lib" / "glemur"
 
 
-def params_text(nCycle, restart=False, nTs=5, dtDump=0.05, dtSave=0.1, n=(16, 16, 32), pressure=False):
+def params_text(nCycle, restart=False, nTs=5, dtDump=0.05, dtSave=0.1, n=(16, 16, 32), pressure=False,
+                inertia=False):
     a = math.sqrt(2.0)
     return f"""&comp
  nx = {n[0]}; ny = {n[1]}; nz = {n[2]}
@@ -46,6 +47,8 @@ def params_text(nCycle, restart=False, nTs=5, dtDump=0.05, dtSave=0.1, n=(16, 16
  maxError = 1e-5
  xPeri = T; yPeri = T; zPeri = F
  pressure = {'T' if pressure else 'F'}
+ inertia = {'T' if inertia else 'F'}
+ nu = 1.
  beta = 0.05
  jMethod = "Stokes"
 /
@@ -55,6 +58,7 @@ def params_text(nCycle, restart=False, nTs=5, dtDump=0.05, dtSave=0.1, n=(16, 16
  dtSave = {dtSave}
  dumpJ = T; dumpDetJac = T; dumpCellVol = T; dumpConvexity = T; dumpWedgeMin = T
  redJxB_B2Max = T; redEpsilonStar = T; redB2 = T; redB2f = T; redConvex = T; redWedgeMin = T; redJMax = T
+ redU2 = T; redUMax = T
 /
 """
 
@@ -186,3 +190,36 @@ def test_invalid_and_unbuilt_methods(tmp_path):
     (d / "params.in").write_text(txt.replace('jMethod = "Stokes"', 'jMethod = "Nonsense"'))
     r = subprocess.run([str(EXE)], cwd=d, capture_output=True, text=True, timeout=120)
     assert r.returncode != 0 and "invalid method for computing J" in r.stdout
+
+
+def test_inertia_run_directory_and_restart(tmp_path):
+    """inertia = T: the velocity is written as VECTORS ufield (zero ghosts)
+    after bfield in dumps and save.vtk, the time series gains U2 and UMax,
+    and a restart from save.vtk continues exactly, velocity included."""
+    a, c = tmp_path / "a", tmp_path / "c"
+    make_run(a, 10, inertia=True)
+    out = run_exe(a)
+    assert "initial U: nil" in out
+    ts = read_ts(a)
+    assert list(ts)[-2:] == ["U2", "UMax"] and ts["UMax"][-1] > 0
+    sv = LegacyVtk(a / "data" / "save.vtk")
+    assert list(sv.point_data)[:3] == ["bfield", "ufield", "jfield"]
+    p = read_params(a, 64)
+    uf = sv.point_data["ufield"].reshape(p.nz + 2, p.ny + 2, p.nx + 2, 3)
+    assert np.abs(uf[1:-1, 1:-1, 1:-1]).max() > 0 and not uf[0].any() and not uf[:, :, 0].any()
+    # the same run through the library: the velocity of the last state
+    B0, xb = configs.init_state(p)
+    g = Relaxation(p)
+    g.upload(xb, B0)
+    g.run(10)
+    np.testing.assert_array_equal(uf[1:-1, 1:-1, 1:-1], g.u())
+    g.close()
+    (a / "params.in").write_text(params_text(10, restart=True, inertia=True))
+    run_exe(a)
+    make_run(c, 20, inertia=True)
+    run_exe(c)
+    sa, sc = LegacyVtk(a / "data" / "save.vtk"), LegacyVtk(c / "data" / "save.vtk")
+    assert sa.field["t"][0] == sc.field["t"][0]
+    np.testing.assert_array_equal(sa.points, sc.points)
+    np.testing.assert_array_equal(sa.point_data["ufield"], sc.point_data["ufield"])
+    np.testing.assert_array_equal(sa.point_data["bfield"], sc.point_data["bfield"])

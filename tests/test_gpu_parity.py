@@ -38,9 +38,14 @@ def stage_by_stage(p, ref):
         if n < 5:
             assert relerr(g.k(n), r.k(n)) < tol, f"k_{n}"
             assert relerr(inner(g.x(n)), inner(r.get()["xb"])) < tol, f"x_{n + 1}"
+            if p.inertia:
+                assert relerr(g.u(n), r.u()) < tol, f"u_{n + 1}"
     md = r.combine()
     assert relerr(inner(g.x(6)), inner(r.xnew())) < tol, "x_new"
     assert relerr(inner(g.x(5)), inner(r.get()["xb"])) < tol, "x_6"
+    if p.inertia:
+        assert relerr(g.u(6), r.u(new=True)) < tol, "u_new"
+        assert relerr(g.u(5), r.u()) < tol, "u_6"
     g.control()
     s = g.state()
     assert abs(s["maxDelta"] - md) <= max(tol * 100 * md, 1e-300)
@@ -54,7 +59,7 @@ def test_stages_match_oracle(name):
 
 
 @pytest.mark.parametrize("name", ["braid_f64", "braid_f32", "tied_f64", "press_f64", "classic_tied_f64",
-                                  "classic_tied_f32"])
+                                  "classic_tied_f32", "inertia_f64", "inertia_f32"])
 def test_stages_match_reference_kernels(name):
     stage_by_stage(cases.make(name), RefLauncher)
 
@@ -114,6 +119,10 @@ def test_run_matches_oracle(name):
     ro = o.reduce()
     for k in ("B2", "JMax", "JxB_B2Max", "residual", "residualPw", "minDetJac", "wedgeMin"):
         assert abs(red[k] - ro[k]) <= rt["red"] * abs(ro[k]), k
+    if p.inertia:
+        assert relerr(g.u(), o.u()) < rt["B"]
+        for k in ("U2", "UMax"):
+            assert ro[k] > 0 and abs(red[k] - ro[k]) <= rt["red"] * abs(ro[k]), k
     assert red["convex"] == ro["convex"]
 
 

@@ -61,7 +61,7 @@ def test_dump_file_layout_and_restart(lib, tmp_path, precision):
     path = tmp_path / "save.vtk"
     _abi.check(lib.gm_io_write_dump(C.byref(p), str(path).encode(), t, dt, _abi.ptr(f["xb"]), _abi.ptr(f["B"]),
                                     _abi.ptr(f["J"]), _abi.ptr(f["D"]), _abi.ptr(f["cv"]), _abi.ptr(f["cx"]),
-                                    _abi.ptr(f["wm"])), "write dump")
+                                    _abi.ptr(f["wm"]), None), "write dump")
     v = LegacyVtk(path)
     rs = "float" if precision == 32 else "double"
     G = (p.nx + 2) * (p.ny + 2) * (p.nz + 2)
@@ -99,7 +99,7 @@ def test_dump_file_layout_and_restart(lib, tmp_path, precision):
     B0 = np.zeros_like(f["B"])
     tt, dd = C.c_double(), C.c_double()
     _abi.check(lib.gm_io_read_state(C.byref(p), str(path).encode(), str(b0).encode(), _abi.ptr(xb), _abi.ptr(B0),
-                                    C.byref(tt), C.byref(dd)), "read state")
+                                    C.byref(tt), C.byref(dd), None), "read state")
     assert tt.value == t and dd.value == dt
     np.testing.assert_array_equal(xb, f["xb"])
     np.testing.assert_array_equal(B0, f["B"])
@@ -111,13 +111,13 @@ def test_dump_without_optional_fields(lib, tmp_path):
     f = fields(p, 2)
     path = tmp_path / "dump3.vtk"
     _abi.check(lib.gm_io_write_dump(C.byref(p), str(path).encode(), 1.0, 0.1, _abi.ptr(f["xb"]), _abi.ptr(f["B"]),
-                                    None, None, None, None, None), "write dump")
+                                    None, None, None, None, None, None), "write dump")
     v = LegacyVtk(path)
     assert list(v.point_data) == ["bfield"]
     # a selected field passed as NULL is refused
     p.dumpJ = 1
     rc = lib.gm_io_write_dump(C.byref(p), str(path).encode(), 1.0, 0.1, _abi.ptr(f["xb"]), _abi.ptr(f["B"]),
-                              None, None, None, None, None)
+                              None, None, None, None, None, None)
     assert rc == _abi.GM_EPARAM
 
 
@@ -126,11 +126,11 @@ def test_restart_reader_errors(lib, tmp_path):
     xb = np.zeros(((p.nz + 2) * (p.ny + 2) * (p.nx + 2) * 3,))
     tt, dd = C.c_double(), C.c_double()
     rc = lib.gm_io_read_state(C.byref(p), str(tmp_path / "missing.vtk").encode(), b"x", _abi.ptr(xb), _abi.ptr(xb),
-                              C.byref(tt), C.byref(dd))
+                              C.byref(tt), C.byref(dd), None)
     assert rc == _abi.GM_EIO
     (tmp_path / "short.vtk").write_bytes(b"# vtk DataFile Version 2.0\nGLEMuR data dump\n")
     rc = lib.gm_io_read_state(C.byref(p), str(tmp_path / "short.vtk").encode(), b"x", _abi.ptr(xb), _abi.ptr(xb),
-                              C.byref(tt), C.byref(dd))
+                              C.byref(tt), C.byref(dd), None)
     assert rc == _abi.GM_EIO
 
 
@@ -160,3 +160,52 @@ def test_time_series_lines(lib, precision):
     keys = hdr.split()[1:]
     assert dict(zip(keys, data))["epsilonStar"] == pytest.approx(1.25e-3, rel=1e-4)
     assert lib.gm_io_ts_line(C.byref(p), C.byref(r), 0.0, 0.0, 0.0, 0, 0.0, 0, 1, buf, 8) == _abi.GM_EPARAM
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_inertia_dump_and_restart(lib, tmp_path, precision):
+    """With inertia the dump carries VECTORS ufield after bfield, zero on the
+    ghost layer (io.cu:269-291), and the restart reads it back into the
+    inner-point velocity (io.cu:466-481)."""
+    p = small(precision)
+    p.inertia = 1
+    f = fields(p, 3)
+    u = np.ascontiguousarray(np.random.default_rng(4).normal(size=(p.nz, p.ny, p.nx, 3)).astype(p.real_dtype()))
+    path = tmp_path / "save.vtk"
+    rc = lib.gm_io_write_dump(C.byref(p), str(path).encode(), 0.5, 0.01, _abi.ptr(f["xb"]), _abi.ptr(f["B"]),
+                              _abi.ptr(f["J"]), _abi.ptr(f["D"]), _abi.ptr(f["cv"]), _abi.ptr(f["cx"]),
+                              _abi.ptr(f["wm"]), None)
+    assert rc == _abi.GM_EPARAM      # the velocity is required with inertia
+    _abi.check(lib.gm_io_write_dump(C.byref(p), str(path).encode(), 0.5, 0.01, _abi.ptr(f["xb"]), _abi.ptr(f["B"]),
+                                    _abi.ptr(f["J"]), _abi.ptr(f["D"]), _abi.ptr(f["cv"]), _abi.ptr(f["cx"]),
+                                    _abi.ptr(f["wm"]), _abi.ptr(u)), "write dump")
+    v = LegacyVtk(path)
+    assert list(v.point_data)[:3] == ["bfield", "ufield", "jfield"]
+    uf = v.point_data["ufield"].reshape(p.nz + 2, p.ny + 2, p.nx + 2, 3)
+    np.testing.assert_array_equal(uf[1:-1, 1:-1, 1:-1], u)
+    gh = np.ones((p.nz + 2, p.ny + 2, p.nx + 2), bool)
+    gh[1:-1, 1:-1, 1:-1] = False
+    assert not uf[gh].any()
+    b0 = tmp_path / "B0.vtk"
+    _abi.check(lib.gm_io_write_b0(C.byref(p), str(b0).encode(), _abi.ptr(f["B"])), "write B0")
+    xb = np.zeros_like(f["xb"])
+    B0 = np.zeros_like(f["B"])
+    ur = np.zeros_like(u)
+    tt, dd = C.c_double(), C.c_double()
+    _abi.check(lib.gm_io_read_state(C.byref(p), str(path).encode(), str(b0).encode(), _abi.ptr(xb), _abi.ptr(B0),
+                                    C.byref(tt), C.byref(dd), _abi.ptr(ur)), "read state")
+    np.testing.assert_array_equal(ur, u)
+    np.testing.assert_array_equal(xb, f["xb"])
+
+
+def test_time_series_velocity_columns(lib):
+    p = small(64)
+    p.inertia = 1
+    p.redU2 = p.redUMax = 1
+    buf = C.create_string_buffer(2048)
+    lib.gm_io_ts_line(C.byref(p), None, 0.0, 0.0, 0.0, 0, 0.0, 1, 1, buf, 2048)
+    assert buf.value.decode().split()[-2:] == ["U2", "UMax"]
+    r = _abi.GmReduction()
+    r.U2, r.UMax = 0.125, 2.5e-3
+    lib.gm_io_ts_line(C.byref(p), C.byref(r), 0.0, 1.0, 0.1, 3, 1e-6, 0, 1, buf, 2048)
+    assert buf.value.decode().split()[-2:] == ["1.25000e-01", "2.50000e-03"]
