@@ -238,7 +238,9 @@ struct Impl : ImplBase {
         if ((rc = alloc((void**)&outB, 3 * NG * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outJ, 3 * N * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outD, NG * sizeof(T)))) return rc;
-        if ((rc = alloc((void**)&stage_buf, 3 * NG * sizeof(T)))) return rc;
+        // ghosted AoS fields, or with inertia the 6-value k records of the inner points
+        const size_t stage_elems = kp.inertia ? std::max(3 * NG, 6 * N) : 3 * NG;
+        if ((rc = alloc((void**)&stage_buf, stage_elems * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&eps, (size_t)(nx + ny + nz) * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&eps_col, (size_t)2 * nz * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&st, sizeof(DevState)))) return rc;

@@ -45,10 +45,19 @@ def stage_by_stage(p, ref):
     assert relerr(inner(g.x(5)), inner(r.get()["xb"])) < tol, "x_6"
     if p.inertia:
         assert relerr(g.u(6), r.u(new=True)) < tol, "u_new"
-        assert relerr(g.u(5), r.u()) < tol, "u_6"
+        # u_6 = u_0 + sum_m (b[6][m] - b[5][m]) k_u,m cancels back to u_0 (here 0)
+        # up to rounding: compared on the scale of the step's velocities
+        un = np.abs(r.u(new=True)).max()
+        assert np.abs(g.u(5).astype(np.float64) - r.u()).max() <= tol * un, "u_6"
     g.control()
     s = g.state()
-    assert abs(s["maxDelta"] - md) <= max(tol * 100 * md, 1e-300)
+    if p.inertia and p.precision == 32:
+        # from rest k_x = dt u is O(dt^2): the FP32 error norm |x_new - x*| of
+        # the first step is rounding of x (~1e-15 near x = 0) and differs
+        # between builds; only its size against maxError decides the step
+        assert max(s["maxDelta"], md) < 1e-3 * p.maxError
+    else:
+        assert abs(s["maxDelta"] - md) <= max(tol * 100 * md, 1e-300)
     g.close()
     r.close()
 

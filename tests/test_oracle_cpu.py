@@ -154,6 +154,19 @@ def test_oracle_matches_reference_kernels(name):
     if p.inertia:
         assert relerr(o.u(), z["u1"]) < tol_stage
     o.close()
+    if p.inertia and p.precision == 32:
+        # From rest the position increments k_x = dt u are O(dt^2), so in FP32
+        # |x_new - x*| (formed in float, errMode 0) is rounding of x for the
+        # first steps (multiples of ulp(4) = 4.8e-7, or ~1e-15 near x = 0): the
+        # error norm, and the dt sequence it drives, are rounding noise that
+        # differs between any two builds.  This case pins the stage arithmetic
+        # (k_0, x_1, u_1 above) and the step's fields below, not the run.
+        o = Oracle(p, B0, xb)
+        o.step()
+        assert relerr(inner(o.xnew()), z["xnew1"]) < tol_stage
+        assert relerr(o.u(new=True), z["unew1"]) < tol_stage
+        o.close()
+        return
     o = Oracle(p, B0, xb)
     o.step()
     s = o.scalars()
