@@ -131,7 +131,8 @@ struct Impl : ImplBase {
     cudaGraphExec_t gexec = nullptr;
     // TMA-fed stage kernel: tensor maps of X[0], X[1], XS[0], XS[1]
     bool use_tma = true;
-    CUtensorMap tmaps[10];
+    CUtensorMap tmaps[10];      // single-case kernel (tile height stage_tma_ty<T>(pressure))
+    CUtensorMap tmaps_b[10];    // batched kernel (tile height STAGE_BATCH_TY)
     dim3 grid2;
     int TZ2 = 32;
     size_t NG = 0, N = 0, NP = 0;
@@ -307,22 +308,32 @@ struct Impl : ImplBase {
     }
 
     // Tensor maps over the padded positions viewed as (px, py, pz, component),
-    // box 36 x 12 x 1 x 3 = one position plane of a 32 x 8 tile with its
-    // 2-point halo.  Box x starts are tile starts (multiples of 32 elements),
-    // so every copy starts on a 16-byte boundary.
+    // box 36 x (ty + 4) x 1 x 3 = one position plane of a 32 x ty tile with its
+    // 2-point halo, and over the k arrays, box 32 x ty x 1 x 3: one set for the
+    // single-case tile height, one for the batched one.  Box x starts are tile
+    // starts (multiples of 32 elements), so every copy starts on a 16-byte
+    // boundary.
     int init_tma(int nsm) {
         CUDA_TRY(gmk::prepare_stage_tma<T>());
+        int rc = encode_maps(tmaps, gmk::stage_tma_ty<T>(gp.pressure));
+        if (!rc) rc = encode_maps(tmaps_b, gmk::STAGE_BATCH_TY);
+        if (rc) return rc;
+        choose_tz2(nsm);
+        return GM_OK;
+    }
+
+    int encode_maps(CUtensorMap* maps, int ty) {
         auto enc = tensor_map_encoder();
         if (!enc) return gm::fail(GM_ECUDA, "cuTensorMapEncodeTiled is unavailable");
         const cuuint64_t es = sizeof(T);
         cuuint64_t dims[4] = {(cuuint64_t)kp.px, (cuuint64_t)kp.py, (cuuint64_t)kp.pz, 3};
         cuuint64_t strides[3] = {(cuuint64_t)kp.px * es, (cuuint64_t)kp.px * kp.py * es, (cuuint64_t)kp.cs * es};
-        cuuint32_t box[4] = {gmk::TX + 4, gmk::STAGE_TMA_TY + 4, 1, 3};
+        cuuint32_t box[4] = {gmk::TX + 4, (cuuint32_t)ty + 4, 1, 3};
         cuuint32_t estr[4] = {1, 1, 1, 1};
         const CUtensorMapDataType dtype = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
         T* bufs[5] = {X[0], X[1], XS[0], XS[1], B0s};
         for (int q = 0; q < 5; q++) {
-            CUresult r = enc(&tmaps[q], dtype, 4, (void*)bufs[q], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CUresult r = enc(&maps[q], dtype, 4, (void*)bufs[q], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             if (r != CUDA_SUCCESS) return gm::fail(GM_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
@@ -331,16 +342,22 @@ struct Impl : ImplBase {
         // (rows start on 16-byte boundaries: kpx is a multiple of 8)
         cuuint64_t kdims[4] = {(cuuint64_t)kp.nx, (cuuint64_t)kp.ny, (cuuint64_t)kp.nz, 3};
         cuuint64_t kstrides[3] = {(cuuint64_t)kp.kpx * es, (cuuint64_t)kp.kpx * kp.ny * es, (cuuint64_t)kp.kcs * es};
-        cuuint32_t kbox[4] = {gmk::TX, gmk::STAGE_TMA_TY, 1, 3};
+        cuuint32_t kbox[4] = {gmk::TX, (cuuint32_t)ty, 1, 3};
         for (int m = 0; m < 5; m++) {
-            CUresult r = enc(&tmaps[5 + m], dtype, 4, (void*)K[m], kdims, kstrides, kbox, estr,
+            CUresult r = enc(&maps[5 + m], dtype, 4, (void*)K[m], kdims, kstrides, kbox, estr,
                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                              CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             if (r != CUDA_SUCCESS) return gm::fail(GM_ECUDA, "cuTensorMapEncodeTiled (k) failed: " + std::to_string((int)r));
         }
-        // z chunking as for k_stage, with the tile height fixed at 8
+        return GM_OK;
+    }
+
+    // z chunking of the single-case TMA kernel: minimise the iterations of the
+    // busiest SM, ceil(tiles / SMs) x (TZ + 2) (the kernel is issue-bound, so
+    // an SM's time follows the work of all the tiles it runs)
+    void choose_tz2(int nsm) {
         const int nx = kp.nx, ny = kp.ny, nz = kp.nz;
-        const int ty = gmk::STAGE_TMA_TY;
+        const int ty = gmk::stage_tma_ty<T>(gp.pressure);
         const long long ncol = (long long)((nx + gmk::TX - 1) / gmk::TX) * ((ny + ty - 1) / ty);
         double best = 1e300;
         for (int nzc = 1; nzc <= nz; nzc++) {
@@ -353,7 +370,6 @@ struct Impl : ImplBase {
         }
         grid2 = dim3((unsigned)((nx + gmk::TX - 1) / gmk::TX), (unsigned)((ny + ty - 1) / ty),
                      (unsigned)((nz + TZ2 - 1) / TZ2));
-        return GM_OK;
     }
 
     StageArgs<T> args(int n) {
@@ -772,7 +788,7 @@ struct Batch : BatchBase {
             cs.emplace_back(new Impl<T>());
             if ((rc = cs.back()->init(&p))) return rc;
             cs.back()->stream = stream;
-            memcpy(h[c].tm, cs.back()->tmaps, sizeof h[c].tm);
+            memcpy(h[c].tm, cs.back()->tmaps_b, sizeof h[c].tm);
             h[c].a = cs.back()->args(0);
             h[c].a.TZ = TZB;
             order.emplace_back(-(long long)p.nx * p.ny * p.nz, c);
@@ -782,7 +798,7 @@ struct Batch : BatchBase {
         std::vector<int4> work;
         for (auto& o : order) {
             const gm_params& p = ps[o.second];
-            const int nbx = (p.nx + gmk::TX - 1) / gmk::TX, nby = (p.ny + gmk::STAGE_TMA_TY - 1) / gmk::STAGE_TMA_TY;
+            const int nbx = (p.nx + gmk::TX - 1) / gmk::TX, nby = (p.ny + gmk::STAGE_BATCH_TY - 1) / gmk::STAGE_BATCH_TY;
             const int nbz = (p.nz + TZB - 1) / TZB;
             for (int bz = 0; bz < nbz; bz++)
                 for (int by = 0; by < nby; by++)

@@ -177,7 +177,23 @@ template <typename T>
 int stage_tma_occupancy(int pressure);
 template <typename T>
 cudaError_t launch_stage_tma(const StageArgsTMA<T>& A, int pressure, dim3 grid, cudaStream_t s);
-constexpr int STAGE_TMA_TY = 8;
+// Row groups of the single-case FP32 pressure stage kernel's tile (32 x 8
+// STAGE_ROWS columns) and the tile heights of the single-case and batched
+// launches.
+#ifndef GM_STAGE_ROWS
+#define GM_STAGE_ROWS 2
+#endif
+constexpr int STAGE_ROWS = GM_STAGE_ROWS;
+constexpr int STAGE_BATCH_TY = 8;
+// Two row groups pay where a point has much work (the pressure gradient:
+// 30.6 against 28.9 G cell-RK-stages/s on 256x256x512); without it the third
+// CTA per SM that one row group allows is worth more (36.3 against 34.7 G on
+// the 128x128x256 braid).  FP64 keeps one: two would not fit two CTAs'
+// shared memory per SM.
+template <typename T, bool PRESS>
+constexpr int stage_rows() { return (sizeof(T) == 4 && PRESS) ? STAGE_ROWS : 1; }
+template <typename T>
+inline int stage_tma_ty(int pressure) { return 8 * (pressure ? stage_rows<T, true>() : stage_rows<T, false>()); }
 // Batched stage launch: `work` holds (case, bx, by, bz) items over the
 // device array `cases`; `counter` is this stage's work counter (zero on
 // entry).  `nblocks` CTAs, persistent.

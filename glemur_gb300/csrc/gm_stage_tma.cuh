@@ -21,22 +21,30 @@
 
 namespace gmk {
 
-constexpr int TY2 = 8;                   // tile rows (= warps per CTA)
-constexpr int HX2 = TX + 4, HY2 = TY2 + 4;
-constexpr int BX2 = TX + 2, BY2 = TY2 + 2;
+constexpr int TY2 = 8;                   // warps per CTA (one tile row each, per row group)
+constexpr int HX2 = TX + 4;              // position-plane row: the tile + 2-point halo
+constexpr int BX2 = TX + 2;              // B-plane row: the tile + face halo
 // resident CTAs per SM the stage kernel is compiled for (register budget)
 #ifndef GM_STAGE_MINB
 #define GM_STAGE_MINB 3
 #endif
-constexpr int PLANE_C = HY2 * HX2;       // elements of one component of a position plane
-constexpr int PLANE_X = 3 * PLANE_C;
 constexpr unsigned kWaitLimit = 1u << 22;
+
+// Tile of R row groups: 32 x 8R columns, each thread owning the points of
+// rows ty, ty + 8, ..., ty + 8 (R - 1) of its column.
+template <int R>
+struct TileShape {
+    static constexpr int TYR = TY2 * R;                  // tile rows
+    static constexpr int HYR = TYR + 4, BYR = TYR + 2;   // position / B plane rows
+    static constexpr int PLANE_C = HYR * HX2;            // elements of one component of a position plane
+    static constexpr int PLANE_X = 3 * PLANE_C;
+};
 
 // Stride of a position-plane slot in elements: the plane rounded up so every
 // slot (a TMA destination) starts on a 128-byte boundary.
-template <typename T>
+template <typename T, int R>
 constexpr int slot_elems() {
-    return (int)(((PLANE_X * sizeof(T) + 127) / 128) * 128 / sizeof(T));
+    return (int)(((TileShape<R>::PLANE_X * sizeof(T) + 127) / 128) * 128 / sizeof(T));
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -113,15 +121,16 @@ __device__ __forceinline__ T det_cols(const T A[3][3]) {
 // s = (4 dy dz B0x, 4 dx dz B0y, 4 dx dy B0z): since jac = [a/2dx, b/2dy,
 // c/2dz], this is jac.B0 / det(jac) of B_JacB0 (rungeKutta.cu:79-99) with
 // the constant factors folded.  x and s come from shared-memory planes at the
-// same offset o.  Returns the columns a, b, c in Am[l][0..2] and
-// 1/det(a, b, c) in *rdet (Delta = 1 / (8 dx dy dz rdet)).
-template <typename T>
+// same offset o; PC is the component stride of a plane.  Returns the columns
+// a, b, c in Am[l][0..2] and 1/det(a, b, c) in *rdet (Delta = 1 / (8 dx dy dz
+// rdet)).
+template <typename T, int PC>
 __device__ __forceinline__ void b_point(const T* __restrict__ xm, const T* __restrict__ x0, const T* __restrict__ xp,
                                         int o, const T* __restrict__ b0s, T Bv[3], T Am[3][3], T* rdet) {
-    const T s0 = b0s[o], s1 = b0s[o + PLANE_C], s2 = b0s[o + 2 * PLANE_C];
+    const T s0 = b0s[o], s1 = b0s[o + PC], s2 = b0s[o + 2 * PC];
 #pragma unroll
     for (int l = 0; l < 3; l++) {
-        const int q = o + l * PLANE_C;
+        const int q = o + l * PC;
         Am[l][0] = x0[q + 1] - x0[q - 1];
         Am[l][1] = x0[q + HX2] - x0[q - HX2];
         Am[l][2] = xp[q] - xm[q];
@@ -156,22 +165,23 @@ __device__ __forceinline__ void ld_b(const double* d, double v[3]) {
 //   XR position-plane slots (the tile + 2-point halo, three components),
 //   2 slots of B0s planes (same box),
 //   2 slots of k-planes (the n arrays k_0..k_{n-1} over the tile; 1 slot in
-//   the last stage with pressure, so that three CTAs fit on an SM),
+//   the late stages, so that the CTAs per SM the kernel is built for fit),
 //   2 B planes (float4 per point: B and a pad),
 //   XR + 4 mbarriers, warp maxima, the abort flag and the work-item slot.
 // Every slot is a multiple of 128 bytes, the alignment TMA destinations need.
-template <typename T, bool PRESS, int NS>
+template <typename T, bool PRESS, int NS, int R>
 struct StageSmem {
     static constexpr int XR = PRESS ? 5 : 4;                      // position ring (one plane of prefetch)
-    static constexpr int SLOT = slot_elems<T>();
+    static constexpr int SLOT = slot_elems<T, R>();
     static constexpr int NK = NS;                                 // k arrays read by stage NS
-    static constexpr int KBOX = 3 * TY2 * TX;                     // elements of one k-array plane
+    static constexpr int KBOX = 3 * TileShape<R>::TYR * TX;       // elements of one k-array plane
     static constexpr int KSLOT = NK * KBOX;
     // k-plane slots: two (the next plane streams in while this one is read),
-    // one in the last stage with pressure (its plane is loaded during the B
-    // phase of the same iteration, behind a second barrier)
-    static constexpr int KS = (PRESS && NS == 5) ? 1 : 2;
-    static constexpr int PLANE_B = 4 * BY2 * BX2;
+    // or one where two would not leave room for the CTAs per SM the kernel is
+    // built for (its plane is then loaded during the B phase of the same
+    // iteration, behind a second barrier)
+    static constexpr int KS = R == 1 ? ((PRESS && NS == 5) ? 1 : 2) : ((NS >= 4 || (PRESS && NS >= 3)) ? 1 : 2);
+    static constexpr int PLANE_B = 4 * TileShape<R>::BYR * BX2;
     static constexpr size_t OFF_B0 = sizeof(T) * (size_t)XR * SLOT;
     static constexpr size_t OFF_K = OFF_B0 + sizeof(T) * 2 * (size_t)SLOT;
     static constexpr size_t OFF_B = OFF_K + sizeof(T) * KS * (size_t)KSLOT;
@@ -197,10 +207,11 @@ struct StageCtl {
 // Kind of a B-region point, fixed for the whole z march of a thread.
 enum { BK_SKIP = 0, BK_INNER = 1, BK_FACE_X = 2, BK_FACE_Y = 3 };
 
-// One RK stage over the 32 x 8 x TZ block (bx, by, bz) of one case.
+// One RK stage over the 32 x 8R x TZ block (bx, by, bz) of one case.
 // Iteration kk of the z march computes B on plane kb = kk - 1 (the tile and
 // its face halo) and then J, k_n and the stage position on plane kc = kk - 2.
-// Each thread keeps its own column's B at kc - 1, kc, kc + 1 and the
+// Each thread keeps, for each of its R points of the plane, B at kc - 1, kc,
+// kc + 1 and the
 // diagonals a, b, c and 1/det of plane kc in registers, so J needs only the
 // four in-plane neighbours' B from shared memory, written in the previous
 // iteration.  Operands arrive by TMA one iteration ahead: position plane
@@ -212,14 +223,16 @@ enum { BK_SKIP = 0, BK_INNER = 1, BK_FACE_X = 2, BK_FACE_Y = 3 };
 // over to the next tile.  Returns false
 // after a bounded wait ran out or an alignment check failed (the status word
 // says which).
-template <typename T, bool PRESS, int NS>
+template <typename T, bool PRESS, int NS, int R>
 __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int by, int bz, unsigned char* base) {
-    using L = StageSmem<T, PRESS, NS>;
+    using L = StageSmem<T, PRESS, NS, R>;
+    using S = TileShape<R>;
     constexpr bool LAST = NS == 5;
     constexpr int n = NS;
     constexpr int XR = L::XR;
     constexpr int SLOT = L::SLOT;
     constexpr int PLANE_B = L::PLANE_B;
+    constexpr int TYR = S::TYR, BYR = S::BYR, PC = S::PLANE_C;
 
     const StageArgs<T>& a = A.a;
     const KP<T>& p = a.p;
@@ -228,7 +241,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
 
     T* xs = reinterpret_cast<T*>(base);                                   // XR position slots
     T* b0r = reinterpret_cast<T*>(base + L::OFF_B0);                       // 2 B0s slots
-    T* kr = reinterpret_cast<T*>(base + L::OFF_K);                         // 2 k slots
+    T* kr = reinterpret_cast<T*>(base + L::OFF_K);                         // k slots
     T* bs = reinterpret_cast<T*>(base + L::OFF_B);                         // 2 B planes
     uint64_t* bars = reinterpret_cast<uint64_t*>(base + L::OFF_BAR);       // x | B0s | k
     T* s_wmax = reinterpret_cast<T*>(base + L::OFF_WMAX);
@@ -238,7 +251,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     // the producer (copy issue and waits) is lane 0 of the last warp, which
     // computes no face-halo B points
     const bool producer = tid == (TY2 - 1) * TX;
-    const int i0 = bx * TX, j0 = by * TY2, k0 = bz * a.TZ;
+    const int i0 = bx * TX, j0 = by * TYR, k0 = bz * a.TZ;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const int kend = min(k0 + a.TZ, nz);
     const int cur = st->cur;
@@ -250,7 +263,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     const int cs = (int)p.cs;
     const int pxy = p.px * p.py;
     const bool zPeri = p.zPeri != 0;
-    constexpr uint32_t kPlaneBytes = PLANE_X * sizeof(T);
+    constexpr uint32_t kPlaneBytes = S::PLANE_X * sizeof(T);
     constexpr uint32_t kKBytes = (uint32_t)(L::KSLOT * sizeof(T));
 
     // self-check of the alignment TMA needs: destination slots on 128 bytes,
@@ -263,31 +276,43 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     }
 
     // ---- per-thread descriptors, fixed for the whole z march ----------------
-    // B-phase point 1: the thread's own tile point
-    const int ic = i0 + tx, jc = j0 + ty;
-    const bool own = ic < nx && jc < ny;
-    const int ox1 = (ty + 2) * HX2 + (tx + 2);           // in a position / B0s plane
-    const int ob1 = 4 * ((ty + 1) * BX2 + (tx + 1));     // in a B plane
-    const int tyx = ty * TX + tx;                        // in a k plane
-    // in a partial tile the ghost column i = nx or row j = ny is a tile point
-    int kind1 = BK_SKIP;
-    const bool xo1 = ic >= nx, yo1 = jc >= ny;
-    if (ic <= nx && jc <= ny && !(xo1 && yo1)) {
-        if (xo1 && !p.xPeri) kind1 = BK_FACE_X;
-        else if (yo1 && !p.yPeri) kind1 = BK_FACE_Y;
-        else kind1 = BK_INNER;
+    // the thread's own points: column i0 + tx, rows ty + 8 r (r < R)
+    const int ic = i0 + tx;
+    int jc[R], ox1[R], ob1[R], tyx[R], kind1[R], gxy1[R], lin0[R];
+    bool own[R], img_xy[R];
+    T exy[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int tyr = ty + TY2 * r;
+        jc[r] = j0 + tyr;
+        own[r] = ic < nx && jc[r] < ny;
+        ox1[r] = (tyr + 2) * HX2 + (tx + 2);           // in a position / B0s plane
+        ob1[r] = 4 * ((tyr + 1) * BX2 + (tx + 1));     // in a B plane
+        tyx[r] = tyr * TX + tx;                        // in a k plane
+        // in a partial tile the ghost column i = nx or row j = ny is a tile point
+        kind1[r] = BK_SKIP;
+        const bool xo1 = ic >= nx, yo1 = jc[r] >= ny;
+        if (ic <= nx && jc[r] <= ny && !(xo1 && yo1)) {
+            if (xo1 && !p.xPeri) kind1[r] = BK_FACE_X;
+            else if (yo1 && !p.yPeri) kind1[r] = BK_FACE_Y;
+            else kind1[r] = BK_INNER;
+        }
+        exy[r] = own[r] ? p.ex[ic] * p.ey[jc[r]] : (T)0;
+        gxy1[r] = (ic + 2) + p.px * (jc[r] + 2);      // padded offset without the plane term
+        lin0[r] = ic + p.kpx * jc[r];                 // k_m index of the own column
+        img_xy[r] = (p.xPeri && (ic < 2 || ic >= nx - 2)) || (p.yPeri && (jc[r] < 2 || jc[r] >= ny - 2));
     }
-    // B-phase point 2: one of the 80 face-halo points (warps 0-2)
+    // one face-halo point for warps 0-2: the rows above and below the tile
+    // (warps 0 and 1) and its left and right columns (warp 2, 2 TYR <= 32 points)
     int jj2 = 0, ii2 = 0, kind2 = BK_SKIP;
     if (ty == 0) { jj2 = 0; ii2 = tx + 1; }
-    else if (ty == 1) { jj2 = BY2 - 1; ii2 = tx + 1; }
-    else if (ty == 2 && tx < 2 * TY2) { jj2 = (tx % TY2) + 1; ii2 = tx < TY2 ? 0 : BX2 - 1; }
+    else if (ty == 1) { jj2 = BYR - 1; ii2 = tx + 1; }
+    else if (ty == 2 && tx < 2 * TYR) { jj2 = (tx % TYR) + 1; ii2 = tx < TYR ? 0 : BX2 - 1; }
     else ii2 = -1;
     const int i2 = i0 - 1 + ii2, j2 = j0 - 1 + jj2;
-    bool xo2 = false, yo2 = false;
     if (ii2 >= 0 && i2 <= nx && j2 <= ny) {
-        xo2 = (i2 < 0 || i2 >= nx);
-        yo2 = (j2 < 0 || j2 >= ny);
+        const bool xo2 = (i2 < 0 || i2 >= nx);
+        const bool yo2 = (j2 < 0 || j2 >= ny);
         if (xo2 && yo2) kind2 = BK_SKIP;
         else if (xo2 && !p.xPeri) kind2 = BK_FACE_X;
         else if (yo2 && !p.yPeri) kind2 = BK_FACE_Y;
@@ -295,12 +320,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     }
     const int ox2 = (jj2 + 1) * HX2 + (ii2 + 1);
     const int ob2 = 4 * (jj2 * BX2 + ii2);
-    // output point
-    const T exy = own ? p.ex[ic] * p.ey[jc] : (T)0;
-    const int gxy1 = (ic + 2) + p.px * (jc + 2);         // padded offset without the plane term
-    const int lin0 = ic + p.kpx * jc;                    // k_m index of the own column
     const int kplane = p.kpx * ny;
-    const bool img_xy = (p.xPeri && (ic < 2 || ic >= nx - 2)) || (p.yPeri && (jc < 2 || jc >= ny - 2));
     const T* __restrict__ ezp = p.ez;
 
     auto xslot = [&](int plane) { return (plane + 20) % XR; };
@@ -335,7 +355,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     auto face_b = [&](int face, int i, int j, int kb, T Bv[3]) {
         Tile<T, 4, XR, 20> tl;
         tl.xs = xs;
-        tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = HY2;
+        tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = S::HYR;
         tl.slot = SLOT;
         T D;
         b_face<T>(p, tl, a.B0, face, i, j, kb, Bv, &D);
@@ -356,10 +376,18 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
 
     T dmax = 0;
     bool bad = false;
-    // own column: B at kc-1, kc, kc+1 and a, b, c, 1/det at kc
-    T Bm[3] = {0, 0, 0}, Bz[3] = {0, 0, 0}, Bp[3] = {0, 0, 0};
-    T Ac[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Rc = 0;
-    T An[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Rn = 0;
+    // own columns: B at kc-1, kc, kc+1 and a, b, c, 1/det at kc
+    T Bm[R][3], Bz[R][3], Bp[R][3], Ac[R][3][3], An[R][3][3], Rc[R], Rn[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+#pragma unroll
+        for (int l = 0; l < 3; l++) {
+            Bm[r][l] = 0; Bz[r][l] = 0; Bp[r][l] = 0;
+            Ac[r][l][0] = 0; Ac[r][l][1] = 0; Ac[r][l][2] = 0;
+            An[r][l][0] = 0; An[r][l][1] = 0; An[r][l][2] = 0;
+        }
+        Rc[r] = 0; Rn[r] = 0;
+    }
 
     for (int kk = k0; kk <= kend + 1; kk++) {
         // (1) the producer waits for position plane kk, the B0s plane of
@@ -392,7 +420,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
         const int mx = (kk + 20) % XR;      // ring slot of position plane kk
         // (3) B on plane kb = kk - 1 into B plane kb & 1
         const int kb = kk - 1;
-        T Bv[3] = {0, 0, 0};
+        T Bv[R][3];
         {
             T* bdst = bs + (kb & 1) * PLANE_B;
             const T* xm = xring(mx, 2);
@@ -400,28 +428,34 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             const T* xq = xring(mx, 0);
             const T* s0 = b0r + (kb & 1) * SLOT;
             const bool zo = (kb < 0 || kb >= nz);
-            T Bh[3], Ah[3][3], Rh;
-            if (!zo) {
-                if (kind1 != BK_SKIP) {
-                    if (kind1 == BK_INNER) b_point<T>(xm, x0, xq, ox1, s0, Bv, An, &Rn);
-                    else face_b(kind1 == BK_FACE_X ? 0 : 1, ic, jc, kb, Bv);
-                    st_b(bdst + ob1, Bv);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                Bv[r][0] = 0; Bv[r][1] = 0; Bv[r][2] = 0;
+                if (!zo) {
+                    if (kind1[r] != BK_SKIP) {
+                        if (kind1[r] == BK_INNER) b_point<T, PC>(xm, x0, xq, ox1[r], s0, Bv[r], An[r], &Rn[r]);
+                        else face_b(kind1[r] == BK_FACE_X ? 0 : 1, ic, jc[r], kb, Bv[r]);
+                        st_b(bdst + ob1[r], Bv[r]);
+                    }
+                } else if (!zPeri) {
+                    // line-tied ghost plane: only the own columns are needed
+                    if (own[r]) face_b(2, ic, jc[r], kb, Bv[r]);
+                } else {
+                    // periodic image plane: only the own columns are needed
+                    if (own[r]) b_point<T, PC>(xm, x0, xq, ox1[r], s0, Bv[r], An[r], &Rn[r]);
                 }
-                if (kind2 != BK_SKIP) {
-                    if (kind2 == BK_INNER) b_point<T>(xm, x0, xq, ox2, s0, Bh, Ah, &Rh);
-                    else face_b(kind2 == BK_FACE_X ? 0 : 1, i2, j2, kb, Bh);
-                    st_b(bdst + ob2, Bh);
-                }
-            } else if (!zPeri) {
-                // line-tied ghost plane: only the own column is needed
-                if (own) face_b(2, ic, jc, kb, Bv);
-            } else {
-                // periodic image plane: only the own column is needed
-                if (own) b_point<T>(xm, x0, xq, ox1, s0, Bv, An, &Rn);
+            }
+            if (!zo && kind2 != BK_SKIP) {
+                T Bh[3], Ah[3][3], Rh;
+                if (kind2 == BK_INNER) b_point<T, PC>(xm, x0, xq, ox2, s0, Bh, Ah, &Rh);
+                else face_b(kind2 == BK_FACE_X ? 0 : 1, i2, j2, kb, Bh);
+                st_b(bdst + ob2, Bh);
             }
         }
 #pragma unroll
-        for (int l = 0; l < 3; l++) { Bm[l] = Bz[l]; Bz[l] = Bp[l]; Bp[l] = Bv[l]; }
+        for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int l = 0; l < 3; l++) { Bm[r][l] = Bz[r][l]; Bz[r][l] = Bp[r][l]; Bp[r][l] = Bv[r][l]; }
         // (4) J, k_n and the stage position on plane kc = kk - 2
         const int kc = kk - 2;
         if (KS == 1 && kc >= k0) {
@@ -438,141 +472,150 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
             __syncthreads();
             if (*s_abort) break;
         }
-        if (kc >= k0 && own) {
+        if (kc >= k0) {
             const T* bc = bs + (kc & 1) * PLANE_B;
-            // in-plane neighbours' B: -x, +x, -y, +y
-            T bxm[3], bxp[3], bym[3], byp[3];
-            ld_b(bc + ob1 - 4, bxm);
-            ld_b(bc + ob1 + 4, bxp);
-            ld_b(bc + ob1 - 4 * BX2, bym);
-            ld_b(bc + ob1 + 4 * BX2, byp);
-            // Stokes current (current.cu:290-406).  The circulation around a
-            // quadrilateral P1..P4, sum (B_a + B_b).(x_b - x_a) over its edges,
-            // regroups exactly into sum B_a.(x_{a+1} - x_{a-1}); for the quads
-            // through the face neighbours (-x,-y,+x,+y), (-y,-z,+y,+z) and
-            // (-z,-x,+z,+x) that is I0 = b.dxB - a.dyB, I1 = c.dyB - b.dzB and
-            // I2 = a.dzB - c.dxB with the diagonals a = x(+x) - x(-x), b, c and
-            // dxB = B(+x) - B(-x), ...  The quads' area vectors are
-            // (1/2) a x b, (1/2) b x c, (1/2) c x a (for a quadrilateral,
-            // (1/4) sum of consecutive edge cross products = (1/2) d1 x d2),
-            // and the matrix with those rows has the inverse
-            // 2 [a b c] P / det(a, b, c), so J = (a I1 + b I2 + c I0) / det.
-            T I0 = 0, I1 = 0, I2 = 0;
-#pragma unroll
-            for (int l = 0; l < 3; l++) {
-                const T dx = bxp[l] - bxm[l], dy = byp[l] - bym[l], dz = Bp[l] - Bm[l];
-                I0 += Ac[l][1] * dx - Ac[l][0] * dy;
-                I1 += Ac[l][2] * dy - Ac[l][1] * dz;
-                I2 += Ac[l][0] * dz - Ac[l][2] * dx;
-            }
-            T Jv[3];
-#pragma unroll
-            for (int l = 0; l < 3; l++) Jv[l] = (Ac[l][0] * I1 + Ac[l][1] * I2 + Ac[l][2] * I0) * Rc;
-            const int lin = lin0 + kplane * kc;
-            T kn[3];
-            cross3(Jv, Bz, kn);
-            const T f = dtT * (exy * __ldg(&ezp[kc]));
-#pragma unroll
-            for (int l = 0; l < 3; l++) kn[l] *= f;
             const T* x0 = xring(mx, 2);   // position plane kc
-            if (PRESS) {
-                Tile<T, 4, XR, 20> tl;
-                tl.xs = xs;
-                tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = HY2;
-                tl.slot = SLOT;
-                T gp[3];
-                const T D = rcp_stage(Rc) * p.inv8dxdydz;     // Delta = det(a, b, c) / (8 dx dy dz)
-                grad_p<T>(p, tl, ic, jc, kc, D, gp);
+            const T ezk = __ldg(&ezp[kc]);
+            const bool zimg = zPeri && (kc < 2 || kc >= nz - 2);
 #pragma unroll
-                for (int l = 0; l < 3; l++) kn[l] += -dtT * gp[l];
-            }
-            T xa[3];
-#pragma unroll
-            for (int l = 0; l < 3; l++) xa[l] = x0[ox1 + l * PLANE_C];
-            const bool images = img_xy || (zPeri && (kc < 2 || kc >= nz - 2));
-            const int g = gxy1 + pxy * (kc + 2);
-            const T* kp = kslot(kc) + tyx;    // k_m component l at kp[(3m + l) * TX * TY2]
-            if (!LAST) {
-                // x_{n+1} = x_n + sum_{m<=n} (b[n+1][m] - b[n][m]) k_m (rungeKutta.cu:216-227)
-#pragma unroll
-                for (int m = 0; m < n; m++) {
-                    const T w = p.db[n][m];
-#pragma unroll
-                    for (int l = 0; l < 3; l++) xa[l] += w * kp[(3 * m + l) * TX * TY2];
-                }
-                const T w = p.db[n][n];
-#pragma unroll
-                for (int l = 0; l < 3; l++) xa[l] += w * kn[l];
-                T* Kn = a.K[n];
-                Kn[lin] = kn[0];
-                Kn[KC + lin] = kn[1];
-                Kn[2 * KC + lin] = kn[2];
-                T* Xo = a.XS[n & 1];
-                if (images) {
-                    store_pos<T>(p, Xo, ic, jc, kc, xa);
-                } else {
-                    Xo[g] = xa[0];
-                    Xo[cs + g] = xa[1];
-                    Xo[2 * cs + g] = xa[2];
-                }
-            } else {
-                // stage 5: x_6, x_new, x* and the error norm (rungeKutta.cu:251-339)
-                T km[6][3];
-#pragma unroll
-                for (int m = 0; m < 5; m++)
-#pragma unroll
-                    for (int l = 0; l < 3; l++) km[m][l] = kp[(3 * m + l) * TX * TY2];
-#pragma unroll
-                for (int l = 0; l < 3; l++) km[5][l] = kn[l];
-#pragma unroll
-                for (int m = 0; m < 6; m++)
-#pragma unroll
-                    for (int l = 0; l < 3; l++) xa[l] += p.db[5][m] * km[m][l];
-                T xnew[3];
+            for (int r = 0; r < R; r++) {
+                if (!own[r]) continue;
+                // in-plane neighbours' B: -x, +x, -y, +y
+                T bxm[3], bxp[3], bym[3], byp[3];
+                ld_b(bc + ob1[r] - 4, bxm);
+                ld_b(bc + ob1[r] + 4, bxp);
+                ld_b(bc + ob1[r] - 4 * BX2, bym);
+                ld_b(bc + ob1[r] + 4 * BX2, byp);
+                // Stokes current (current.cu:290-406).  The circulation around a
+                // quadrilateral P1..P4, sum (B_a + B_b).(x_b - x_a) over its edges,
+                // regroups exactly into sum B_a.(x_{a+1} - x_{a-1}); for the quads
+                // through the face neighbours (-x,-y,+x,+y), (-y,-z,+y,+z) and
+                // (-z,-x,+z,+x) that is I0 = b.dxB - a.dyB, I1 = c.dyB - b.dzB and
+                // I2 = a.dzB - c.dxB with the diagonals a = x(+x) - x(-x), b, c and
+                // dxB = B(+x) - B(-x), ...  The quads' area vectors are
+                // (1/2) a x b, (1/2) b x c, (1/2) c x a (for a quadrilateral,
+                // (1/4) sum of consecutive edge cross products = (1/2) d1 x d2),
+                // and the matrix with those rows has the inverse
+                // 2 [a b c] P / det(a, b, c), so J = (a I1 + b I2 + c I0) / det.
+                T I0 = 0, I1 = 0, I2 = 0;
 #pragma unroll
                 for (int l = 0; l < 3; l++) {
-                    xnew[l] = xa[l];
-                    T xst = xa[l];
-                    T dl = 0;
-                    if (l < 2 || p.zUpdate) {
-                        if (p.errMode == 0) {
-#pragma unroll
-                            for (int m = 0; m < 6; m++) {
-                                xnew[l] += p.c[m] * km[m][l];
-                                xst += p.cst[m] * km[m][l];
-                            }
-                            dl = fabs(xnew[l] - xst);
-                        } else {
-                            // sum (c - c*) k: no cancellation against x
-                            T e = 0;
-#pragma unroll
-                            for (int m = 0; m < 6; m++) {
-                                xnew[l] += p.c[m] * km[m][l];
-                                e += p.cmcT[m] * km[m][l];
-                            }
-                            dl = fabs(e);
-                        }
-                    }
-                    if (dl > dmax) dmax = dl;     // NaN never wins (maths.cu:144-153)
-                    if (!isfinite(dl) || !isfinite(xnew[l])) bad = true;   // NaN/Inf anywhere in k_0..k_5
+                    const T dx = bxp[l] - bxm[l], dy = byp[l] - bym[l], dz = Bp[r][l] - Bm[r][l];
+                    I0 += Ac[r][l][1] * dx - Ac[r][l][0] * dy;
+                    I1 += Ac[r][l][2] * dy - Ac[r][l][1] * dz;
+                    I2 += Ac[r][l][0] * dz - Ac[r][l][2] * dx;
                 }
-                if (images) {
-                    store_pos<T>(p, a.X[cur], ic, jc, kc, xa);
-                    store_pos<T>(p, a.X[cur ^ 1], ic, jc, kc, xnew);
+                T Jv[3];
+#pragma unroll
+                for (int l = 0; l < 3; l++) Jv[l] = (Ac[r][l][0] * I1 + Ac[r][l][1] * I2 + Ac[r][l][2] * I0) * Rc[r];
+                const int lin = lin0[r] + kplane * kc;
+                T kn[3];
+                cross3(Jv, Bz[r], kn);
+                const T f = dtT * (exy[r] * ezk);
+#pragma unroll
+                for (int l = 0; l < 3; l++) kn[l] *= f;
+                if (PRESS) {
+                    Tile<T, 4, XR, 20> tl;
+                    tl.xs = xs;
+                    tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = S::HYR;
+                    tl.slot = SLOT;
+                    T gp[3];
+                    const T D = rcp_stage(Rc[r]) * p.inv8dxdydz;     // Delta = det(a, b, c) / (8 dx dy dz)
+                    grad_p<T>(p, tl, ic, jc[r], kc, D, gp);
+#pragma unroll
+                    for (int l = 0; l < 3; l++) kn[l] += -dtT * gp[l];
+                }
+                T xa[3];
+#pragma unroll
+                for (int l = 0; l < 3; l++) xa[l] = x0[ox1[r] + l * PC];
+                const bool images = img_xy[r] || zimg;
+                const int g = gxy1[r] + pxy * (kc + 2);
+                const T* kp = kslot(kc) + tyx[r];    // k_m component l at kp[(3m + l) * TX * TYR]
+                if (!LAST) {
+                    // x_{n+1} = x_n + sum_{m<=n} (b[n+1][m] - b[n][m]) k_m (rungeKutta.cu:216-227)
+#pragma unroll
+                    for (int m = 0; m < n; m++) {
+                        const T w = p.db[n][m];
+#pragma unroll
+                        for (int l = 0; l < 3; l++) xa[l] += w * kp[(3 * m + l) * TX * TYR];
+                    }
+                    const T w = p.db[n][n];
+#pragma unroll
+                    for (int l = 0; l < 3; l++) xa[l] += w * kn[l];
+                    T* Kn = a.K[n];
+                    Kn[lin] = kn[0];
+                    Kn[KC + lin] = kn[1];
+                    Kn[2 * KC + lin] = kn[2];
+                    T* Xo = a.XS[n & 1];
+                    if (images) {
+                        store_pos<T>(p, Xo, ic, jc[r], kc, xa);
+                    } else {
+                        Xo[g] = xa[0];
+                        Xo[cs + g] = xa[1];
+                        Xo[2 * cs + g] = xa[2];
+                    }
                 } else {
-                    T* X6 = a.X[cur];
-                    T* Xn = a.X[cur ^ 1];
-                    X6[g] = xa[0]; X6[cs + g] = xa[1]; X6[2 * cs + g] = xa[2];
-                    Xn[g] = xnew[0]; Xn[cs + g] = xnew[1]; Xn[2 * cs + g] = xnew[2];
+                    // stage 5: x_6, x_new, x* and the error norm (rungeKutta.cu:251-339)
+                    T km[6][3];
+#pragma unroll
+                    for (int m = 0; m < 5; m++)
+#pragma unroll
+                        for (int l = 0; l < 3; l++) km[m][l] = kp[(3 * m + l) * TX * TYR];
+#pragma unroll
+                    for (int l = 0; l < 3; l++) km[5][l] = kn[l];
+#pragma unroll
+                    for (int m = 0; m < 6; m++)
+#pragma unroll
+                        for (int l = 0; l < 3; l++) xa[l] += p.db[5][m] * km[m][l];
+                    T xnew[3];
+#pragma unroll
+                    for (int l = 0; l < 3; l++) {
+                        xnew[l] = xa[l];
+                        T xst = xa[l];
+                        T dl = 0;
+                        if (l < 2 || p.zUpdate) {
+                            if (p.errMode == 0) {
+#pragma unroll
+                                for (int m = 0; m < 6; m++) {
+                                    xnew[l] += p.c[m] * km[m][l];
+                                    xst += p.cst[m] * km[m][l];
+                                }
+                                dl = fabs(xnew[l] - xst);
+                            } else {
+                                // sum (c - c*) k: no cancellation against x
+                                T e = 0;
+#pragma unroll
+                                for (int m = 0; m < 6; m++) {
+                                    xnew[l] += p.c[m] * km[m][l];
+                                    e += p.cmcT[m] * km[m][l];
+                                }
+                                dl = fabs(e);
+                            }
+                        }
+                        if (dl > dmax) dmax = dl;     // NaN never wins (maths.cu:144-153)
+                        if (!isfinite(dl) || !isfinite(xnew[l])) bad = true;   // NaN/Inf anywhere in k_0..k_5
+                    }
+                    if (images) {
+                        store_pos<T>(p, a.X[cur], ic, jc[r], kc, xa);
+                        store_pos<T>(p, a.X[cur ^ 1], ic, jc[r], kc, xnew);
+                    } else {
+                        T* X6 = a.X[cur];
+                        T* Xn = a.X[cur ^ 1];
+                        X6[g] = xa[0]; X6[cs + g] = xa[1]; X6[2 * cs + g] = xa[2];
+                        Xn[g] = xnew[0]; Xn[cs + g] = xnew[1]; Xn[2 * cs + g] = xnew[2];
+                    }
                 }
             }
         }
         // the diagonals of plane kb become those of the next iteration's kc
 #pragma unroll
-        for (int l = 0; l < 3; l++) {
-            Ac[l][0] = An[l][0]; Ac[l][1] = An[l][1]; Ac[l][2] = An[l][2];
+        for (int r = 0; r < R; r++) {
+#pragma unroll
+            for (int l = 0; l < 3; l++) {
+                Ac[r][l][0] = An[r][l][0]; Ac[r][l][1] = An[r][l][1]; Ac[r][l][2] = An[r][l][2];
+            }
+            Rc[r] = Rn[r];
         }
-        Rc = Rn;
     }
     // drain copies still in flight (after an abort), bounded
     if (producer && *s_abort) {
@@ -597,9 +640,9 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
 
 // Shared-memory set-up common to the stage kernels: the 128-byte aligned
 // base, the mbarriers and the abort flag.
-template <typename T, bool PRESS, int NS>
+template <typename T, bool PRESS, int NS, int R>
 __device__ __forceinline__ unsigned char* stage_smem_setup(unsigned char* smraw) {
-    using L = StageSmem<T, PRESS, NS>;
+    using L = StageSmem<T, PRESS, NS, R>;
     unsigned char* base = smraw + ((128u - (smem_u32(smraw) & 127u)) & 127u);
     uint64_t* bars = reinterpret_cast<uint64_t*>(base + L::OFF_BAR);
     StageCtl* ctl = reinterpret_cast<StageCtl*>(base + L::OFF_CTL);
@@ -613,14 +656,17 @@ __device__ __forceinline__ unsigned char* stage_smem_setup(unsigned char* smraw)
     return base;
 }
 
-// One RK stage of one case: one CTA per 32 x 8 x TZ block.
+// One RK stage of one case: one CTA per 32 x 8R x TZ block, R =
+// stage_rows<T, PRESS>() (minimum CTAs per SM: 3 for one FP32 row group, 2 for
+// two, 2 in FP64).
 template <typename T, bool PRESS, int NS>
-__global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? GM_STAGE_MINB : 2)
+__global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? (stage_rows<T, PRESS>() == 1 ? GM_STAGE_MINB : 2) : 2)
     k_stage_tma(const __grid_constant__ StageArgsTMA<T> A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     if (A.a.st->done) return;
-    unsigned char* base = stage_smem_setup<T, PRESS, NS>(smraw);
-    stage_tile<T, PRESS, NS>(A, blockIdx.x, blockIdx.y, blockIdx.z, base);
+    constexpr int R = stage_rows<T, PRESS>();
+    unsigned char* base = stage_smem_setup<T, PRESS, NS, R>(smraw);
+    stage_tile<T, PRESS, NS, R>(A, blockIdx.x, blockIdx.y, blockIdx.z, base);
 }
 
 // One RK stage of many cases: a persistent launch whose CTAs take work items
@@ -630,9 +676,9 @@ template <typename T, bool PRESS, int NS>
 __global__ void __launch_bounds__(TX * TY2, 2)
     k_stage_tma_batch(const StageArgsTMA<T>* __restrict__ cases, const int4* __restrict__ work, int nwork,
                       int* __restrict__ counter) {
-    using L = StageSmem<T, PRESS, NS>;
+    using L = StageSmem<T, PRESS, NS, 1>;
     extern __shared__ __align__(128) unsigned char smraw[];
-    unsigned char* base = stage_smem_setup<T, PRESS, NS>(smraw);
+    unsigned char* base = stage_smem_setup<T, PRESS, NS, 1>(smraw);
     int* s_w = &reinterpret_cast<StageCtl*>(base + L::OFF_CTL)->work;
     for (;;) {
         if (threadIdx.x == 0 && threadIdx.y == 0) *s_w = atomicAdd(counter, 1);
@@ -641,21 +687,28 @@ __global__ void __launch_bounds__(TX * TY2, 2)
         __syncthreads();   // s_w is rewritten only after every thread has read it
         if (w >= nwork) break;
         const int4 it = work[w];
-        if (!stage_tile<T, PRESS, NS>(cases[it.x], it.y, it.z, it.w, base)) break;
+        if (!stage_tile<T, PRESS, NS, 1>(cases[it.x], it.y, it.z, it.w, base)) break;
         __syncthreads();   // the next tile's copies overwrite slots this one read
     }
 }
 
+template <typename T, int R>
+size_t stage_tma_smem_bytes_r(int pressure, int n) {
+    switch (n) {
+        case 0: return pressure ? StageSmem<T, true, 0, R>::BYTES : StageSmem<T, false, 0, R>::BYTES;
+        case 1: return pressure ? StageSmem<T, true, 1, R>::BYTES : StageSmem<T, false, 1, R>::BYTES;
+        case 2: return pressure ? StageSmem<T, true, 2, R>::BYTES : StageSmem<T, false, 2, R>::BYTES;
+        case 3: return pressure ? StageSmem<T, true, 3, R>::BYTES : StageSmem<T, false, 3, R>::BYTES;
+        case 4: return pressure ? StageSmem<T, true, 4, R>::BYTES : StageSmem<T, false, 4, R>::BYTES;
+        default: return pressure ? StageSmem<T, true, 5, R>::BYTES : StageSmem<T, false, 5, R>::BYTES;
+    }
+}
+
+// dynamic shared memory of the single-case stage kernel
 template <typename T>
 size_t stage_tma_smem_bytes(int pressure, int n) {
-    switch (n) {
-        case 0: return pressure ? StageSmem<T, true, 0>::BYTES : StageSmem<T, false, 0>::BYTES;
-        case 1: return pressure ? StageSmem<T, true, 1>::BYTES : StageSmem<T, false, 1>::BYTES;
-        case 2: return pressure ? StageSmem<T, true, 2>::BYTES : StageSmem<T, false, 2>::BYTES;
-        case 3: return pressure ? StageSmem<T, true, 3>::BYTES : StageSmem<T, false, 3>::BYTES;
-        case 4: return pressure ? StageSmem<T, true, 4>::BYTES : StageSmem<T, false, 4>::BYTES;
-        default: return pressure ? StageSmem<T, true, 5>::BYTES : StageSmem<T, false, 5>::BYTES;
-    }
+    return pressure ? stage_tma_smem_bytes_r<T, stage_rows<T, true>()>(1, n)
+                    : stage_tma_smem_bytes_r<T, stage_rows<T, false>()>(0, n);
 }
 
 template <typename T, bool PRESS, int NS>
@@ -688,7 +741,7 @@ cudaError_t prepare_stage_tma() {
 template <typename T>
 int stage_tma_batch_occupancy(int pressure) {
     int nb = 0;
-    const size_t sm = stage_tma_smem_bytes<T>(pressure, 5);
+    const size_t sm = stage_tma_smem_bytes_r<T, 1>(pressure, 5);
     cudaError_t e = pressure
         ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma_batch<T, true, 5>, TX * TY2, sm)
         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage_tma_batch<T, false, 5>, TX * TY2, sm);
@@ -699,7 +752,7 @@ template <typename T>
 cudaError_t launch_stage_tma_batch(const StageArgsTMA<T>* cases, const int4* work, int nwork, int* counter, int n,
                                    int pressure, int nblocks, cudaStream_t s) {
     const dim3 block(TX, TY2, 1);
-    const size_t sm = stage_tma_smem_bytes<T>(pressure, n);
+    const size_t sm = stage_tma_smem_bytes_r<T, 1>(pressure, n);
 #define GMK_LAUNCH_B(PR)                                                                                        \
     switch (n) {                                                                                                \
         case 0: k_stage_tma_batch<T, PR, 0><<<nblocks, block, sm, s>>>(cases, work, nwork, counter); break;      \
