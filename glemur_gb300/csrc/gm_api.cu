@@ -396,11 +396,12 @@ struct Impl : ImplBase {
     int upload(const void* xb, const void* b0, double t, double dt) override {
         if (!xb || !b0) return gm::fail(GM_EPARAM, "gm_upload: null array");
         const size_t bytes = 3 * NG * sizeof(T);
-        CUDA_TRY(cudaMemcpyAsync(stage_buf, b0, bytes, cudaMemcpyHostToDevice, stream));
+        // host or device arrays (unified addressing)
+        CUDA_TRY(cudaMemcpyAsync(stage_buf, b0, bytes, cudaMemcpyDefault, stream));
         CUDA_TRY(gmk::launch_unpack<T>(kp, stage_buf, B0, stream));
         CUDA_TRY(gmk::launch_scale_b0<T>(kp, B0, B0s, stream));
         CUDA_TRY(cudaMemcpyAsync(outB, stage_buf, bytes, cudaMemcpyDeviceToDevice, stream));   // main.cu:195
-        CUDA_TRY(cudaMemcpyAsync(stage_buf, xb, bytes, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(stage_buf, xb, bytes, cudaMemcpyDefault, stream));
         T* bufs[4] = {X[0], X[1], XS[0], XS[1]};
         for (T* b : bufs) {
             CUDA_TRY(gmk::launch_unpack<T>(kp, stage_buf, b, stream));

@@ -499,6 +499,82 @@ __global__ void k_input(const T* __restrict__ B0, int nx, int ny, int nz, __nv_b
     }
 }
 
+// ---- the warm-start grid: displacement -> smoothed -> positions ------------
+
+// Displacement channels 0..2 of the network output (BF16, [V][ld]) to float.
+__global__ void k_wg_load(const __nv_bfloat16* __restrict__ y, int ld, long long V, float* __restrict__ d) {
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int c = 0; c < 3; c++) d[3 * v + c] = __bfloat162float(y[v * ld + c]);
+}
+
+// One 3x3x3 box-filter pass, periodic in x / y as selected, zero beyond the
+// z range: out(i, j, k) = (1/27) sum of the 27 neighbours.
+__global__ void k_wg_box(const float* __restrict__ in, float* __restrict__ out, int nx, int ny, int nz, int xper,
+                         int yper) {
+    const long long V = (long long)nx * ny * nz;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long long)nx * ny));
+        float acc[3] = {0.f, 0.f, 0.f};
+        for (int dk = -1; dk <= 1; dk++) {
+            const int kk = k + dk;
+            if (kk < 0 || kk >= nz) continue;
+            for (int dj = -1; dj <= 1; dj++) {
+                int jj = j + dj;
+                if (jj < 0 || jj >= ny) {
+                    if (!yper) continue;
+                    jj = (jj + ny) % ny;
+                }
+                for (int di = -1; di <= 1; di++) {
+                    int ii = i + di;
+                    if (ii < 0 || ii >= nx) {
+                        if (!xper) continue;
+                        ii = (ii + nx) % nx;
+                    }
+                    const float* q = in + 3 * (ii + (long long)nx * (jj + (long long)ny * kk));
+                    acc[0] += q[0]; acc[1] += q[1]; acc[2] += q[2];
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) out[3 * v + c] = acc[c] * (1.f / 27.f);
+    }
+}
+
+// Positions of the warm grid in the reference layout (ghosted AoS): the
+// identity grid xid plus the displacement (in grid spacings) at the inner
+// points, the first and last inner z-planes held; periodic x / y ghosts are
+// the images of the opposite inner points shifted by -/+ (L + d) (x first,
+// then y, so corners carry both shifts); other ghosts keep xid.
+template <typename T>
+__global__ void k_wg_grid(const float* __restrict__ d, const T* __restrict__ xid, T* __restrict__ xb, int nx, int ny,
+                          int nz, int xper, int yper, double dx, double dy, double dz, double Lx, double Ly) {
+    const long long G = (long long)(nx + 2) * (ny + 2) * (nz + 2);
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < G; g += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(g % (nx + 2)), j = (int)((g / (nx + 2)) % (ny + 2));
+        const int k = (int)(g / ((long long)(nx + 2) * (ny + 2)));
+        int is = i, js = j;
+        double sx = 0, sy = 0;
+        if (xper && i == 0) { is = nx; sx = -(Lx + dx); }
+        if (xper && i == nx + 1) { is = 1; sx = Lx + dx; }
+        if (yper && j == 0) { js = ny; sy = -(Ly + dy); }
+        if (yper && j == ny + 1) { js = 1; sy = Ly + dy; }
+        const long long gs = is + (long long)(nx + 2) * (js + (long long)(ny + 2) * k);
+        double x[3] = {(double)xid[3 * gs], (double)xid[3 * gs + 1], (double)xid[3 * gs + 2]};
+        if (is >= 1 && is <= nx && js >= 1 && js <= ny && k >= 2 && k <= nz - 1) {
+            const float* q = d + 3 * ((is - 1) + (long long)nx * ((js - 1) + (long long)ny * (k - 1)));
+            x[0] += (double)q[0] * dx;
+            x[1] += (double)q[1] * dy;
+            x[2] += (double)q[2] * dz;
+        }
+        x[0] += sx;
+        x[1] += sy;
+        xb[3 * g] = (T)x[0];
+        xb[3 * g + 1] = (T)x[1];
+        xb[3 * g + 2] = (T)x[2];
+    }
+}
+
 static unsigned nb(long long n) {
     long long b = (n + 255) / 256;
     return (unsigned)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
@@ -617,6 +693,29 @@ int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, 
         gmnn::k_input<double><<<gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>((const double*)B0, nx, ny, nz,
                                                                                (__nv_bfloat16*)x, ld, sx, sy);
     return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_input");
+}
+
+int gm_nn_warm_grid(const void* y, int ldy, const gm_params* p, int passes, const void* xid, float* scratch,
+                    void* xb, void* stream) {
+    if (!y || !p || !xid || !scratch || !xb || passes < 0 || ldy < 3)
+        return gm::fail(GM_EPARAM, "gm_nn_warm_grid: bad argument");
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    const long long V = (long long)nx * ny * nz, G = (long long)(nx + 2) * (ny + 2) * (nz + 2);
+    cudaStream_t s = (cudaStream_t)stream;
+    float* a = scratch;
+    float* b = scratch + 3 * V;
+    gmnn::k_wg_load<<<gmnn::nb(V), 256, 0, s>>>((const __nv_bfloat16*)y, ldy, V, a);
+    for (int q = 0; q < passes; q++) {
+        gmnn::k_wg_box<<<gmnn::nb(V), 256, 0, s>>>(a, b, nx, ny, nz, p->xPeri, p->yPeri);
+        float* t = a; a = b; b = t;
+    }
+    if (p->precision == 32)
+        gmnn::k_wg_grid<float><<<gmnn::nb(G), 256, 0, s>>>(a, (const float*)xid, (float*)xb, nx, ny, nz, p->xPeri,
+                                                            p->yPeri, p->dx, p->dy, p->dz, p->Lx, p->Ly);
+    else
+        gmnn::k_wg_grid<double><<<gmnn::nb(G), 256, 0, s>>>(a, (const double*)xid, (double*)xb, nx, ny, nz, p->xPeri,
+                                                             p->yPeri, p->dx, p->dy, p->dz, p->Lx, p->Ly);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "gm_nn_warm_grid");
 }
 
 int gm_nn_zero(void* p, size_t bytes, void* stream) {

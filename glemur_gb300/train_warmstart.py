@@ -159,6 +159,33 @@ def warm_grid(net, p, B0, smooth=2):
     return xb.astype(np.float32)
 
 
+class DeviceWarmGrid:
+    """The warm grid built on the device (gm_nn_warm_grid): the network's
+    displacement smoothed and added to the identity grid, periodic ghosts
+    set, without a host round trip; the same grid as warm_grid up to the
+    float rounding of the smoothing."""
+
+    def __init__(self, p, xid):
+        import torch
+        from . import _abi
+        self.p = p
+        self.lib = _abi.load()
+        self.xid = torch.from_numpy(np.ascontiguousarray(xid)).cuda()
+        self.xb = torch.empty_like(self.xid)
+        self.scratch = torch.empty(6 * p.nx * p.ny * p.nz, dtype=torch.float32, device="cuda")
+
+    def build(self, net, B0_dev, smooth=2):
+        import torch
+        from . import _abi
+        net.set_input_b0(B0_dev, self.p.precision)
+        y = net.forward()
+        stream = torch.cuda.current_stream().cuda_stream
+        _abi.check(self.lib.gm_nn_warm_grid(_abi.VP(y.data_ptr()), y.stride(0), self.p, smooth,
+                                            _abi.VP(self.xid.data_ptr()), _abi.VP(self.scratch.data_ptr()),
+                                            _abi.VP(self.xb.data_ptr()), _abi.VP(stream)), "gm_nn_warm_grid")
+        return self.xb
+
+
 def time_to_residual(g, p, xb, B0, residual, max_attempts, check_every=50):
     """Upload, then relax until the weighted residual is at most `residual`.
     Returns (seconds, attempts, residual at start, min Delta seen, reached)."""
@@ -195,15 +222,18 @@ def evaluate(net, seeds, residual, max_attempts, log=print, smooth=2):
         g.state()
         tp, ap, rp0, mdp, okp = time_to_residual(g, p, xb0, B0, residual, max_attempts)
         d_true = displacement(p, g.download()["xb"], xb0)
-        # the warm start's own cost: inference, grid build, validity check
+        # the warm start's own cost: B0 to the device, inference, grid build
+        # (on the device), upload, validity check
+        wg = DeviceWarmGrid(p, xb0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        xw = warm_grid(net, p, B0, smooth)
-        g.upload(xw, B0)
+        B0_dev = torch.from_numpy(B0).cuda()
+        xw_dev = wg.build(net, B0_dev, smooth)
+        torch.cuda.synchronize()
+        g.upload_ptr(xw_dev.data_ptr(), B0_dev.data_ptr())
         accepted = g.refresh()["minDetJac"] > 0
-        if not accepted:
-            xw = xb0
         t_net = time.perf_counter() - t0
+        xw = xw_dev.cpu().numpy() if accepted else xb0
         d_pred = displacement(p, xw, xb0)
         rms_true = float(np.sqrt((d_true.astype(np.float64) ** 2).mean()))
         rms_err = float(np.sqrt(((d_pred.astype(np.float64) - d_true) ** 2).mean()))

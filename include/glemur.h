@@ -210,7 +210,8 @@ int gm_destroy(gm_handle* h);
  * own non-blocking stream. */
 int gm_set_stream(gm_handle* h, void* stream);
 
-/* Copy the initial state to the device (src/main.cu:181-232). */
+/* Copy the initial state to the device (src/main.cu:181-232).  xb and B0
+ * (reference layout) may be host or device arrays. */
 int gm_upload(gm_handle* h, const void* xb, const void* B0, double t, double dt);
 
 /* ---- the relaxation hot path -------------------------------------------- */
@@ -416,6 +417,16 @@ int gm_nn_adam(float* W, float* mW, float* vW, const float* gW, float* b, float*
  * 0 <= sy < ny): a whole-cell translation for data augmentation. */
 int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, int sx, int sy,
                 void* stream);
+/* Warm-start grid on the device: the displacement (channels 0..2 of the
+ * network output y, BF16 [V][ldy], in grid spacings) smoothed by `passes`
+ * 3x3x3 box filters (periodic x / y as p selects, zero beyond z), added to the
+ * identity grid xid (device, reference layout, REAL of p->precision) at the
+ * inner points except the first and last z-planes, with periodic x / y ghosts
+ * as images of the opposite inner points shifted by -/+ (L + d); written to
+ * xb (device, same layout).  scratch: device floats, 6 nx ny nz.  No
+ * counterpart in the reference (its runs start from the identity grid). */
+int gm_nn_warm_grid(const void* y, int ldy, const gm_params* p, int passes, const void* xid, float* scratch,
+                    void* xb, void* stream);
 /* Zero `bytes` bytes of device memory (cudaMemsetAsync). */
 int gm_nn_zero(void* p, size_t bytes, void* stream);
 

@@ -177,3 +177,28 @@ def test_gpu_input_and_loss_translation():
     e[0] = 0
     e[-1] = 0
     assert float(net.loss_acc.item()) == pytest.approx(float((e * e).sum()), rel=1e-3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("smooth", [0, 2])
+def test_gpu_warm_grid_matches_host_build(smooth):
+    """gm_nn_warm_grid (smoothing, displacement, periodic images on the
+    device) builds the grid the host path warm_grid builds, up to the float
+    rounding of the smoothing (the host smooths in double)."""
+    import torch
+    from glemur_gb300 import configs
+    from glemur_gb300.train_warmstart import DeviceWarmGrid, warm_grid
+    from glemur_gb300.warmstart import UNet, load_weights
+    p = configs.random_braid(900003, shape=(64, 64, 128), precision=32)
+    B0, xb0 = configs.init_state(p)
+    net = UNet((64, 64, 128), seed=0)
+    net.load_state_dict(load_weights())
+    host = warm_grid(net, p, B0, smooth)
+    dev = DeviceWarmGrid(p, xb0).build(net, torch.from_numpy(B0).cuda(), smooth).cpu().numpy()
+    net.check_status()
+    disp = np.abs(host.astype(np.float64) - xb0).max()
+    assert disp > 0.1 * p.dx                       # the network moved the grid
+    assert np.abs(dev.astype(np.float64) - host).max() <= 1e-5 * max(disp, 1.0)
+    # line-tied z ghost planes and the held first / last inner planes stay at
+    # the identity (away from the periodic images, which are recomputed)
+    np.testing.assert_array_equal(dev[[0, 1, -2, -1], 1:-1, 1:-1], xb0[[0, 1, -2, -1], 1:-1, 1:-1])
