@@ -2,13 +2,13 @@
 (glemur_gb300/weights/unet_64x64x128.npz), held-out random braids on the
 64x64x128 grid reach the force-free residual 0.1 sooner from the network's
 grid than from the identity grid, counting the warm start's own cost
-(inference, smoothing, grid build, the min Delta > 0 acceptance check) in its
-time.  The held-out seeds lie outside the training range; every predicted
+(inference, the grid build on the device, the min Delta > 0 acceptance
+check) in its time.  The held-out seeds lie outside the training range; every predicted
 grid must be accepted (no folded cell).  The predicted grid starts at a
 higher residual than the identity grid (its small grid-scale errors show up
 as current), but its displacement is close to the relaxed one, so it needs
 far fewer attempts: on these seeds 1100 / 2100 / 1100 against 3900 / 5050 /
-2650, and 1.8x less wall time over 32 held-out seeds."""
+2650, and 2x less wall time over 32 held-out seeds."""
 import pytest
 
 pytestmark = pytest.mark.gpu
