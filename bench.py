@@ -239,6 +239,8 @@ def run_gpu(args):
     g = Relaxation(p)
     g.set_stream(stream.cuda_stream)
     g.upload(xb, B0)
+    # tile depth chosen by timing (stages 0..4 on the uploaded state, untimed here)
+    tune = g.autotune(3) if not args.no_autotune else None
     # warm-up (also captures the step graph)
     g.steps_async(max(args.warmup, 3))
     g.state()
@@ -299,6 +301,8 @@ def run_gpu(args):
     g2 = Relaxation(p)
     g2.set_stream(stream.cuda_stream)
     g2.upload_ptr(xb_h.data_ptr(), B0_h.data_ptr())
+    if not args.no_autotune:
+        g2.autotune(3)
     g2.steps_async(3)
     g2.state()
     barrier()
@@ -331,7 +335,8 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(p, {"attempted": st["nAttempted"], "accepted": st["timeIndex"]}),
+            "config": workload_config(p, {"attempted": st["nAttempted"], "accepted": st["timeIndex"],
+                                          "tile_z": tune["tz"] if tune else None}),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": peak_kind, "kernel": "k_stage (one RK stage)",
@@ -361,6 +366,7 @@ def run_batch(args):
     b = BatchRelaxation(ps)
     for c, (B0, xb) in enumerate(inits):
         b.upload(c, xb, B0)
+    tune = b.autotune(2) if not args.no_autotune else None   # work-item depth, untimed
     b.steps_async(max(args.warmup, 3))       # warm-up, captures the step graph
     b.state(0)
     for c, (B0, xb) in enumerate(inits):     # start every case afresh
@@ -407,7 +413,7 @@ def run_batch(args):
             "config": {"workload": "batch64: random braids, seeds 1000..1063, 2-8 blobs, sizes drawn from "
                                    "32^3, 48x48x96, 64x64x128, 96x96x192", "shapes": shapes,
                        "residual_target": args.batch_residual, "max_accepted": args.batch_cycles,
-                       "check_every": 10, "parallelism": "single"},
+                       "check_every": 10, "parallelism": "single", "tile_z": tune["tzb"] if tune else 32},
             "wall_s": wall, "p50_case_s": secs[len(secs) // 2], "p99_case_s": secs[min(len(secs) - 1, int(0.99 * len(secs)))],
             "converged": conv, "folded_dtmin": folded, "budget_reached": len(out) - conv - folded,
             "sequential_single_case": {"value": work / seq_t, "unit": UNIT, "seconds": seq_t},
@@ -424,6 +430,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the cost model's tile depth")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--workload", default="braid6", choices=["braid6", "batch64", "large"])
     ap.add_argument("--large-shape", default="256,256,512", help="grid of --workload large")

@@ -137,12 +137,14 @@ SIGNATURES = {
     "gm_set_dt": (C.c_int, [VP, C.c_double, C.c_double, C.c_int]),
     "gm_refresh": (C.c_int, [VP, P(GmReduction)]),
     "gm_download": (C.c_int, [VP, VP, VP, VP, VP]),
+    "gm_autotune": (C.c_int, [VP, C.c_int, P(C.c_int), P(C.c_double)]),
     "gm_download_k": (C.c_int, [VP, C.c_int, VP]),
     "gm_download_x": (C.c_int, [VP, C.c_int, VP]),
     "gm_upload_u": (C.c_int, [VP, VP]),
     "gm_download_u": (C.c_int, [VP, C.c_int, VP]),
     "gm_reduce_noalloc": (C.c_int, [P(GmParams), VP, VP, VP, VP, VP]),
     "gm_batch_create": (C.c_int, [P(GmParams), C.c_int, P(VP)]),
+    "gm_batch_autotune": (C.c_int, [VP, C.c_int, P(C.c_int), P(C.c_double)]),
     "gm_batch_destroy": (C.c_int, [VP]),
     "gm_batch_upload": (C.c_int, [VP, C.c_int, VP, VP, C.c_double, C.c_double]),
     "gm_batch_steps_async": (C.c_int, [VP, C.c_int]),

@@ -69,6 +69,12 @@ class BatchRelaxation:
                                          ptr(out["detJac"])), "gm_batch_download")
         return out
 
+    def autotune(self, trials: int = 3) -> dict:
+        """gm_batch_autotune: time work-item depths 16, 32, 64; keep the fastest."""
+        tzb, ms = C.c_int(), C.c_double()
+        check(self.lib.gm_batch_autotune(self.h, trials, C.byref(tzb), C.byref(ms)), "gm_batch_autotune")
+        return dict(tzb=tzb.value, ms_stages_0_4=ms.value)
+
     def stop(self, c: int):
         check(self.lib.gm_batch_stop(self.h, c), "gm_batch_stop")
 

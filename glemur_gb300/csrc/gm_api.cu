@@ -88,6 +88,7 @@ struct ImplBase {
     virtual int upload_u(const void* u) = 0;
     virtual int download_u(int which, void* u) = 0;
     virtual int step(gm_step_result* r) = 0;
+    virtual int autotune(int trials, int* tz, double* ms) = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     int64_t launches = 0;
@@ -490,6 +491,74 @@ struct Impl : ImplBase {
         return GM_OK;
     }
 
+    // Autotuner of the TMA stage kernel's z-chunk depth TZ2 (the tile shape in
+    // z: planes a CTA marches through, each chunk paying two halo planes).
+    // Candidates: the few best depths by the cost model of choose_tz2 and the
+    // current one.  Each is timed with CUDA events on the handle's stream over
+    // `trials` rounds of stages 0..4 on the uploaded state (those stages write
+    // only the stage buffers, not the step-start grid), after one untimed
+    // round; the fastest is kept and the step graph recaptured with it.
+    int autotune(int trials, int* tz_out, double* ms_out) override {
+        if (!uploaded) return gm::fail(GM_ENOTREADY, "gm_autotune before gm_upload");
+        if (trials < 1) return gm::fail(GM_EPARAM, "gm_autotune: trials must be >= 1");
+        if (!use_tma) {   // the generic kernel's tile is chosen by its own model
+            if (tz_out) *tz_out = TZ;
+            if (ms_out) *ms_out = 0;
+            return GM_OK;
+        }
+        int dev = 0, nsm = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const int nx = kp.nx, ny = kp.ny, nz = kp.nz, ty = gmk::stage_tma_ty<T>(gp.pressure);
+        const long long ncol = (long long)((nx + gmk::TX - 1) / gmk::TX) * ((ny + ty - 1) / ty);
+        std::vector<std::pair<double, int>> cand;
+        int last = -1;
+        for (int nzc = 1; nzc <= nz; nzc++) {
+            const int tz = (nz + nzc - 1) / nzc;
+            if (tz < 4 && nz >= 4) break;
+            if (tz == last) continue;
+            last = tz;
+            const long long tiles = ncol * ((nz + tz - 1) / tz);
+            cand.emplace_back((double)((tiles + nsm - 1) / nsm) * (tz + 2), tz);
+        }
+        std::sort(cand.begin(), cand.end());
+        std::vector<int> tzs;
+        for (size_t q = 0; q < cand.size() && tzs.size() < 4; q++) tzs.push_back(cand[q].second);
+        if (std::find(tzs.begin(), tzs.end(), TZ2) == tzs.end()) tzs.push_back(TZ2);
+        cudaEvent_t e0, e1;
+        CUDA_TRY(cudaEventCreate(&e0));
+        CUDA_TRY(cudaEventCreate(&e1));
+        double best_ms = 1e300;
+        int best_tz = TZ2;
+        int rc = GM_OK;
+        for (int tz : tzs) {
+            TZ2 = tz;
+            grid2 = dim3(grid2.x, grid2.y, (unsigned)((nz + tz - 1) / tz));
+            for (int r = 0; r <= trials && rc == GM_OK; r++) {
+                if (r == 1 && cudaEventRecord(e0, stream) != cudaSuccess) rc = GM_ECUDA;
+                for (int n = 0; n < 5 && rc == GM_OK; n++) rc = stage(n);
+            }
+            if (rc != GM_OK) break;
+            float ms = 0;
+            if (cudaEventRecord(e1, stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                rc = gm::fail(GM_ECUDA, "gm_autotune: event timing failed");
+                break;
+            }
+            if (ms < best_ms) { best_ms = ms; best_tz = tz; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        TZ2 = best_tz;
+        grid2 = dim3(grid2.x, grid2.y, (unsigned)((nz + best_tz - 1) / best_tz));
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+        if (rc != GM_OK) return rc;
+        if (tz_out) *tz_out = best_tz;
+        if (ms_out) *ms_out = best_ms / trials;
+        return GM_OK;
+    }
+
     int read_state() {
         CUDA_TRY(cudaMemcpyAsync(h_st, st, sizeof(DevState), cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
@@ -743,14 +812,17 @@ struct BatchBase {
     virtual int download(int c, void* xb, void* B, void* J, void* D) = 0;
     virtual int stop(int c) = 0;
     virtual int run(int nCycle, double residual, int pointwise, int checkEvery, gm_batch_case* out) = 0;
+    virtual int autotune(int trials, int* tzb, double* ms) = 0;
     int ncases = 0;
     int64_t launches = 0;
 };
 
 template <typename T>
 struct Batch : BatchBase {
-    static constexpr int TZB = 32;          // planes per work item
+    int TZB = 32;                           // planes per work item (gm_batch_autotune)
     std::vector<std::unique_ptr<Impl<T>>> cs;
+    std::vector<StageArgsTMA<T>> hcases;    // host copy of d_cases
+    std::vector<gm_params> params;
     cudaStream_t stream = nullptr;
     StageArgsTMA<T>* d_cases = nullptr;
     int4* d_work = nullptr;
@@ -777,8 +849,9 @@ struct Batch : BatchBase {
             if ((ps[c].pressure != 0) != (pressure != 0) || ps[c].precision != ps[0].precision)
                 return gm::fail(GM_EPARAM, "gm_batch_create: all cases need the same precision and pressure flag");
         CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        std::vector<StageArgsTMA<T>> h(n);
-        std::vector<std::pair<long long, int>> order;
+        hcases.resize(n);
+        params.assign(ps, ps + n);
+        std::vector<StageArgsTMA<T>>& h = hcases;
         for (int c = 0; c < n; c++) {
             gm_params p = ps[c];
             p.stageKernel = 0;
@@ -791,32 +864,93 @@ struct Batch : BatchBase {
             cs.back()->stream = stream;
             memcpy(h[c].tm, cs.back()->tmaps_b, sizeof h[c].tm);
             h[c].a = cs.back()->args(0);
-            h[c].a.TZ = TZB;
+        }
+        CUDA_TRY(cudaMalloc((void**)&d_cases, n * sizeof(StageArgsTMA<T>)));
+        CUDA_TRY(cudaMalloc((void**)&d_counters, 8 * sizeof(int)));
+        CUDA_TRY(cudaMemsetAsync(d_counters, 0, 8 * sizeof(int), stream));
+        int rc = set_work(TZB);
+        if (rc) return rc;
+        int dev = 0, nsm = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        nblocks = nsm * gmk::stage_tma_batch_occupancy<T>(pressure);
+        return GM_OK;
+    }
+
+    // Work items of depth tzb planes, largest cases first; the cases' TZ and
+    // the device copies follow.
+    int set_work(int tzb) {
+        TZB = tzb;
+        std::vector<std::pair<long long, int>> order;
+        for (int c = 0; c < ncases; c++) {
+            hcases[c].a.TZ = TZB;
+            const gm_params& p = params[c];
             order.emplace_back(-(long long)p.nx * p.ny * p.nz, c);
         }
-        // work items, largest cases first
         std::sort(order.begin(), order.end());
         std::vector<int4> work;
         for (auto& o : order) {
-            const gm_params& p = ps[o.second];
+            const gm_params& p = params[o.second];
             const int nbx = (p.nx + gmk::TX - 1) / gmk::TX, nby = (p.ny + gmk::STAGE_BATCH_TY - 1) / gmk::STAGE_BATCH_TY;
             const int nbz = (p.nz + TZB - 1) / TZB;
             for (int bz = 0; bz < nbz; bz++)
                 for (int by = 0; by < nby; by++)
                     for (int bx = 0; bx < nbx; bx++) work.push_back(make_int4(o.second, bx, by, bz));
         }
-        nwork = (int)work.size();
-        CUDA_TRY(cudaMalloc((void**)&d_cases, n * sizeof(StageArgsTMA<T>)));
-        CUDA_TRY(cudaMalloc((void**)&d_work, work.size() * sizeof(int4)));
-        CUDA_TRY(cudaMalloc((void**)&d_counters, 8 * sizeof(int)));
-        CUDA_TRY(cudaMemcpyAsync(d_cases, h.data(), n * sizeof(StageArgsTMA<T>), cudaMemcpyHostToDevice, stream));
-        CUDA_TRY(cudaMemcpyAsync(d_work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice, stream));
-        CUDA_TRY(cudaMemsetAsync(d_counters, 0, 8 * sizeof(int), stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
-        int dev = 0, nsm = 152;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        nblocks = nsm * gmk::stage_tma_batch_occupancy<T>(pressure);
+        if (d_work) CUDA_TRY(cudaFree(d_work));
+        d_work = nullptr;
+        nwork = (int)work.size();
+        CUDA_TRY(cudaMalloc((void**)&d_work, work.size() * sizeof(int4)));
+        CUDA_TRY(cudaMemcpyAsync(d_cases, hcases.data(), ncases * sizeof(StageArgsTMA<T>), cudaMemcpyHostToDevice,
+                                 stream));
+        CUDA_TRY(cudaMemcpyAsync(d_work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+        return GM_OK;
+    }
+
+    // Autotuner of the work-item depth (planes per tile): each candidate is
+    // timed with CUDA events over `trials` rounds of the batched stages 0..4
+    // (which write only the cases' stage buffers), after one untimed round;
+    // the fastest is kept.
+    int autotune(int trials, int* tzb_out, double* ms_out) override {
+        if (!uploaded_all()) return gm::fail(GM_ENOTREADY, "gm_batch_autotune before every case is uploaded");
+        if (trials < 1) return gm::fail(GM_EPARAM, "gm_batch_autotune: trials must be >= 1");
+        cudaEvent_t e0, e1;
+        CUDA_TRY(cudaEventCreate(&e0));
+        CUDA_TRY(cudaEventCreate(&e1));
+        double best_ms = 1e300;
+        int best = TZB, rc = GM_OK;
+        for (int tzb : {16, 32, 64}) {
+            if ((rc = set_work(tzb))) break;
+            for (int r = 0; r <= trials && rc == GM_OK; r++) {
+                if (r == 1 && cudaEventRecord(e0, stream) != cudaSuccess) rc = GM_ECUDA;
+                for (int n = 0; n < 5 && rc == GM_OK; n++) {
+                    if (cudaMemsetAsync(d_counters + n, 0, sizeof(int), stream) != cudaSuccess ||
+                        gmk::launch_stage_tma_batch<T>(d_cases, d_work, nwork, d_counters + n, n, pressure, nblocks,
+                                                       stream) != cudaSuccess)
+                        rc = gm::fail(GM_ECUDA, "gm_batch_autotune: launch failed");
+                }
+            }
+            if (rc != GM_OK) break;
+            float ms = 0;
+            if (cudaEventRecord(e1, stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                rc = gm::fail(GM_ECUDA, "gm_batch_autotune: event timing failed");
+                break;
+            }
+            if (ms < best_ms) { best_ms = ms; best = tzb; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        const int rc2 = set_work(best);
+        if (cudaMemsetAsync(d_counters, 0, 8 * sizeof(int), stream) != cudaSuccess && rc == GM_OK) rc = GM_ECUDA;
+        if (rc != GM_OK) return rc;
+        if (rc2 != GM_OK) return rc2;
+        if (tzb_out) *tzb_out = best;
+        if (ms_out) *ms_out = best_ms / trials;
         return GM_OK;
     }
 
@@ -1064,6 +1198,11 @@ int gm_download_u(gm_handle* h, int which, void* u) {
     return h->impl->download_u(which, u);
 }
 
+int gm_autotune(gm_handle* h, int trials, int* tz, double* ms) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->autotune(trials, tz, ms);
+}
+
 int gm_download_k(gm_handle* h, int m, void* k) {
     if (!h) return gm::fail(GM_EPARAM, "null handle");
     return h->impl->download_k(m, k);
@@ -1096,6 +1235,11 @@ int gm_batch_create(const gm_params* cases, int nCases, gm_batch** out) {
     }
     *out = b;
     return GM_OK;
+}
+
+int gm_batch_autotune(gm_batch* b, int trials, int* tzb, double* ms) {
+    if (!b) return gm::fail(GM_EPARAM, "null batch");
+    return b->impl->autotune(trials, tzb, ms);
 }
 
 int gm_batch_destroy(gm_batch* b) {

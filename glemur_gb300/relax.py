@@ -135,6 +135,12 @@ class Relaxation:
         check(self.lib.gm_download_x(self.h, which, ptr(x)), "gm_download_x")
         return x
 
+    def autotune(self, trials: int = 3) -> dict:
+        """gm_autotune: time the stage kernel's z-chunk depths, keep the fastest."""
+        tz, ms = C.c_int(), C.c_double()
+        check(self.lib.gm_autotune(self.h, trials, C.byref(tz), C.byref(ms)), "gm_autotune")
+        return dict(tz=tz.value, ms_stages_0_4=ms.value)
+
     def upload_u(self, u: np.ndarray):
         """Velocity of an inertia run at the inner points, [nz, ny, nx, 3]."""
         u = np.ascontiguousarray(u, dtype=self.dtype)

@@ -267,6 +267,17 @@ int gm_download(gm_handle* h, void* xb, void* B, void* J, void* detJac);
  * the 8 corner wedge products (gridWedgeMin, maths.cu:494-569). */
 int gm_grid_fields(gm_handle* h, void* cellVol, void* convexity, void* wedgeMin);
 
+/* Autotuner of the stage kernel's z-chunk depth (the planes one CTA
+ * marches through): times `trials` rounds of stages 0..4 on the uploaded
+ * state for each candidate depth (the cost model's best few and the current
+ * one) with CUDA events on the handle's stream, keeps the fastest and
+ * recaptures the step graph.  Stages 0..4 write only the stage buffers, so
+ * the state a run starts from is unchanged; results do not depend on the
+ * depth.  Call after gm_upload; *tz and *ms (mean time of stages 0..4) may be
+ * NULL.  No counterpart in the reference (its block shape is fixed,
+ * src/main.cu:130-137). */
+int gm_autotune(gm_handle* h, int trials, int* tz, double* ms);
+
 /* Stage increments k_0..k_4 of the last step (inner AoS in the reference kk
  * layout src/rungeKutta.cu:236: 3*nx*ny*nz values each, or 6*nx*ny*nz with
  * inertia, the position increment then the velocity increment per point)
@@ -342,6 +353,10 @@ typedef struct gm_batch_case {
 
 int gm_batch_create(const gm_params* cases, int nCases, gm_batch** out);
 int gm_batch_destroy(gm_batch* b);
+/* Autotuner of the batched work-item depth (planes per tile: 16, 32 or 64),
+ * timed as gm_autotune does over the batched stages 0..4; call after every
+ * case is uploaded.  No counterpart in the reference. */
+int gm_batch_autotune(gm_batch* b, int trials, int* tzb, double* ms);
 int gm_batch_upload(gm_batch* b, int c, const void* xb, const void* B0, double t, double dt);
 /* Enqueue nSteps attempted steps of every case (graph replays, no sync). */
 int gm_batch_steps_async(gm_batch* b, int nSteps);

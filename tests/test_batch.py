@@ -97,3 +97,42 @@ def test_batch_run_stops_each_case():
         assert o["seconds"] > 0 and o["attempted"] == s["nAttempted"]
     assert any(o["converged"] for o in out)
     b.close()
+
+
+@pytest.mark.gpu
+def test_autotuners_keep_results_identical():
+    """gm_autotune / gm_batch_autotune time tile depths on the uploaded state
+    (stages 0..4 only) and keep the fastest: the run that follows must equal
+    an untuned run bit for bit, since no arithmetic depends on the tiling."""
+    p = configs.random_braid(11, shape=(64, 48, 96), precision=32)
+    B0, xb = configs.init_state(p)
+    runs = []
+    for tune in (False, True):
+        g = Relaxation(p)
+        g.upload(xb, B0)
+        if tune:
+            r = g.autotune(2)
+            assert r["tz"] >= 4 and r["ms_stages_0_4"] > 0
+        g.steps_async(30)
+        runs.append((g.state(), g.download()))
+        g.close()
+    (s0, f0), (s1, f1) = runs
+    for k in ("t", "dt", "timeIndex", "nAttempted"):
+        assert s0[k] == s1[k], k
+    np.testing.assert_array_equal(f0["xb"], f1["xb"])
+    ps = cases(32)
+    outs = []
+    for tune in (False, True):
+        b = BatchRelaxation(ps)
+        for c, q in enumerate(ps):
+            B0, xb = configs.init_state(q)
+            b.upload(c, xb, B0)
+        if tune:
+            r = b.autotune(2)
+            assert r["tzb"] in (16, 32, 64) and r["ms_stages_0_4"] > 0
+        b.steps_async(20)
+        outs.append([(b.state(c)["nAttempted"], b.download(c)["xb"]) for c in range(len(ps))])
+        b.close()
+    for (n0, x0), (n1, x1) in zip(*outs):
+        assert n0 == n1
+        np.testing.assert_array_equal(x0, x1)
