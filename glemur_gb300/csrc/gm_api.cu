@@ -913,8 +913,10 @@ struct Batch : BatchBase {
 
     // Autotuner of the work-item depth (planes per tile): each candidate is
     // timed with CUDA events over `trials` rounds of the batched stages 0..4
-    // (which write only the cases' stage buffers), after one untimed round;
-    // the fastest is kept.
+    // (which write only the cases' stage buffers), after one untimed round.
+    // The timing has every case active; as cases finish, fewer and larger
+    // items balance worse, so the smallest depth within 3 % of the fastest is
+    // kept.
     int autotune(int trials, int* tzb_out, double* ms_out) override {
         if (!uploaded_all()) return gm::fail(GM_ENOTREADY, "gm_batch_autotune before every case is uploaded");
         if (trials < 1) return gm::fail(GM_EPARAM, "gm_batch_autotune: trials must be >= 1");
@@ -923,7 +925,10 @@ struct Batch : BatchBase {
         CUDA_TRY(cudaEventCreate(&e1));
         double best_ms = 1e300;
         int best = TZB, rc = GM_OK;
-        for (int tzb : {16, 32, 64}) {
+        double t_of[3] = {0, 0, 0};
+        const int cands[3] = {16, 32, 64};
+        for (int ci = 0; ci < 3; ci++) {
+            const int tzb = cands[ci];
             if ((rc = set_work(tzb))) break;
             for (int r = 0; r <= trials && rc == GM_OK; r++) {
                 if (r == 1 && cudaEventRecord(e0, stream) != cudaSuccess) rc = GM_ECUDA;
@@ -941,10 +946,14 @@ struct Batch : BatchBase {
                 rc = gm::fail(GM_ECUDA, "gm_batch_autotune: event timing failed");
                 break;
             }
-            if (ms < best_ms) { best_ms = ms; best = tzb; }
+            t_of[ci] = ms;
+            if (ms < best_ms) best_ms = ms;
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        const double fastest = best_ms;
+        for (int ci = 2; ci >= 0; ci--)
+            if (rc == GM_OK && t_of[ci] > 0 && t_of[ci] <= 1.03 * fastest) { best = cands[ci]; best_ms = t_of[ci]; }
         const int rc2 = set_work(best);
         if (cudaMemsetAsync(d_counters, 0, 8 * sizeof(int), stream) != cudaSuccess && rc == GM_OK) rc = GM_ECUDA;
         if (rc != GM_OK) return rc;
