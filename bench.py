@@ -240,7 +240,11 @@ def run_gpu(args):
     g.set_stream(stream.cuda_stream)
     g.upload(xb, B0)
     # tile depth chosen by timing (stages 0..4 on the uploaded state, untimed here)
-    tune = g.autotune(3) if not args.no_autotune else None
+    if args.tile_z:
+        g.set_tile_z(args.tile_z)
+        tune = {"tz": args.tile_z}
+    else:
+        tune = g.autotune(3) if not args.no_autotune else None
     # warm-up (also captures the step graph)
     g.steps_async(max(args.warmup, 3))
     g.state()
@@ -301,7 +305,9 @@ def run_gpu(args):
     g2 = Relaxation(p)
     g2.set_stream(stream.cuda_stream)
     g2.upload_ptr(xb_h.data_ptr(), B0_h.data_ptr())
-    if not args.no_autotune:
+    if args.tile_z:
+        g2.set_tile_z(args.tile_z)
+    elif not args.no_autotune:
         g2.autotune(3)
     g2.steps_async(3)
     g2.state()
@@ -431,6 +437,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the cost model's tile depth")
+    ap.add_argument("--tile-z", type=int, default=0, help="set the stage kernel's z-chunk depth (no autotuning)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--workload", default="braid6", choices=["braid6", "batch64", "large"])
     ap.add_argument("--large-shape", default="256,256,512", help="grid of --workload large")

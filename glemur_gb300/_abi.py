@@ -138,6 +138,7 @@ SIGNATURES = {
     "gm_refresh": (C.c_int, [VP, P(GmReduction)]),
     "gm_download": (C.c_int, [VP, VP, VP, VP, VP]),
     "gm_autotune": (C.c_int, [VP, C.c_int, P(C.c_int), P(C.c_double)]),
+    "gm_set_tile_z": (C.c_int, [VP, C.c_int]),
     "gm_download_k": (C.c_int, [VP, C.c_int, VP]),
     "gm_download_x": (C.c_int, [VP, C.c_int, VP]),
     "gm_upload_u": (C.c_int, [VP, VP]),

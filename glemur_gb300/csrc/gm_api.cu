@@ -89,6 +89,7 @@ struct ImplBase {
     virtual int download_u(int which, void* u) = 0;
     virtual int step(gm_step_result* r) = 0;
     virtual int autotune(int trials, int* tz, double* ms) = 0;
+    virtual int set_tile_z(int tz) = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     int64_t launches = 0;
@@ -556,6 +557,16 @@ struct Impl : ImplBase {
         if (rc != GM_OK) return rc;
         if (tz_out) *tz_out = best_tz;
         if (ms_out) *ms_out = best_ms / trials;
+        return GM_OK;
+    }
+
+    int set_tile_z(int tz) override {
+        if (!use_tma) return gm::fail(GM_EPARAM, "gm_set_tile_z: the run does not use the TMA stage kernel");
+        if (tz < 1 || tz > kp.nz) return gm::fail(GM_EPARAM, "gm_set_tile_z: depth must be 1..nz");
+        TZ2 = tz;
+        grid2 = dim3(grid2.x, grid2.y, (unsigned)((kp.nz + tz - 1) / tz));
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
         return GM_OK;
     }
 
@@ -1205,6 +1216,11 @@ int gm_upload_u(gm_handle* h, const void* u) {
 int gm_download_u(gm_handle* h, int which, void* u) {
     if (!h) return gm::fail(GM_EPARAM, "null handle");
     return h->impl->download_u(which, u);
+}
+
+int gm_set_tile_z(gm_handle* h, int tz) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->set_tile_z(tz);
 }
 
 int gm_autotune(gm_handle* h, int trials, int* tz, double* ms) {

@@ -141,6 +141,9 @@ class Relaxation:
         check(self.lib.gm_autotune(self.h, trials, C.byref(tz), C.byref(ms)), "gm_autotune")
         return dict(tz=tz.value, ms_stages_0_4=ms.value)
 
+    def set_tile_z(self, tz: int):
+        check(self.lib.gm_set_tile_z(self.h, tz), "gm_set_tile_z")
+
     def upload_u(self, u: np.ndarray):
         """Velocity of an inertia run at the inner points, [nz, ny, nx, 3]."""
         u = np.ascontiguousarray(u, dtype=self.dtype)

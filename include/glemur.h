@@ -277,6 +277,10 @@ int gm_grid_fields(gm_handle* h, void* cellVol, void* convexity, void* wedgeMin)
  * NULL.  No counterpart in the reference (its block shape is fixed,
  * src/main.cu:130-137). */
 int gm_autotune(gm_handle* h, int trials, int* tz, double* ms);
+/* Set the stage kernel's z-chunk depth directly (1..nz; the TMA stage kernel
+ * only), e.g. to repeat a depth gm_autotune chose; the step graph is
+ * recaptured.  No counterpart in the reference. */
+int gm_set_tile_z(gm_handle* h, int tz);
 
 /* Stage increments k_0..k_4 of the last step (inner AoS in the reference kk
  * layout src/rungeKutta.cu:236: 3*nx*ny*nz values each, or 6*nx*ny*nz with
