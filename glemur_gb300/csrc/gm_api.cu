@@ -494,8 +494,8 @@ struct Impl : ImplBase {
 
     // Autotuner of the TMA stage kernel's z-chunk depth TZ2 (the tile shape in
     // z: planes a CTA marches through, each chunk paying two halo planes).
-    // Candidates: the few best depths by the cost model of choose_tz2 and the
-    // current one.  Each is timed with CUDA events on the handle's stream over
+    // Candidates: the eight best depths by the cost model of choose_tz2 and
+    // the current one.  Each is timed with CUDA events on the handle's stream over
     // `trials` rounds of stages 0..4 on the uploaded state (those stages write
     // only the stage buffers, not the step-start grid), after one untimed
     // round; the fastest is kept and the step graph recaptured with it.
@@ -524,7 +524,7 @@ struct Impl : ImplBase {
         }
         std::sort(cand.begin(), cand.end());
         std::vector<int> tzs;
-        for (size_t q = 0; q < cand.size() && tzs.size() < 4; q++) tzs.push_back(cand[q].second);
+        for (size_t q = 0; q < cand.size() && tzs.size() < 8; q++) tzs.push_back(cand[q].second);
         if (std::find(tzs.begin(), tzs.end(), TZ2) == tzs.end()) tzs.push_back(TZ2);
         cudaEvent_t e0, e1;
         CUDA_TRY(cudaEventCreate(&e0));

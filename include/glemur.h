@@ -269,7 +269,7 @@ int gm_grid_fields(gm_handle* h, void* cellVol, void* convexity, void* wedgeMin)
 
 /* Autotuner of the stage kernel's z-chunk depth (the planes one CTA
  * marches through): times `trials` rounds of stages 0..4 on the uploaded
- * state for each candidate depth (the cost model's best few and the current
+ * state for each candidate depth (the cost model's best eight and the current
  * one) with CUDA events on the handle's stream, keeps the fastest and
  * recaptures the step graph.  Stages 0..4 write only the stage buffers, so
  * the state a run starts from is unchanged; results do not depend on the
