@@ -91,6 +91,8 @@ int run(gm_params& p, long activeDevice) {
     }
     if (gm_upload(h, xb.data(), B0.data(), t, dt)) return fail("could not copy the state to the device");
     if (p.inertia && p.fRestart && gm_upload_u(h, u.data())) return fail("could not copy the velocity to the device");
+    // the stage kernel's tile depth, timed once on this state (results do not depend on it)
+    if (gm_autotune(h, 2, nullptr, nullptr)) return fail("autotuning failed");
 
     gm_state s;
     memset(&s, 0, sizeof s);
