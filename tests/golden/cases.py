@@ -18,6 +18,10 @@ reference's boundary handling:
   the oracle only.)
 * inertia_f64 / inertia_f32 -- the velocity equation (inertia = T,
   src/rungeKutta.cu:195-212, 311-322) with damping nu = 1.
+* inertia_press_f64, classic_press_tied_f64, classic_inertia_tied_f64 -- the
+  options together: the pressure force in the velocity equation, the
+  pressure gradient beside the Classic current (both read Delta), and the
+  Classic current driving the velocity equation.
 """
 from __future__ import annotations
 
@@ -56,6 +60,23 @@ def make(name: str):
         p.inertia = 1
         p.nu = 1.0
         return configs.derive(p)
+    if name == "inertia_press_f64":
+        p = _braid((17, 17, 18), 64)
+        p.inertia = 1
+        p.nu = 1.0
+        p.pressure = 1
+        p.beta = 0.05
+        return configs.derive(p)
+    if name in ("classic_press_tied_f64", "classic_inertia_tied_f64"):
+        p = _braid((17, 12, 17), 64, peri=(0, 0, 0))
+        p.set_str("jMethod", "Classic")
+        if name == "classic_press_tied_f64":
+            p.pressure = 1
+            p.beta = 0.05
+        else:
+            p.inertia = 1
+            p.nu = 1.0
+        return configs.derive(p)
     if name == "analytic_f64":
         p = configs.defaults(64)
         p.nx, p.ny, p.nz = 16, 16, 16
@@ -74,5 +95,6 @@ def make(name: str):
 
 
 NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64", "classic_tied_f64",
-         "classic_tied_f32", "inertia_f64", "inertia_f32"]
+         "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64", "classic_press_tied_f64",
+         "classic_inertia_tied_f64"]
 N_ACCEPTED = 10
