@@ -68,7 +68,9 @@ def make(name: str):
         p.beta = 0.05
         return configs.derive(p)
     if name in ("classic_press_tied_f64", "classic_inertia_tied_f64"):
-        p = _braid((17, 12, 17), 64, peri=(0, 0, 0))
+        # nz = 18 with inertia: the reference's inertia blocks are 4 deep, and
+        # JClassic leaves the edge halo of a block one layer deep unloaded
+        p = _braid((17, 12, 17 if name == "classic_press_tied_f64" else 18), 64, peri=(0, 0, 0))
         p.set_str("jMethod", "Classic")
         if name == "classic_press_tied_f64":
             p.pressure = 1
