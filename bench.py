@@ -106,11 +106,20 @@ class Clocks:
     def __init__(self, gpu_index=0):
         self.idx = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        # the raw samples: GLEMUR_CLOCKS_CSV keeps them at a chosen path,
+        # otherwise a temporary file is used and removed after the summary
+        keep = os.environ.get("GLEMUR_CLOCKS_CSV")
+        if keep:
+            self.path, self.temp = Path(keep), False
+        else:
+            import tempfile
+            fd, name = tempfile.mkstemp(prefix="glemur_clocks_", suffix=".csv")
+            os.close(fd)
+            self.path, self.temp = Path(name), True
 
     def __enter__(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
+            self.path.parent.mkdir(parents=True, exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -129,10 +138,13 @@ class Clocks:
             self.f.close()
 
     def summary(self):
-        if not self.proc or not self.path.exists():
+        text = self.path.read_text() if self.path.exists() else ""
+        if self.temp:
+            self.path.unlink(missing_ok=True)
+        if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         rows = []
-        for line in self.path.read_text().splitlines():
+        for line in text.splitlines():
             f = [x.strip() for x in line.split(",")]
             if len(f) >= 9:
                 rows.append(f)
