@@ -136,11 +136,12 @@ class Clocks:
             except Exception:
                 self.proc.kill()
             self.f.close()
-
-    def summary(self):
-        text = self.path.read_text() if self.path.exists() else ""
+        self.text = self.path.read_text() if self.path.exists() else ""
         if self.temp:
             self.path.unlink(missing_ok=True)
+
+    def summary(self):
+        text = getattr(self, "text", "")
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         rows = []
