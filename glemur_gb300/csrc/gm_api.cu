@@ -61,7 +61,6 @@ int check_params(const gm_params* p) {
     if (strncmp(p->jMethod, "Stokes ", 7) != 0 && strncmp(p->jMethod, "Classic ", 8) != 0)
         return gm::fail(GM_EPARAM, "jMethod: the Stokes and Classic currents are implemented");
     if (p->pressure && strncmp(p->pMethod, "Classic ", 8) != 0) return gm::fail(GM_EPARAM, "pMethod must be Classic");
-    if (p->jxbAver) return gm::fail(GM_EPARAM, "jxbAver = T is not implemented");
     if (p->initShearA != 0 || p->initShearB != 0)
         return gm::fail(GM_EPARAM, "initial-distortion ghost corrections (initShearA/B != 0) are not implemented");
     if (!(p->dx > 0 && p->dy > 0 && p->dz > 0)) return gm::fail(GM_EPARAM, "dx, dy, dz must be > 0 (call gm_params_derive)");
@@ -131,6 +130,7 @@ struct Impl : ImplBase {
     int nparts = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    int64_t step_launches = 7;      // kernel launches in the captured step
     // TMA-fed stage kernel: tensor maps of X[0], X[1], XS[0], XS[1]
     bool use_tma = true;
     CUtensorMap tmaps[10];      // single-case kernel (tile height stage_tma_ty<T>(pressure))
@@ -187,6 +187,8 @@ struct Impl : ImplBase {
         kp.jClassic = strncmp(p->jMethod, "Classic ", 8) == 0;
         kp.inertia = p->inertia != 0;
         kp.nu = (T)p->nu;
+        kp.jxbAver = p->jxbAver != 0 && !p->inertia;   // the reference applies it in the frictional branch only
+        kp.jxbW = (T)p->jxbAverWeight;
         kp.beta = (T)p->beta;
         kp.p0Amp = (T)p->p0Amp;
         kp.p0W2 = (T)(p->p0Width * p->p0Width);
@@ -297,9 +299,9 @@ struct Impl : ImplBase {
         smem_diag = gmk::stage_smem_bytes<T>(TY, gmk::MODE_DIAG, p->pressure);
         nparts = (int)(grid.x * grid.y * grid.z);
         // the TMA kernel computes the Stokes current of the frictional
-        // equation only; the Classic current and the inertial equation run in
-        // the generic kernel
-        use_tma = p->stageKernel == 0 && strncmp(p->jMethod, "Classic ", 8) != 0 && !p->inertia;
+        // equation only; the Classic current, the inertial equation and the
+        // averaged Lorentz force run in the generic kernel
+        use_tma = p->stageKernel == 0 && strncmp(p->jMethod, "Classic ", 8) != 0 && !p->inertia && !p->jxbAver;
         if (use_tma) {
             if ((rc = init_tma(nsm))) return rc;
         }
@@ -442,6 +444,16 @@ struct Impl : ImplBase {
             A.a.TZ = TZ2;
             CUDA_TRY(gmk::launch_stage_tma<T>(A, gp.pressure, grid2, stream));
         } else {
+            if (kp.jxbAver) {
+                // the averaged Lorentz force reads J and B of this stage at every
+                // point's neighbours (current() before kk(), main.cu:272-281):
+                // a J pass exports them first
+                StageArgs<T> aj = args(n);
+                aj.jpass = 1;
+                CUDA_TRY(gmk::launch_stage<T>(aj, gmk::MODE_DIAG, gp.pressure, grid, block, smem_diag, stream));
+                CUDA_TRY(gmk::launch_export_ghosts<T>(kp, outB, outD, stream));
+                launches += 1 + kp.xPeri + kp.yPeri + kp.zPeri;
+            }
             StageArgs<T> a = args(n);
             CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_STAGE, gp.pressure, grid, block, smem_stage, stream));
         }
@@ -478,6 +490,7 @@ struct Impl : ImplBase {
             cudaGraph_t g = nullptr;
             cudaError_t e2 = cudaStreamEndCapture(cs, &g);
             stream = saved;
+            step_launches = launches - saved_launches;
             launches = saved_launches;
             cudaStreamDestroy(cs);
             if (e != cudaSuccess || rc != GM_OK || e2 != cudaSuccess)
@@ -487,7 +500,7 @@ struct Impl : ImplBase {
         }
         for (int s = 0; s < nsteps; s++) {
             CUDA_TRY(cudaGraphLaunch(gexec, stream));
-            launches += 7;
+            launches += step_launches;
         }
         return GM_OK;
     }
@@ -868,7 +881,7 @@ struct Batch : BatchBase {
             p.stageKernel = 0;
             int rc = check_params(&p);
             if (rc) return rc;
-            if (strncmp(p.jMethod, "Stokes ", 7) != 0 || p.inertia)
+            if (strncmp(p.jMethod, "Stokes ", 7) != 0 || p.inertia || p.jxbAver)
                 return gm::fail(GM_EPARAM, "gm_batch_create: batched cases use the frictional equation and the Stokes current");
             cs.emplace_back(new Impl<T>());
             if ((rc = cs.back()->init(&p))) return rc;

@@ -69,6 +69,8 @@ struct KP {
     int jClassic;            // jMethod = "Classic": the finite-difference current (generic kernel only)
     int inertia;             // the velocity equation (generic kernel only)
     T nu;                    // velocity damping
+    int jxbAver;             // neighbour-averaged Lorentz force (generic kernel only)
+    T jxbW;                  // its weight
     T beta, p0Amp, p0W2;     // pressure: p0(X) = beta (1 + p0Amp exp(-(X^2+Y^2)/p0W2))
     T inv_p0W2;              // 1 / p0W2
     double maxError, dtMin;  // run-precision values widened to double
@@ -112,6 +114,7 @@ struct StageArgs {
     double* log;             // per attempt: maxDelta, dt after the update, accepted
     int n;                   // stage index 0..5
     int TZ;                  // planes per CTA
+    int jpass;               // diagnostic mode on the stage's own input grid (the J pass of jxbAver)
     // diagnostic mode outputs (reference layout) and partials
     T* outB;                 // ghosted AoS
     T* outJ;                 // inner AoS

@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
     t.i0 = i0; t.j0 = j0;
     const int kend = min(k0 + a.TZ, p.nz);
     const int cur = st->cur;
-    const T* __restrict__ Xin = (MODE == MODE_DIAG || a.n == 0) ? a.X[cur] : a.XS[(a.n - 1) & 1];
+    const T* __restrict__ Xin = ((MODE == MODE_DIAG && !a.jpass) || a.n == 0) ? a.X[cur] : a.XS[(a.n - 1) & 1];
     const T dtT = (T)st->dt;
     const int n = a.n;
     const long long N = p.N;
@@ -494,6 +494,36 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                     T uc[3] = {0, 0, 0}, ku[3] = {0, 0, 0};
                     if (!p.inertia) {
                         cross3(Jv, Bc, kn);
+                        if (p.jxbAver) {
+                            // rungeKutta.cu:172-178, 357-443: J x B at the six face
+                            // neighbours from this stage's J (inner) and B (ghosted),
+                            // written by the J pass; the +z neighbour's B with the
+                            // reference's plane stride (nx+1)(ny+1)
+                            const T w6 = p.jxbW / (T)6;
+                            const long long nx2 = p.nx + 2, ny2 = p.ny + 2;
+#pragma unroll
+                            for (int l = 0; l < 3; l++) kn[l] *= ((T)1 - p.jxbW);
+#pragma unroll
+                            for (int m = 0; m < 6; m++) {
+                                bool in = false;
+                                long long qj = 0, qb = 0;
+                                if (m == 0) { in = i > 0; qj = lin - 1; qb = i + nx2 * ((j + 1) + ny2 * (long long)(kc + 1)); }
+                                else if (m == 1) { in = i < p.nx - 1; qj = lin + 1; qb = (i + 2) + nx2 * ((j + 1) + ny2 * (long long)(kc + 1)); }
+                                else if (m == 2) { in = j > 0; qj = lin - p.nx; qb = (i + 1) + nx2 * (j + ny2 * (long long)(kc + 1)); }
+                                else if (m == 3) { in = j < p.ny - 1; qj = lin + p.nx; qb = (i + 1) + nx2 * ((j + 2) + ny2 * (long long)(kc + 1)); }
+                                else if (m == 4) { in = kc > 0; qj = lin - (long long)p.nx * p.ny; qb = (i + 1) + nx2 * ((j + 1) + ny2 * (long long)kc); }
+                                else { in = kc < p.nz - 1; qj = lin + (long long)p.nx * p.ny;
+                                       qb = (i + 1) + nx2 * (j + 1) + (long long)(kc + 2) * (p.nx + 1) * (p.ny + 1); }
+                                T c[3] = {0, 0, 0};
+                                if (in) {
+                                    const T jn[3] = {a.outJ[3 * qj], a.outJ[3 * qj + 1], a.outJ[3 * qj + 2]};
+                                    const T bn[3] = {a.outB[3 * qb], a.outB[3 * qb + 1], a.outB[3 * qb + 2]};
+                                    cross3(jn, bn, c);
+                                }
+#pragma unroll
+                                for (int l = 0; l < 3; l++) kn[l] += c[l] * w6;
+                            }
+                        }
                         const T eps = p.ex[i] * p.ey[j] * p.ez[kc];
                         const T f = dtT * eps;
 #pragma unroll

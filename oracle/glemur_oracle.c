@@ -64,6 +64,8 @@ typedef struct {
     int jClassic;              /* jMethod = "Classic" (else "Stokes")            */
     int inertia;               /* the velocity equation (rungeKutta.cu:195-212)  */
     R nu;                      /* velocity damping                               */
+    int jxbAver;               /* neighbour-averaged Lorentz force               */
+    R jxbAverWeight;
 } P;
 
 typedef struct orc_state {
@@ -108,6 +110,8 @@ static void to_P(const gm_params* g, P* p) {
     p->jClassic = strncmp(g->jMethod, "Classic ", 8) == 0;
     p->inertia = g->inertia != 0;
     p->nu = (R)g->nu;
+    p->jxbAver = g->jxbAver != 0;
+    p->jxbAverWeight = (R)g->jxbAverWeight;
 }
 
 /* ghosted (i, j, k in 0..n+1) and inner (0..n-1) linear point indices */
@@ -800,6 +804,37 @@ static void grad_p(orc_state* s) {
     }
 }
 
+/* jxbAver, src/rungeKutta.cu:357-443: J x B at the six face neighbours
+ * (zero beyond the inner range), each scaled by jxbAverWeight / 6.  J is the
+ * current stage's inner J, B the ghosted B of the stage; the +z neighbour's B
+ * is read with the reference's plane stride (nx+1)(ny+1) (rungeKutta.cu:428),
+ * which lands on another point of the array. */
+static void jxb_aver(const orc_state* s, int i, int j, int k, R jxb[6][3]) {
+    const P* p = &s->p;
+    const size_t nx = (size_t)p->nx, ny = (size_t)p->ny;
+    const R w6 = p->jxbAverWeight / 6;
+    int m, l;
+    for (m = 0; m < 6; m++) {
+        const R* J = NULL;
+        const R* B = NULL;
+        switch (m) {
+            case 0: if (i > 0) { J = &s->J[3 * II(p, i - 1, j, k)]; B = &s->B[3 * GI(p, i, j + 1, k + 1)]; } break;
+            case 1: if (i < p->nx - 1) { J = &s->J[3 * II(p, i + 1, j, k)]; B = &s->B[3 * GI(p, i + 2, j + 1, k + 1)]; } break;
+            case 2: if (j > 0) { J = &s->J[3 * II(p, i, j - 1, k)]; B = &s->B[3 * GI(p, i + 1, j, k + 1)]; } break;
+            case 3: if (j < p->ny - 1) { J = &s->J[3 * II(p, i, j + 1, k)]; B = &s->B[3 * GI(p, i + 1, j + 2, k + 1)]; } break;
+            case 4: if (k > 0) { J = &s->J[3 * II(p, i, j, k - 1)]; B = &s->B[3 * GI(p, i + 1, j + 1, k)]; } break;
+            default:
+                if (k < p->nz - 1) {
+                    J = &s->J[3 * II(p, i, j, k + 1)];
+                    B = &s->B[3 * ((size_t)(i + 1) + (nx + 2) * (size_t)(j + 1) + (size_t)(k + 2) * (nx + 1) * (ny + 1))];
+                }
+        }
+        if (J) cross3(J, B, jxb[m]);
+        else jxb[m][0] = jxb[m][1] = jxb[m][2] = 0;
+        for (l = 0; l < 3; l++) jxb[m][l] *= w6;
+    }
+}
+
 /* epsilon profile, src/rungeKutta.cu:180-185 (evaluated in double) */
 static R eps_profile(const P* p, int i, int j, int k) {
     if (!p->epsilonProf) return 1;
@@ -826,6 +861,15 @@ static void kk_stage(orc_state* s, int n, R dt) {
                 R kn[6], xs[3], epsilon;
                 if (!p->inertia) {
                     cross3(&s->J[3 * q], &s->B[3 * g], kn);
+                    if (p->jxbAver) {
+                        /* rungeKutta.cu:172-178 */
+                        R jxb[6][3];
+                        jxb_aver(s, i, j, k, jxb);
+                        for (l = 0; l < 3; l++) {
+                            kn[l] *= (1 - p->jxbAverWeight);
+                            for (m = 0; m < 6; m++) kn[l] += jxb[m][l];
+                        }
+                    }
                     epsilon = eps_profile(p, i, j, k);
                     for (l = 0; l < 3; l++) {
                         kn[l] *= dt * epsilon;

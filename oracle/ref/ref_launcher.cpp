@@ -407,7 +407,6 @@ void ref_close(void) {
 int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* xb, double t, double dt) {
     if (!load_driver()) return -3;
     ref_close();
-    if (g->jxbAver) { g_err = "jxbAver runs are not driven by this launcher"; return -1; }
     S.classic = strncmp(g->jMethod, "Classic ", 8) == 0;
     if (strncmp(g->jMethod, "Stokes ", 7) != 0 && !S.classic) { g_err = "only jMethod = Stokes or Classic"; return -1; }
     S.prec = g->precision;

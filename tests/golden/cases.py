@@ -22,6 +22,8 @@ reference's boundary handling:
   options together: the pressure force in the velocity equation, the
   pressure gradient beside the Classic current (both read Delta), and the
   Classic current driving the velocity equation.
+* jxbaver_f64 -- the neighbour-averaged Lorentz force (jxbAver = T,
+  src/rungeKutta.cu:172-178, 357-443), weight 0.3.
 """
 from __future__ import annotations
 
@@ -79,6 +81,11 @@ def make(name: str):
             p.inertia = 1
             p.nu = 1.0
         return configs.derive(p)
+    if name == "jxbaver_f64":
+        p = _braid((17, 17, 18), 64)
+        p.jxbAver = 1
+        p.jxbAverWeight = 0.3
+        return configs.derive(p)
     if name == "analytic_f64":
         p = configs.defaults(64)
         p.nx, p.ny, p.nz = 16, 16, 16
@@ -98,5 +105,5 @@ def make(name: str):
 
 NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64", "classic_tied_f64",
          "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64", "classic_press_tied_f64",
-         "classic_inertia_tied_f64"]
+         "classic_inertia_tied_f64", "jxbaver_f64"]
 N_ACCEPTED = 10
