@@ -171,7 +171,9 @@ SIGNATURES = {
                              P(C.c_float), P(C.c_float), C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
                              C.c_float, VP, C.c_int, C.c_int, VP, C.c_int, C.c_int, P(C.c_float), VP]),
     "gm_nn_input": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, VP, C.c_int, C.c_int, C.c_int, VP]),
-    "gm_nn_warm_grid": (C.c_int, [VP, C.c_int, P(GmParams), C.c_int, VP, VP, VP, VP]),
+    "gm_nn_disp_accumulate": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                                         C.c_int, VP, VP]),
+    "gm_nn_warm_grid": (C.c_int, [VP, P(GmParams), C.c_int, VP, VP, VP, VP]),
     "gm_nn_zero": (C.c_int, [VP, C.c_size_t, VP]),
     "gm_device_count": (C.c_int, [P(C.c_int)]),
     "gm_set_device": (C.c_int, [C.c_int]),

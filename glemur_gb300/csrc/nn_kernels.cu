@@ -501,11 +501,24 @@ __global__ void k_input(const T* __restrict__ B0, int nx, int ny, int nz, __nv_b
 
 // ---- the warm-start grid: displacement -> smoothed -> positions ------------
 
-// Displacement channels 0..2 of the network output (BF16, [V][ld]) to float.
-__global__ void k_wg_load(const __nv_bfloat16* __restrict__ y, int ld, long long V, float* __restrict__ d) {
-    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+// Displacement channels 0..2 of a network output (BF16, [V][ld]) computed on
+// the input translated by (sx, sy) (gm_nn_input), moved back to the grid's
+// own cells and weighted: d(i, j, k) = w y((i - sx) mod nx, (j - sy) mod ny, k),
+// added to d unless `first`.
+__global__ void k_wg_acc(const __nv_bfloat16* __restrict__ y, int ld, int nx, int ny, int nz, int sx, int sy, float w,
+                         int first, float* __restrict__ d) {
+    const long long V = (long long)nx * ny * nz;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(v % nx), j = (int)((v / nx) % ny);
+        const long long k = v / ((long long)nx * ny);
+        const int is = (i - sx + nx) % nx, js = (j - sy + ny) % ny;
+        const long long u = is + (long long)nx * (js + (long long)ny * k);
 #pragma unroll
-        for (int c = 0; c < 3; c++) d[3 * v + c] = __bfloat162float(y[v * ld + c]);
+        for (int c = 0; c < 3; c++) {
+            const float val = w * __bfloat162float(y[u * ld + c]);
+            d[3 * v + c] = first ? val : d[3 * v + c] + val;
+        }
+    }
 }
 
 // One 3x3x3 box-filter pass, periodic in x / y as selected, zero beyond the
@@ -695,16 +708,27 @@ int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, 
     return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_input");
 }
 
-int gm_nn_warm_grid(const void* y, int ldy, const gm_params* p, int passes, const void* xid, float* scratch,
-                    void* xb, void* stream) {
-    if (!y || !p || !xid || !scratch || !xb || passes < 0 || ldy < 3)
+int gm_nn_disp_accumulate(const void* y, int ldy, int nx, int ny, int nz, int sx, int sy, float w, int first,
+                          float* d, void* stream) {
+    if (!y || !d || ldy < 3 || sx < 0 || sx >= nx || sy < 0 || sy >= ny)
+        return gm::fail(GM_EPARAM, "gm_nn_disp_accumulate: bad argument");
+    const long long V = (long long)nx * ny * nz;
+    gmnn::k_wg_acc<<<gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)y, ldy, nx, ny, nz, sx, sy, w,
+                                                                   first, d);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "gm_nn_disp_accumulate");
+}
+
+int gm_nn_warm_grid(const float* d, const gm_params* p, int passes, const void* xid, float* scratch, void* xb,
+                    void* stream) {
+    if (!d || !p || !xid || !scratch || !xb || passes < 0)
         return gm::fail(GM_EPARAM, "gm_nn_warm_grid: bad argument");
     const int nx = p->nx, ny = p->ny, nz = p->nz;
     const long long V = (long long)nx * ny * nz, G = (long long)(nx + 2) * (ny + 2) * (nz + 2);
     cudaStream_t s = (cudaStream_t)stream;
     float* a = scratch;
     float* b = scratch + 3 * V;
-    gmnn::k_wg_load<<<gmnn::nb(V), 256, 0, s>>>((const __nv_bfloat16*)y, ldy, V, a);
+    if (cudaMemcpyAsync(a, d, 3 * V * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return gm::fail(GM_ECUDA, "gm_nn_warm_grid: copy of the displacement failed");
     for (int q = 0; q < passes; q++) {
         gmnn::k_wg_box<<<gmnn::nb(V), 256, 0, s>>>(a, b, nx, ny, nz, p->xPeri, p->yPeri);
         float* t = a; a = b; b = t;

@@ -159,10 +159,18 @@ def warm_grid(net, p, B0, smooth=2):
     return xb.astype(np.float32)
 
 
+# input translations for test-time averaging: not multiples of 4 (the two 2x
+# poolings make the network equivariant to those, so they would repeat the
+# same prediction)
+TTA_SHIFTS = ((0, 0), (2, 2), (1, 3), (3, 1), (2, 0), (0, 2), (1, 1), (3, 3))
+
+
 class DeviceWarmGrid:
-    """The warm grid built on the device (gm_nn_warm_grid): the network's
-    displacement smoothed and added to the identity grid, periodic ghosts
-    set, without a host round trip; the same grid as warm_grid up to the
+    """The warm grid built on the device: the network's displacement
+    (optionally averaged over input translations, gm_nn_disp_accumulate),
+    smoothed and added to the identity grid with periodic ghosts set
+    (gm_nn_warm_grid), without a host round trip; with one translation and
+    the same smoothing it is the grid warm_grid builds on the host, up to the
     float rounding of the smoothing."""
 
     def __init__(self, p, xid):
@@ -172,17 +180,25 @@ class DeviceWarmGrid:
         self.lib = _abi.load()
         self.xid = torch.from_numpy(np.ascontiguousarray(xid)).cuda()
         self.xb = torch.empty_like(self.xid)
-        self.scratch = torch.empty(6 * p.nx * p.ny * p.nz, dtype=torch.float32, device="cuda")
+        V = p.nx * p.ny * p.nz
+        self.d = torch.empty(3 * V, dtype=torch.float32, device="cuda")
+        self.scratch = torch.empty(6 * V, dtype=torch.float32, device="cuda")
 
-    def build(self, net, B0_dev, smooth=2):
+    def build(self, net, B0_dev, smooth=2, tta=1):
         import torch
         from . import _abi
-        net.set_input_b0(B0_dev, self.p.precision)
-        y = net.forward()
-        stream = torch.cuda.current_stream().cuda_stream
-        _abi.check(self.lib.gm_nn_warm_grid(_abi.VP(y.data_ptr()), y.stride(0), self.p, smooth,
-                                            _abi.VP(self.xid.data_ptr()), _abi.VP(self.scratch.data_ptr()),
-                                            _abi.VP(self.xb.data_ptr()), _abi.VP(stream)), "gm_nn_warm_grid")
+        p = self.p
+        stream = _abi.VP(torch.cuda.current_stream().cuda_stream)
+        shifts = TTA_SHIFTS[:max(1, tta)]
+        for q, sh in enumerate(shifts):
+            net.set_input_b0(B0_dev, p.precision, sh)
+            y = net.forward()
+            _abi.check(self.lib.gm_nn_disp_accumulate(_abi.VP(y.data_ptr()), y.stride(0), p.nx, p.ny, p.nz, sh[0], sh[1],
+                                                      1.0 / len(shifts), 1 if q == 0 else 0,
+                                                      _abi.VP(self.d.data_ptr()), stream), "gm_nn_disp_accumulate")
+        _abi.check(self.lib.gm_nn_warm_grid(_abi.VP(self.d.data_ptr()), p, smooth, _abi.VP(self.xid.data_ptr()),
+                                            _abi.VP(self.scratch.data_ptr()), _abi.VP(self.xb.data_ptr()), stream),
+                   "gm_nn_warm_grid")
         return self.xb
 
 
@@ -210,7 +226,7 @@ def time_to_residual(g, p, xb, B0, residual, max_attempts, check_every=50):
     return time.perf_counter() - t0, att, r0, mind, reached
 
 
-def evaluate(net, seeds, residual, max_attempts, log=print, smooth=2):
+def evaluate(net, seeds, residual, max_attempts, log=print, smooth=2, tta=1):
     import torch
     rows = []
     for s in seeds:
@@ -228,7 +244,7 @@ def evaluate(net, seeds, residual, max_attempts, log=print, smooth=2):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         B0_dev = torch.from_numpy(B0).cuda()
-        xw_dev = wg.build(net, B0_dev, smooth)
+        xw_dev = wg.build(net, B0_dev, smooth, tta)
         torch.cuda.synchronize()
         g.upload_ptr(xw_dev.data_ptr(), B0_dev.data_ptr())
         accepted = g.refresh()["minDetJac"] > 0
@@ -356,6 +372,7 @@ def main(argv=None):
     ap.add_argument("--shape", default="64,64,128", help="grid (nx,ny,nz), each divisible by 4")
     ap.add_argument("--large", action="store_true", help="also evaluate the 256x256x512 pressure case")
     ap.add_argument("--smooth", default="2", help="comma-separated box-filter passes to evaluate")
+    ap.add_argument("--tta", default="1", help="comma-separated numbers of input translations to average")
     a = ap.parse_args(argv)
     global SHAPE
     SHAPE = tuple(int(v) for v in a.shape.split(","))
@@ -376,13 +393,15 @@ def main(argv=None):
                       loss_last=hist[-1][2] if hist else None)
         if a.out:
             save_weights(net.state_dict(), a.out)
-    variants = [int(v) for v in a.smooth.split(",")]
-    for sm in variants:
-        rows = evaluate(net, [EVAL_SEED0 + i for i in range(a.eval)], a.residual, a.max_cycles, log, smooth=sm)
-        report[f"smooth{sm}"] = dict(summary=summarize(rows), rows=rows)
-        log(f"smooth {sm}: " + json.dumps(report[f"smooth{sm}"]["summary"]))
-    best = min(variants, key=lambda v: -(report[f"smooth{v}"]["summary"]["speedup_total"] or 0))
-    report.update(best_smooth=best, summary=report[f"smooth{best}"]["summary"])
+    variants = [(int(s), int(q)) for s in a.smooth.split(",") for q in a.tta.split(",")]
+    key = lambda v: f"smooth{v[0]}" + (f"_tta{v[1]}" if v[1] > 1 else "")
+    for sm, tt in variants:
+        rows = evaluate(net, [EVAL_SEED0 + i for i in range(a.eval)], a.residual, a.max_cycles, log, smooth=sm,
+                        tta=tt)
+        report[key((sm, tt))] = dict(summary=summarize(rows), rows=rows)
+        log(f"{key((sm, tt))}: " + json.dumps(report[key((sm, tt))]["summary"]))
+    best = min(variants, key=lambda v: -(report[key(v)]["summary"]["speedup_total"] or 0))
+    report.update(best_variant=key(best), summary=report[key(best)]["summary"])
     if a.large:
         report["large"] = evaluate_large(net.state_dict(), a.residual, 4 * a.max_cycles, log=log)
     log(json.dumps(report["summary"]))

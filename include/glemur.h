@@ -436,16 +436,23 @@ int gm_nn_adam(float* W, float* mW, float* vW, const float* gW, float* b, float*
  * 0 <= sy < ny): a whole-cell translation for data augmentation. */
 int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, int sx, int sy,
                 void* stream);
-/* Warm-start grid on the device: the displacement (channels 0..2 of the
- * network output y, BF16 [V][ldy], in grid spacings) smoothed by `passes`
- * 3x3x3 box filters (periodic x / y as p selects, zero beyond z), added to the
- * identity grid xid (device, reference layout, REAL of p->precision) at the
- * inner points except the first and last z-planes, with periodic x / y ghosts
- * as images of the opposite inner points shifted by -/+ (L + d); written to
- * xb (device, same layout).  scratch: device floats, 6 nx ny nz.  No
- * counterpart in the reference (its runs start from the identity grid). */
-int gm_nn_warm_grid(const void* y, int ldy, const gm_params* p, int passes, const void* xid, float* scratch,
-                    void* xb, void* stream);
+/* Test-time translation averaging of the warm-start network: the displacement
+ * channels 0..2 of an output y (BF16 [V][ldy], in grid spacings) computed on
+ * the input translated by (sx, sy) (gm_nn_input), moved back to the grid's
+ * own cells, times w, written to d (float [V][3], device) when `first`, else
+ * added.  No counterpart in the reference. */
+int gm_nn_disp_accumulate(const void* y, int ldy, int nx, int ny, int nz, int sx, int sy, float w, int first,
+                          float* d, void* stream);
+/* Warm-start grid on the device: the displacement d (float [V][3], grid
+ * spacings) smoothed by `passes` 3x3x3 box filters (periodic x / y as p
+ * selects, zero beyond z), added to the identity grid xid (device, reference
+ * layout, REAL of p->precision) at the inner points except the first and last
+ * z-planes, with periodic x / y ghosts as images of the opposite inner points
+ * shifted by -/+ (L + d); written to xb (device, same layout).  scratch:
+ * device floats, 6 nx ny nz.  No counterpart in the reference (its runs start
+ * from the identity grid). */
+int gm_nn_warm_grid(const float* d, const gm_params* p, int passes, const void* xid, float* scratch, void* xb,
+                    void* stream);
 /* Zero `bytes` bytes of device memory (cudaMemsetAsync). */
 int gm_nn_zero(void* p, size_t bytes, void* stream);
 
