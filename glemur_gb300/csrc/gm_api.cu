@@ -58,8 +58,9 @@ int check_params(const gm_params* p) {
     if (p->precision != 32 && p->precision != 64) return gm::fail(GM_EPARAM, "precision must be 32 or 64");
     if (p->nx < 3 || p->ny < 3 || p->nz < 3) return gm::fail(GM_EPARAM, "nx, ny, nz must be >= 3");
     if ((long long)p->nx * p->ny * p->nz > (1ll << 31)) return gm::fail(GM_EPARAM, "grid too large");
-    if (strncmp(p->jMethod, "Stokes ", 7) != 0 && strncmp(p->jMethod, "Classic ", 8) != 0)
-        return gm::fail(GM_EPARAM, "jMethod: the Stokes and Classic currents are implemented");
+    if (strncmp(p->jMethod, "Stokes ", 7) != 0 && strncmp(p->jMethod, "Classic ", 8) != 0 &&
+        strncmp(p->jMethod, "Stokes4th ", 10) != 0)
+        return gm::fail(GM_EPARAM, "jMethod: the Stokes, Stokes4th and Classic currents are implemented");
     if (p->pressure && strncmp(p->pMethod, "Classic ", 8) != 0) return gm::fail(GM_EPARAM, "pMethod must be Classic");
     if (p->initShearA != 0 || p->initShearB != 0)
         return gm::fail(GM_EPARAM, "initial-distortion ghost corrections (initShearA/B != 0) are not implemented");
@@ -185,6 +186,7 @@ struct Impl : ImplBase {
         kp.errMode = p->errMode;
         kp.refDt = p->errMode == 0;
         kp.jClassic = strncmp(p->jMethod, "Classic ", 8) == 0;
+        kp.jOct = strncmp(p->jMethod, "Stokes4th ", 10) == 0;
         kp.inertia = p->inertia != 0;
         kp.nu = (T)p->nu;
         kp.jxbAver = p->jxbAver != 0 && !p->inertia;   // the reference applies it in the frictional branch only
@@ -299,9 +301,9 @@ struct Impl : ImplBase {
         smem_diag = gmk::stage_smem_bytes<T>(TY, gmk::MODE_DIAG, p->pressure);
         nparts = (int)(grid.x * grid.y * grid.z);
         // the TMA kernel computes the Stokes current of the frictional
-        // equation only; the Classic current, the inertial equation and the
+        // equation only; the other currents, the inertial equation and the
         // averaged Lorentz force run in the generic kernel
-        use_tma = p->stageKernel == 0 && strncmp(p->jMethod, "Classic ", 8) != 0 && !p->inertia && !p->jxbAver;
+        use_tma = p->stageKernel == 0 && strncmp(p->jMethod, "Stokes ", 7) == 0 && !p->inertia && !p->jxbAver;
         if (use_tma) {
             if ((rc = init_tma(nsm))) return rc;
         }
@@ -444,15 +446,20 @@ struct Impl : ImplBase {
             A.a.TZ = TZ2;
             CUDA_TRY(gmk::launch_stage_tma<T>(A, gp.pressure, grid2, stream));
         } else {
-            if (kp.jxbAver) {
+            if (kp.jxbAver || kp.jOct) {
                 // the averaged Lorentz force reads J and B of this stage at every
-                // point's neighbours (current() before kk(), main.cu:272-281):
-                // a J pass exports them first
+                // point's neighbours, and the octilateral current B at the edge
+                // neighbours with the reference's ghost values (current() before
+                // kk(), main.cu:272-281): a J pass exports B (and J) first
                 StageArgs<T> aj = args(n);
                 aj.jpass = 1;
                 CUDA_TRY(gmk::launch_stage<T>(aj, gmk::MODE_DIAG, gp.pressure, grid, block, smem_diag, stream));
                 CUDA_TRY(gmk::launch_export_ghosts<T>(kp, outB, outD, stream));
                 launches += 1 + kp.xPeri + kp.yPeri + kp.zPeri;
+                if (kp.jOct) {
+                    CUDA_TRY(gmk::launch_j_oct<T>(args(n), stream));
+                    launches++;
+                }
             }
             StageArgs<T> a = args(n);
             CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_STAGE, gp.pressure, grid, block, smem_stage, stream));
@@ -710,6 +717,16 @@ struct Impl : ImplBase {
         int rc = read_state();
         if (rc) return rc;
         StageArgs<T> a = args(0);
+        if (kp.jOct) {
+            // the octilateral current needs the exported B with its ghosts
+            // first; the diagnostic pass then reads J from it
+            StageArgs<T> aj = args(0);
+            aj.jpass = 1;
+            CUDA_TRY(gmk::launch_stage<T>(aj, gmk::MODE_DIAG, gp.pressure, grid, block, smem_diag, stream));
+            CUDA_TRY(gmk::launch_export_ghosts<T>(kp, outB, outD, stream));
+            CUDA_TRY(gmk::launch_j_oct<T>(aj, stream));
+            launches += 2 + kp.xPeri + kp.yPeri + kp.zPeri;
+        }
         CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_DIAG, gp.pressure, grid, block, smem_diag, stream));
         CUDA_TRY(gmk::launch_finalize<T>(part, nparts, red, stream));
         CUDA_TRY(gmk::launch_export_ghosts<T>(kp, outB, outD, stream));

@@ -67,6 +67,7 @@ struct KP {
     T Lx, Ly, Lz, Ox, Oy, Oz;
     int xPeri, yPeri, zPeri, zUpdate, errMode, refDt;
     int jClassic;            // jMethod = "Classic": the finite-difference current (generic kernel only)
+    int jOct;                // jMethod = "Stokes4th": J from the octilateral pass (outJ; generic kernel only)
     int inertia;             // the velocity equation (generic kernel only)
     T nu;                    // velocity damping
     int jxbAver;             // neighbour-averaged Lorentz force (generic kernel only)
@@ -123,6 +124,8 @@ struct StageArgs {
 };
 
 // Host-side launchers (explicitly instantiated for float and double).
+template <typename T>
+cudaError_t launch_j_oct(const StageArgs<T>& a, cudaStream_t s);
 template <typename T>
 cudaError_t launch_stage(const StageArgs<T>& a, int mode, int pressure, dim3 grid, dim3 block, size_t smem,
                          cudaStream_t s);

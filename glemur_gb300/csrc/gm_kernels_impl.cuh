@@ -469,7 +469,11 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                 T Bc[3], Jv[3];
 #pragma unroll
                 for (int l = 0; l < 3; l++) Bc[l] = t.b(kc, l, j, i);
-                if (p.jClassic) {
+                if (p.jOct && !a.jpass) {
+                    // the octilateral current, computed by k_j_oct after the J pass
+                    const long long lj = (long long)i + (long long)p.nx * ((long long)j + (long long)p.ny * kc);
+                    Jv[0] = a.outJ[3 * lj]; Jv[1] = a.outJ[3 * lj + 1]; Jv[2] = a.outJ[3 * lj + 2];
+                } else if (p.jClassic) {
                     j_classic<T>(p, t, a.B0, i, j, kc, Jv);
                 } else {
                     T xn[6][3], bn[6][3];
@@ -947,6 +951,98 @@ __global__ void k_pack_k(const KP<T> p, const T* __restrict__ k, T* __restrict__
     }
 }
 
+// Octilateral Stokes current (JStokes4th, src/current.cu:413-736) at every
+// inner point, from the positions (padded SoA) and the ghosted B of the
+// reference layout (as the J pass exports it, ghost edges included).  For
+// each plane through the point, axes (u, v) = (x, y), (y, z), (z, x): the
+// circulation of B around the eight neighbours (-1,-1) (0,-1) (1,-1) (1,0)
+// (1,1) (0,1) (-1,1) (-1,0) and the area vector (1/2) of the corner cross
+// products plus (1/4) of the inner diamond's; then the 3x3 solve.
+template <typename T>
+__global__ void k_j_oct(const __grid_constant__ StageArgs<T> a) {
+    const KP<T>& p = a.p;
+    // the stage's input grid (the step start for stage 0, chosen on the device)
+    const T* __restrict__ X = a.n == 0 ? a.X[a.st->cur] : a.XS[(a.n - 1) & 1];
+    const T* __restrict__ B = a.outB;
+    T* __restrict__ J = a.outJ;
+    const int ax[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+    const int ring[9][2] = {{0, 0}, {1, 0}, {2, 0}, {2, 1}, {2, 2}, {1, 2}, {0, 2}, {0, 1}, {0, 0}};
+    const int dia[5][2] = {{0, 1}, {1, 0}, {2, 1}, {1, 2}, {0, 1}};
+    const long long nx2 = p.nx + 2, ny2 = p.ny + 2;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < p.N; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % p.nx), j = (int)((q / p.nx) % p.ny), k = (int)(q / ((long long)p.nx * p.ny));
+        auto xat = [&](const int o[3], int l) { return X[l * p.cs + gidx(p.px, p.py, i + o[0], j + o[1], k + o[2])]; };
+        auto bat = [&](const int o[3], int l) {
+            return B[3 * ((i + 1 + o[0]) + nx2 * ((j + 1 + o[1]) + ny2 * (long long)(k + 1 + o[2]))) + l];
+        };
+        T NA[3][3], II[3];
+#pragma unroll
+        for (int pl = 0; pl < 3; pl++) {
+            T xr[9][3], br[9][3], dx[8][3], dd[4][3], c[4][3];
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+                int o[3] = {0, 0, 0};
+                o[ax[pl][0]] = ring[e][0] - 1;
+                o[ax[pl][1]] = ring[e][1] - 1;
+#pragma unroll
+                for (int l = 0; l < 3; l++) { xr[e][l] = xat(o, l); br[e][l] = bat(o, l); }
+            }
+#pragma unroll
+            for (int l = 0; l < 3; l++) { xr[8][l] = xr[0][l]; br[8][l] = br[0][l]; }
+            T I = 0;
+#pragma unroll
+            for (int l = 0; l < 3; l++) {
+#pragma unroll
+                for (int e = 0; e < 8; e++) dx[e][l] = xr[e + 1][l] - xr[e][l];
+                I += (br[1][l] + br[0][l]) / 2 * dx[0][l] + (br[2][l] + br[1][l]) / 2 * dx[1][l] +
+                     (br[3][l] + br[2][l]) / 2 * dx[2][l] + (br[4][l] + br[3][l]) / 2 * dx[3][l] +
+                     (br[5][l] + br[4][l]) / 2 * dx[4][l] + (br[6][l] + br[5][l]) / 2 * dx[5][l] +
+                     (br[7][l] + br[6][l]) / 2 * dx[6][l] + (br[8][l] + br[7][l]) / 2 * dx[7][l];
+            }
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                int o0[3] = {0, 0, 0}, o1[3] = {0, 0, 0};
+                o0[ax[pl][0]] = dia[e][0] - 1; o0[ax[pl][1]] = dia[e][1] - 1;
+                o1[ax[pl][0]] = dia[e + 1][0] - 1; o1[ax[pl][1]] = dia[e + 1][1] - 1;
+#pragma unroll
+                for (int l = 0; l < 3; l++) dd[e][l] = xat(o1, l) - xat(o0, l);
+            }
+            II[pl] = I;
+            cross3(dx[1], dx[2], c[0]);
+            cross3(dx[3], dx[4], c[1]);
+            cross3(dx[5], dx[6], c[2]);
+            cross3(dx[7], dx[0], c[3]);
+#pragma unroll
+            for (int l = 0; l < 3; l++) NA[pl][l] = (c[0][l] + c[1][l] + c[2][l] + c[3][l]) / 2;
+            cross3(dd[0], dd[1], c[0]);
+            cross3(dd[1], dd[2], c[1]);
+            cross3(dd[2], dd[3], c[2]);
+            cross3(dd[3], dd[0], c[3]);
+#pragma unroll
+            for (int l = 0; l < 3; l++) NA[pl][l] += (c[0][l] + c[1][l] + c[2][l] + c[3][l]) / 4;
+        }
+        const T det = NA[0][0] * NA[1][1] * NA[2][2] + NA[0][1] * NA[1][2] * NA[2][0] + NA[0][2] * NA[1][0] * NA[2][1] -
+                      NA[0][0] * NA[1][2] * NA[2][1] - NA[0][1] * NA[1][0] * NA[2][2] - NA[0][2] * NA[1][1] * NA[2][0];
+        T N1[3][3];
+        N1[0][0] = (NA[1][1] * NA[2][2] - NA[1][2] * NA[2][1]) / det;
+        N1[0][1] = (NA[0][2] * NA[2][1] - NA[0][1] * NA[2][2]) / det;
+        N1[0][2] = (NA[0][1] * NA[1][2] - NA[0][2] * NA[1][1]) / det;
+        N1[1][0] = (NA[1][2] * NA[2][0] - NA[1][0] * NA[2][2]) / det;
+        N1[1][1] = (NA[0][0] * NA[2][2] - NA[0][2] * NA[2][0]) / det;
+        N1[1][2] = (NA[0][2] * NA[1][0] - NA[0][0] * NA[1][2]) / det;
+        N1[2][0] = (NA[1][0] * NA[2][1] - NA[1][1] * NA[2][0]) / det;
+        N1[2][1] = (NA[0][1] * NA[2][0] - NA[0][0] * NA[2][1]) / det;
+        N1[2][2] = (NA[0][0] * NA[1][1] - NA[0][1] * NA[1][0]) / det;
+#pragma unroll
+        for (int l = 0; l < 3; l++) {
+            T Jl = 0;
+#pragma unroll
+            for (int m = 0; m < 3; m++) Jl += N1[l][m] * II[m];
+            J[3 * q + l] = Jl;
+        }
+    }
+}
+
 // Two k-layout arrays (x and velocity increments) into the reference's
 // six-value kk record per inner point.
 template <typename T>
@@ -1194,6 +1290,12 @@ cudaError_t launch_pack_k(const KP<T>& p, const T* k, T* aos, cudaStream_t s) {
 }
 
 template <typename T>
+cudaError_t launch_j_oct(const StageArgs<T>& a, cudaStream_t s) {
+    k_j_oct<T><<<nblk(a.p.N), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_pack_k6(const KP<T>& p, const T* kx, const T* ku, T* aos, cudaStream_t s) {
     k_pack_k6<T><<<nblk(p.N), 256, 0, s>>>(p, kx, ku, aos);
     return cudaGetLastError();
@@ -1241,6 +1343,7 @@ cudaError_t launch_eps_star(const KP<T>& p, const T* B, const T* J, const T* X, 
     template cudaError_t launch_scale_b0<T>(const KP<T>&, const T*, T*, cudaStream_t);                            \
     template cudaError_t launch_pack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \
     template cudaError_t launch_pack_k6<T>(const KP<T>&, const T*, const T*, T*, cudaStream_t);                  \
+    template cudaError_t launch_j_oct<T>(const StageArgs<T>&, cudaStream_t);                                    \
     template cudaError_t launch_unpack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                          \
     template cudaError_t launch_export_ghosts<T>(const KP<T>&, T*, T*, cudaStream_t);                            \
     template cudaError_t launch_grid_fields<T>(const KP<T>&, const T*, T*, T*, T*, cudaStream_t);                 \

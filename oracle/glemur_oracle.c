@@ -62,6 +62,7 @@ typedef struct {
     int errMode;
     R p0Amp, p0Width;
     int jClassic;              /* jMethod = "Classic" (else "Stokes")            */
+    int jOct;                  /* jMethod = "Stokes4th": octilateral contours    */
     int inertia;               /* the velocity equation (rungeKutta.cu:195-212)  */
     R nu;                      /* velocity damping                               */
     int jxbAver;               /* neighbour-averaged Lorentz force               */
@@ -108,6 +109,7 @@ static void to_P(const gm_params* g, P* p) {
     p->errMode = g->errMode;
     p->p0Amp = (R)g->p0Amp; p->p0Width = (R)g->p0Width;
     p->jClassic = strncmp(g->jMethod, "Classic ", 8) == 0;
+    p->jOct = strncmp(g->jMethod, "Stokes4th ", 10) == 0;
     p->inertia = g->inertia != 0;
     p->nu = (R)g->nu;
     p->jxbAver = g->jxbAver != 0;
@@ -655,6 +657,95 @@ static void j_stokes(orc_state* s) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Octilateral Stokes current, JStokes4th src/current.cu:413-736            */
+/* ------------------------------------------------------------------------ */
+
+/* For each of the three planes through the point (axes (u, v) = (x, y),
+ * (y, z), (z, x)), the contour through the eight neighbours P(a, b),
+ * a, b in {-1, 0, 1} along u and v, in the order (-1,-1) (0,-1) (1,-1) (1,0)
+ * (1,1) (0,1) (-1,1) (-1,0): the circulation sum (B_end + B_start)/2 . dx over
+ * its eight edges, and the area vector (1/2) sum of the corner cross products
+ * dx2 x dx3 + dx4 x dx5 + dx6 x dx7 + dx8 x dx1 plus (1/4) that of the inner
+ * diamond through the face neighbours (current.cu:513-736); J solves the 3x3
+ * system as JStokes does, dividing by the determinant. */
+static void j_stokes4th(orc_state* s) {
+    const P* p = &s->p;
+    static const int ax[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+    static const int ring[9][2] = {{0, 0}, {1, 0}, {2, 0}, {2, 1}, {2, 2}, {1, 2}, {0, 2}, {0, 1}, {0, 0}};
+    static const int dia[5][2] = {{0, 1}, {1, 0}, {2, 1}, {1, 2}, {0, 1}};   /* dxA..dxD */
+    int k;
+#pragma omp parallel for schedule(static)
+    for (k = 0; k < p->nz; k++) {
+        int i, j, l, m, pl, e;
+        for (j = 0; j < p->ny; j++)
+            for (i = 0; i < p->nx; i++) {
+                R NA[3][3], NA1[3][3], II_[3], detNA;
+                for (pl = 0; pl < 3; pl++) {
+                    const R* X[9];
+                    const R* Bp[9];
+                    R dx[8][3], dd[4][3], I = 0, c[4][3];
+                    for (e = 0; e < 8; e++) {
+                        int o[3] = {0, 0, 0};
+                        o[ax[pl][0]] = ring[e][0] - 1;
+                        o[ax[pl][1]] = ring[e][1] - 1;
+                        {
+                            const size_t g = GI(p, i + 1 + o[0], j + 1 + o[1], k + 1 + o[2]);
+                            X[e] = &s->xb[3 * g];
+                            Bp[e] = &s->B[3 * g];
+                        }
+                    }
+                    X[8] = X[0]; Bp[8] = Bp[0];
+                    for (l = 0; l < 3; l++) {
+                        for (e = 0; e < 8; e++) dx[e][l] = X[e + 1][l] - X[e][l];
+                        I += (Bp[1][l] + Bp[0][l]) / 2 * dx[0][l] + (Bp[2][l] + Bp[1][l]) / 2 * dx[1][l] +
+                             (Bp[3][l] + Bp[2][l]) / 2 * dx[2][l] + (Bp[4][l] + Bp[3][l]) / 2 * dx[3][l] +
+                             (Bp[5][l] + Bp[4][l]) / 2 * dx[4][l] + (Bp[6][l] + Bp[5][l]) / 2 * dx[5][l] +
+                             (Bp[7][l] + Bp[6][l]) / 2 * dx[6][l] + (Bp[8][l] + Bp[7][l]) / 2 * dx[7][l];
+                    }
+                    /* the inner diamond: dxA..dxD between the face neighbours */
+                    for (e = 0; e < 4; e++) {
+                        int o0[3] = {0, 0, 0}, o1[3] = {0, 0, 0};
+                        o0[ax[pl][0]] = dia[e][0] - 1; o0[ax[pl][1]] = dia[e][1] - 1;
+                        o1[ax[pl][0]] = dia[e + 1][0] - 1; o1[ax[pl][1]] = dia[e + 1][1] - 1;
+                        {
+                            const R* a = &s->xb[3 * GI(p, i + 1 + o0[0], j + 1 + o0[1], k + 1 + o0[2])];
+                            const R* b = &s->xb[3 * GI(p, i + 1 + o1[0], j + 1 + o1[1], k + 1 + o1[2])];
+                            for (l = 0; l < 3; l++) dd[e][l] = b[l] - a[l];
+                        }
+                    }
+                    II_[pl] = I;
+                    cross3(dx[1], dx[2], c[0]);
+                    cross3(dx[3], dx[4], c[1]);
+                    cross3(dx[5], dx[6], c[2]);
+                    cross3(dx[7], dx[0], c[3]);
+                    for (l = 0; l < 3; l++) NA[pl][l] = (c[0][l] + c[1][l] + c[2][l] + c[3][l]) / 2;
+                    cross3(dd[0], dd[1], c[0]);
+                    cross3(dd[1], dd[2], c[1]);
+                    cross3(dd[2], dd[3], c[2]);
+                    cross3(dd[3], dd[0], c[3]);
+                    for (l = 0; l < 3; l++) NA[pl][l] += (c[0][l] + c[1][l] + c[2][l] + c[3][l]) / 4;
+                }
+                detNA = NA[0][0] * NA[1][1] * NA[2][2] + NA[0][1] * NA[1][2] * NA[2][0] + NA[0][2] * NA[1][0] * NA[2][1] -
+                        NA[0][0] * NA[1][2] * NA[2][1] - NA[0][1] * NA[1][0] * NA[2][2] - NA[0][2] * NA[1][1] * NA[2][0];
+                NA1[0][0] = (NA[1][1] * NA[2][2] - NA[1][2] * NA[2][1]) / detNA;
+                NA1[0][1] = (NA[0][2] * NA[2][1] - NA[0][1] * NA[2][2]) / detNA;
+                NA1[0][2] = (NA[0][1] * NA[1][2] - NA[0][2] * NA[1][1]) / detNA;
+                NA1[1][0] = (NA[1][2] * NA[2][0] - NA[1][0] * NA[2][2]) / detNA;
+                NA1[1][1] = (NA[0][0] * NA[2][2] - NA[0][2] * NA[2][0]) / detNA;
+                NA1[1][2] = (NA[0][2] * NA[1][0] - NA[0][0] * NA[1][2]) / detNA;
+                NA1[2][0] = (NA[1][0] * NA[2][1] - NA[1][1] * NA[2][0]) / detNA;
+                NA1[2][1] = (NA[0][1] * NA[2][0] - NA[0][0] * NA[2][1]) / detNA;
+                NA1[2][2] = (NA[0][0] * NA[1][1] - NA[0][1] * NA[1][0]) / detNA;
+                for (l = 0; l < 3; l++) {
+                    R Jl = 0;
+                    for (m = 0; m < 3; m++) Jl += NA1[l][m] * II_[m];
+                    s->J[3 * II(p, i, j, k) + l] = Jl;
+                }
+            }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Finite-difference current, JClassic src/current.cu:10-218                */
 /* ------------------------------------------------------------------------ */
 
@@ -965,6 +1056,7 @@ void orc_refresh_fields(orc_state* s) {
     b_jac_b0(s);
     set_b_bound(s);
     if (s->p.jClassic) j_classic(s);
+    else if (s->p.jOct) j_stokes4th(s);
     else j_stokes(s);
 }
 

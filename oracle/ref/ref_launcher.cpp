@@ -190,6 +190,7 @@ struct Ref {
     size_t NG = 0, N = 0;
     bool open = false;
     bool classic = false;   // jMethod = "Classic": JClassic instead of JStokes
+    bool oct = false;       // jMethod = "Stokes4th": JStokes4th (same shared memory as JStokes)
 };
 Ref S;
 
@@ -203,6 +204,7 @@ const char* kname(const char* base, int prec) {
     else if (b == "setPeriFace") s = "_Z11setPeriFaceP" + r + "i";
     else if (b == "JStokes") s = "_Z7JStokes7VarsDeviii";
     else if (b == "JClassic") s = "_Z8JClassic7VarsDeviii";
+    else if (b == "JStokes4th") s = "_Z10JStokes4th7VarsDeviii";
     else if (b == "gradPClassic") s = "_Z12gradPClassic7VarsDeviii";
     else if (b == "kk") s = "_Z2kk7VarsDeviiii" + r;
     else if (b == "setGridPeriFace") s = "_Z15setGridPeriFaceP" + r + "i";
@@ -408,7 +410,11 @@ int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* 
     if (!load_driver()) return -3;
     ref_close();
     S.classic = strncmp(g->jMethod, "Classic ", 8) == 0;
-    if (strncmp(g->jMethod, "Stokes ", 7) != 0 && !S.classic) { g_err = "only jMethod = Stokes or Classic"; return -1; }
+    S.oct = strncmp(g->jMethod, "Stokes4th ", 10) == 0;
+    if (strncmp(g->jMethod, "Stokes ", 7) != 0 && !S.classic && !S.oct) {
+        g_err = "only jMethod = Stokes, Stokes4th or Classic";
+        return -1;
+    }
     S.prec = g->precision;
     S.rs = S.prec == 64 ? 8 : 4;
     S.gp = *g;
@@ -420,7 +426,7 @@ int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* 
     CK(D.ModuleLoad(&S.mod, cubin));
     int rc = 0;
     if ((rc = get_fn(&S.fBJ, "B_JacB0")) || (rc = get_fn(&S.fBound, "updateBbound")) ||
-        (rc = get_fn(&S.fPeri, "setPeriFace")) || (rc = get_fn(&S.fJ, S.classic ? "JClassic" : "JStokes")) ||
+        (rc = get_fn(&S.fPeri, "setPeriFace")) || (rc = get_fn(&S.fJ, S.classic ? "JClassic" : (S.oct ? "JStokes4th" : "JStokes"))) ||
         (rc = get_fn(&S.fGradP, "gradPClassic")) || (rc = get_fn(&S.fKK, "kk")) ||
         (rc = get_fn(&S.fGridPeri, "setGridPeriFace")) || (rc = get_fn(&S.fXNS, "xNewStar")) ||
         (rc = get_fn(&S.fMaxBlock, "maxBlock")))

@@ -24,6 +24,10 @@ reference's boundary handling:
   Classic current driving the velocity equation.
 * jxbaver_f64 -- the neighbour-averaged Lorentz force (jxbAver = T,
   src/rungeKutta.cu:172-178, 357-443), weight 0.3.
+* oct_f64 / oct_tied_f64 / oct_f32 -- the octilateral Stokes current
+  (jMethod = "Stokes4th", src/current.cu:413-736), periodic x, y and every
+  face line-tied: it reads B at the in-plane edge neighbours, ghost edges
+  included.
 """
 from __future__ import annotations
 
@@ -86,6 +90,13 @@ def make(name: str):
         p.jxbAver = 1
         p.jxbAverWeight = 0.3
         return configs.derive(p)
+    if name in ("oct_f64", "oct_tied_f64", "oct_f32"):
+        if name == "oct_tied_f64":
+            p = _braid((17, 12, 17), 64, peri=(0, 0, 0))
+        else:
+            p = _braid((17, 17, 18), 32 if name.endswith("32") else 64)
+        p.set_str("jMethod", "Stokes4th")
+        return configs.derive(p)
     if name == "analytic_f64":
         p = configs.defaults(64)
         p.nx, p.ny, p.nz = 16, 16, 16
@@ -105,5 +116,5 @@ def make(name: str):
 
 NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64", "classic_tied_f64",
          "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64", "classic_press_tied_f64",
-         "classic_inertia_tied_f64", "jxbaver_f64"]
+         "classic_inertia_tied_f64", "jxbaver_f64", "oct_f64", "oct_tied_f64", "oct_f32"]
 N_ACCEPTED = 10

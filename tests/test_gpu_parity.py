@@ -69,7 +69,8 @@ def test_stages_match_oracle(name):
 
 @pytest.mark.parametrize("name", ["braid_f64", "braid_f32", "tied_f64", "press_f64", "classic_tied_f64",
                                   "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64",
-                                  "classic_press_tied_f64", "classic_inertia_tied_f64", "jxbaver_f64"])
+                                  "classic_press_tied_f64", "classic_inertia_tied_f64", "jxbaver_f64", "oct_f64",
+                                  "oct_tied_f64", "oct_f32"])
 def test_stages_match_reference_kernels(name):
     stage_by_stage(cases.make(name), RefLauncher)
 
