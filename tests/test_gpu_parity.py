@@ -102,7 +102,7 @@ def test_run_matches_oracle(name):
         # the truncation error rather than by rounding noise
         p.errMode = 1
         p.dt0 = 0.2
-    rt = RUN_TOL[p.precision]
+    rt = dict(RUN_TOL[p.precision])
     B0, xb = configs.init_state(p)
     g = Relaxation(p)
     g.upload(xb, B0)
@@ -111,6 +111,23 @@ def test_run_matches_oracle(name):
     sg = g.run(nacc)
     n, lg = o.run(nacc, log=True)
     so = o.scalars()
+    if p.precision == 64:
+        # some cases' step-size controllers amplify rounding strongly (the
+        # octilateral current on the all-line-tied grid: a 1e-13 change of
+        # dt0 moves t by 4e-5 after 25 steps, in the oracle itself): the run
+        # tolerances are at least 10x the spread that perturbation causes
+        o2 = Oracle(p, B0, xb, dt=p.dt0 * (1 + 1e-13))
+        o2.run(nacc)
+        o.refresh()
+        o2.refresh()
+        fa, fb = o.get(), o2.get()
+        spread = dict(t=abs(o2.scalars()["t"] - so["t"]) / abs(so["t"]),
+                      x=relerr(inner(fb["xb"]), inner(fa["xb"])), B=relerr(inner(fb["B"]), inner(fa["B"])),
+                      J=relerr(fb["J"], fa["J"]))
+        o2.close()
+        for k_, v in spread.items():
+            rt[k_] = max(rt[k_], 10 * v)
+        rt["red"] = max(rt["red"], 10 * spread["J"])
     assert sg["timeIndex"] == so["timeIndex"] == nacc
     if p.precision == 64:
         assert sg["nAttempted"] == so["nAttempted"], "accept/reject sequences differ"
