@@ -68,6 +68,7 @@ struct KP {
     int xPeri, yPeri, zPeri, zUpdate, errMode, refDt;
     int jClassic;            // jMethod = "Classic": the finite-difference current (generic kernel only)
     int jOct;                // jMethod = "Stokes4th": J from the octilateral pass (outJ; generic kernel only)
+    int jQuint;              // jMethod = "StokesQuint": J from the quintilateral pass (outJ; generic kernel only)
     int inertia;             // the velocity equation (generic kernel only)
     T nu;                    // velocity damping
     int jxbAver;             // neighbour-averaged Lorentz force (generic kernel only)
@@ -126,6 +127,8 @@ struct StageArgs {
 // Host-side launchers (explicitly instantiated for float and double).
 template <typename T>
 cudaError_t launch_j_oct(const StageArgs<T>& a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_j_quint(const StageArgs<T>& a, cudaStream_t s);
 template <typename T>
 cudaError_t launch_stage(const StageArgs<T>& a, int mode, int pressure, dim3 grid, dim3 block, size_t smem,
                          cudaStream_t s);

@@ -469,8 +469,8 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                 T Bc[3], Jv[3];
 #pragma unroll
                 for (int l = 0; l < 3; l++) Bc[l] = t.b(kc, l, j, i);
-                if (p.jOct && !a.jpass) {
-                    // the octilateral current, computed by k_j_oct after the J pass
+                if ((p.jOct || p.jQuint) && !a.jpass) {
+                    // the octilateral / quintilateral current, computed after the J pass
                     const long long lj = (long long)i + (long long)p.nx * ((long long)j + (long long)p.ny * kc);
                     Jv[0] = a.outJ[3 * lj]; Jv[1] = a.outJ[3 * lj + 1]; Jv[2] = a.outJ[3 * lj + 2];
                 } else if (p.jClassic) {
@@ -1043,6 +1043,142 @@ __global__ void k_j_oct(const __grid_constant__ StageArgs<T> a) {
     }
 }
 
+// Quintilateral Stokes current (JStokesQuint, src/current.cu:737-1199) at
+// every inner point, from the positions and the exported ghosted B, as
+// k_j_oct.  Per plane, axes (u, v, w) = (x, y, z), (y, z, x), (z, x, y) and
+// P(a, b) the neighbour at in-plane offsets (a - 1, b - 1): the diamond through
+// the face neighbours, with a corner triangle's two outer edges in place of one
+// diamond edge where the orientation tests pick one.  The tests are the
+// reference's as written: each later test reads the edge vectors the previous
+// one stored, the third compares with 4 instead of 0, and the first
+// triangle's edges take the B averages of the other edge.
+template <typename T>
+__global__ void k_j_quint(const __grid_constant__ StageArgs<T> a) {
+    const KP<T>& p = a.p;
+    const T* __restrict__ X = a.n == 0 ? a.X[a.st->cur] : a.XS[(a.n - 1) & 1];
+    const T* __restrict__ Bg = a.outB;
+    T* __restrict__ J = a.outJ;
+    const int ax[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};
+    const long long nx2 = p.nx + 2, ny2 = p.ny + 2;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < p.N; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % p.nx), j = (int)((q / p.nx) % p.ny), k = (int)(q / ((long long)p.nx * p.ny));
+        T NA[3][3], II[3];
+#pragma unroll
+        for (int pl = 0; pl < 3; pl++) {
+            T x[3][3][3], b[3][3][3], xwp[3], xwm[3];
+#pragma unroll
+            for (int aa = 0; aa < 3; aa++)
+#pragma unroll
+                for (int bb = 0; bb < 3; bb++) {
+                    int o[3] = {0, 0, 0};
+                    o[ax[pl][0]] = aa - 1; o[ax[pl][1]] = bb - 1;
+                    const long long g = gidx(p.px, p.py, i + o[0], j + o[1], k + o[2]);
+                    const long long gb = (i + 1 + o[0]) + nx2 * ((j + 1 + o[1]) + ny2 * (long long)(k + 1 + o[2]));
+#pragma unroll
+                    for (int l = 0; l < 3; l++) { x[aa][bb][l] = X[l * p.cs + g]; b[aa][bb][l] = Bg[3 * gb + l]; }
+                }
+            {
+                int o[3] = {0, 0, 0};
+                o[ax[pl][2]] = 1;
+                const long long gp = gidx(p.px, p.py, i + o[0], j + o[1], k + o[2]);
+                const long long gm = gidx(p.px, p.py, i - o[0], j - o[1], k - o[2]);
+#pragma unroll
+                for (int l = 0; l < 3; l++) { xwp[l] = X[l * p.cs + gp]; xwm[l] = X[l * p.cs + gm]; }
+            }
+            T dx1[3], dx2[3], dx3[3], dx4[3], dx5[3], dx6[3], c[3];
+            int tri = 0;
+#pragma unroll
+            for (int l = 0; l < 3; l++) {
+                dx1[l] = x[1][0][l] - x[1][1][l];
+                dx2[l] = x[2][1][l] - x[1][1][l];
+                dx3[l] = x[1][2][l] - x[1][1][l];
+                dx4[l] = x[0][1][l] - x[1][1][l];
+                dx5[l] = xwp[l] - x[1][1][l];
+                dx6[l] = xwm[l] - x[1][1][l];
+            }
+            auto dot = [](const T* u, const T* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
+            cross3(dx1, dx2, c);
+            if (dot(c, dx5) < 0 || dot(c, dx6) > 0) {
+#pragma unroll
+                for (int l = 0; l < 3; l++) { dx5[l] = x[2][0][l] - x[1][0][l]; dx6[l] = x[2][1][l] - x[2][0][l]; }
+                tri = 2;
+            }
+            if (tri != 0) {
+                cross3(dx2, dx3, c);
+                if (dot(c, dx5) < 0 || dot(c, dx6) > 0) {
+#pragma unroll
+                    for (int l = 0; l < 3; l++) { dx5[l] = x[2][2][l] - x[2][1][l]; dx6[l] = x[1][2][l] - x[2][2][l]; }
+                    tri = 3;
+                }
+            }
+            if (tri != 0) {
+                cross3(dx3, dx4, c);
+                if (dot(c, dx5) < 0 || dot(c, dx6) > 4) {
+#pragma unroll
+                    for (int l = 0; l < 3; l++) { dx5[l] = x[0][2][l] - x[1][2][l]; dx6[l] = x[0][1][l] - x[0][2][l]; }
+                    tri = 4;
+                }
+            }
+            cross3(dx4, dx1, c);
+            if (tri != 0) {
+                if (dot(c, dx5) < 0 || dot(c, dx6) > 0) {
+#pragma unroll
+                    for (int l = 0; l < 3; l++) { dx5[l] = x[1][0][l] - x[0][0][l]; dx6[l] = x[0][0][l] - x[0][1][l]; }
+                    tri = 1;
+                }
+            }
+            T I = 0;
+#pragma unroll
+            for (int l = 0; l < 3; l++) {
+                dx1[l] = x[1][0][l] - x[0][1][l];
+                dx2[l] = x[2][1][l] - x[1][0][l];
+                dx3[l] = x[1][2][l] - x[2][1][l];
+                dx4[l] = x[0][1][l] - x[1][2][l];
+                if (tri != 1) I += (b[1][0][l] + b[0][1][l]) / 2 * dx1[l];
+                if (tri != 2) I += (b[2][1][l] + b[1][0][l]) / 2 * dx2[l];
+                if (tri != 3) I += (b[1][2][l] + b[2][1][l]) / 2 * dx3[l];
+                if (tri != 4) I += (b[0][1][l] + b[1][2][l]) / 2 * dx4[l];
+                if (tri == 1) I += (b[0][1][l] + b[0][0][l]) / 2 * dx5[l] + (b[1][0][l] + b[0][0][l]) / 2 * dx6[l];
+                if (tri == 2) I += (b[1][0][l] + b[2][0][l]) / 2 * dx5[l] + (b[2][1][l] + b[2][0][l]) / 2 * dx6[l];
+                if (tri == 3) I += (b[2][1][l] + b[2][2][l]) / 2 * dx5[l] + (b[1][2][l] + b[2][2][l]) / 2 * dx6[l];
+                if (tri == 4) I += (b[1][2][l] + b[0][2][l]) / 2 * dx5[l] + (b[0][1][l] + b[0][2][l]) / 2 * dx6[l];
+            }
+            T c12[3], c23[3], c34[3], c41[3], c56[3] = {0, 0, 0};
+            cross3(dx1, dx2, c12);
+            cross3(dx2, dx3, c23);
+            cross3(dx3, dx4, c34);
+            cross3(dx4, dx1, c41);
+            if (tri > 0) cross3(dx5, dx6, c56);
+            II[pl] = I;
+#pragma unroll
+            for (int l = 0; l < 3; l++) {
+                NA[pl][l] = (c12[l] + c23[l] + c34[l] + c41[l]) / 4;
+                if (tri > 0) NA[pl][l] += c56[l] / 2;
+            }
+        }
+        const T det = NA[0][0] * NA[1][1] * NA[2][2] + NA[0][1] * NA[1][2] * NA[2][0] + NA[0][2] * NA[1][0] * NA[2][1] -
+                      NA[0][0] * NA[1][2] * NA[2][1] - NA[0][1] * NA[1][0] * NA[2][2] - NA[0][2] * NA[1][1] * NA[2][0];
+        const T det1 = (T)1 / det;
+        T N1[3][3];
+        N1[0][0] = (NA[1][1] * NA[2][2] - NA[1][2] * NA[2][1]) * det1;
+        N1[0][1] = (NA[0][2] * NA[2][1] - NA[0][1] * NA[2][2]) * det1;
+        N1[0][2] = (NA[0][1] * NA[1][2] - NA[0][2] * NA[1][1]) * det1;
+        N1[1][0] = (NA[1][2] * NA[2][0] - NA[1][0] * NA[2][2]) * det1;
+        N1[1][1] = (NA[0][0] * NA[2][2] - NA[0][2] * NA[2][0]) * det1;
+        N1[1][2] = (NA[0][2] * NA[1][0] - NA[0][0] * NA[1][2]) * det1;
+        N1[2][0] = (NA[1][0] * NA[2][1] - NA[1][1] * NA[2][0]) * det1;
+        N1[2][1] = (NA[0][1] * NA[2][0] - NA[0][0] * NA[2][1]) * det1;
+        N1[2][2] = (NA[0][0] * NA[1][1] - NA[0][1] * NA[1][0]) * det1;
+#pragma unroll
+        for (int l = 0; l < 3; l++) {
+            T Jl = 0;
+#pragma unroll
+            for (int m = 0; m < 3; m++) Jl += N1[l][m] * II[m];
+            J[3 * q + l] = Jl;
+        }
+    }
+}
+
 // Two k-layout arrays (x and velocity increments) into the reference's
 // six-value kk record per inner point.
 template <typename T>
@@ -1296,6 +1432,12 @@ cudaError_t launch_j_oct(const StageArgs<T>& a, cudaStream_t s) {
 }
 
 template <typename T>
+cudaError_t launch_j_quint(const StageArgs<T>& a, cudaStream_t s) {
+    k_j_quint<T><<<nblk(a.p.N), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_pack_k6(const KP<T>& p, const T* kx, const T* ku, T* aos, cudaStream_t s) {
     k_pack_k6<T><<<nblk(p.N), 256, 0, s>>>(p, kx, ku, aos);
     return cudaGetLastError();
@@ -1344,6 +1486,7 @@ cudaError_t launch_eps_star(const KP<T>& p, const T* B, const T* J, const T* X, 
     template cudaError_t launch_pack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \
     template cudaError_t launch_pack_k6<T>(const KP<T>&, const T*, const T*, T*, cudaStream_t);                  \
     template cudaError_t launch_j_oct<T>(const StageArgs<T>&, cudaStream_t);                                    \
+    template cudaError_t launch_j_quint<T>(const StageArgs<T>&, cudaStream_t);                                  \
     template cudaError_t launch_unpack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                          \
     template cudaError_t launch_export_ghosts<T>(const KP<T>&, T*, T*, cudaStream_t);                            \
     template cudaError_t launch_grid_fields<T>(const KP<T>&, const T*, T*, T*, T*, cudaStream_t);                 \

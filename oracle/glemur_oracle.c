@@ -63,6 +63,7 @@ typedef struct {
     R p0Amp, p0Width;
     int jClassic;              /* jMethod = "Classic" (else "Stokes")            */
     int jOct;                  /* jMethod = "Stokes4th": octilateral contours    */
+    int jQuint;                /* jMethod = "StokesQuint": quintilaterals        */
     int inertia;               /* the velocity equation (rungeKutta.cu:195-212)  */
     R nu;                      /* velocity damping                               */
     int jxbAver;               /* neighbour-averaged Lorentz force               */
@@ -110,6 +111,7 @@ static void to_P(const gm_params* g, P* p) {
     p->p0Amp = (R)g->p0Amp; p->p0Width = (R)g->p0Width;
     p->jClassic = strncmp(g->jMethod, "Classic ", 8) == 0;
     p->jOct = strncmp(g->jMethod, "Stokes4th ", 10) == 0;
+    p->jQuint = strncmp(g->jMethod, "StokesQuint ", 12) == 0;
     p->inertia = g->inertia != 0;
     p->nu = (R)g->nu;
     p->jxbAver = g->jxbAver != 0;
@@ -746,6 +748,150 @@ static void j_stokes4th(orc_state* s) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Quintilateral Stokes current, JStokesQuint src/current.cu:737-1199       */
+/* ------------------------------------------------------------------------ */
+
+/* For each plane through the point, axes (u, v, w) = (x, y, z), (y, z, x),
+ * (z, x, y), with P(a, b) the in-plane neighbour at offsets (a - 1, b - 1):
+ * the diamond through the face neighbours P(0,1) P(1,0) P(2,1) P(1,2), and,
+ * when the orientation tests of current.cu:863-896 pick a corner triangle,
+ * that triangle's two outer edges in place of one diamond edge.  The tests
+ * are restated as written: each later test looks at the edge vectors the
+ * previous one stored, the third compares with 4 instead of 0, and the first
+ * triangle's edges take the B averages of the other edge (current.cu:919-
+ * 922).  Area vector: (1/4) of the diamond's consecutive cross products plus
+ * (1/2) of the triangle's; the solve multiplies by 1/det. */
+static void j_stokes_quint(orc_state* s) {
+    const P* p = &s->p;
+    static const int ax[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};
+    int k;
+#pragma omp parallel for schedule(static)
+    for (k = 0; k < p->nz; k++) {
+        int i, j, l, m, pl;
+        for (j = 0; j < p->ny; j++)
+            for (i = 0; i < p->nx; i++) {
+                R NA[3][3], NA1[3][3], II_[3], detN, detN1;
+                for (pl = 0; pl < 3; pl++) {
+#define PO(a_, b_, w_, out)                                                   \
+    do {                                                                      \
+        int o_[3] = {0, 0, 0};                                                \
+        o_[ax[pl][0]] = (a_) - 1; o_[ax[pl][1]] = (b_) - 1; o_[ax[pl][2]] = (w_); \
+        (out) = GI(p, i + 1 + o_[0], j + 1 + o_[1], k + 1 + o_[2]);          \
+    } while (0)
+                    size_t g;
+                    const R *xc, *x[3][3], *xw_p, *xw_m, *b[3][3];
+                    R dx1[3], dx2[3], dx3[3], dx4[3], dx5[3], dx6[3], c[3], I = 0;
+                    int a, bb, tri = 0;
+                    for (a = 0; a < 3; a++)
+                        for (bb = 0; bb < 3; bb++) {
+                            PO(a, bb, 0, g);
+                            x[a][bb] = &s->xb[3 * g];
+                            b[a][bb] = &s->B[3 * g];
+                        }
+                    xc = x[1][1];
+                    PO(1, 1, 1, g); xw_p = &s->xb[3 * g];
+                    PO(1, 1, -1, g); xw_m = &s->xb[3 * g];
+#undef PO
+                    for (l = 0; l < 3; l++) {
+                        dx1[l] = x[1][0][l] - xc[l];
+                        dx2[l] = x[2][1][l] - xc[l];
+                        dx3[l] = x[1][2][l] - xc[l];
+                        dx4[l] = x[0][1][l] - xc[l];
+                        dx5[l] = xw_p[l] - xc[l];
+                        dx6[l] = xw_m[l] - xc[l];
+                    }
+                    cross3(dx1, dx2, c);
+                    if (dot3(c, dx5) < 0 || dot3(c, dx6) > 0) {
+                        for (l = 0; l < 3; l++) {
+                            dx5[l] = x[2][0][l] - x[1][0][l];
+                            dx6[l] = x[2][1][l] - x[2][0][l];
+                        }
+                        tri = 2;
+                    }
+                    if (tri != 0) {
+                        cross3(dx2, dx3, c);
+                        if (dot3(c, dx5) < 0 || dot3(c, dx6) > 0) {
+                            for (l = 0; l < 3; l++) {
+                                dx5[l] = x[2][2][l] - x[2][1][l];
+                                dx6[l] = x[1][2][l] - x[2][2][l];
+                            }
+                            tri = 3;
+                        }
+                    }
+                    if (tri != 0) {
+                        cross3(dx3, dx4, c);
+                        if (dot3(c, dx5) < 0 || dot3(c, dx6) > 4) {
+                            for (l = 0; l < 3; l++) {
+                                dx5[l] = x[0][2][l] - x[1][2][l];
+                                dx6[l] = x[0][1][l] - x[0][2][l];
+                            }
+                            tri = 4;
+                        }
+                    }
+                    cross3(dx4, dx1, c);
+                    if (tri != 0) {
+                        if (dot3(c, dx5) < 0 || dot3(c, dx6) > 0) {
+                            for (l = 0; l < 3; l++) {
+                                dx5[l] = x[1][0][l] - x[0][0][l];
+                                dx6[l] = x[0][0][l] - x[0][1][l];
+                            }
+                            tri = 1;
+                        }
+                    }
+                    for (l = 0; l < 3; l++) {
+                        dx1[l] = x[1][0][l] - x[0][1][l];
+                        dx2[l] = x[2][1][l] - x[1][0][l];
+                        dx3[l] = x[1][2][l] - x[2][1][l];
+                        dx4[l] = x[0][1][l] - x[1][2][l];
+                        if (tri != 1) I += (b[1][0][l] + b[0][1][l]) / 2 * dx1[l];
+                        if (tri != 2) I += (b[2][1][l] + b[1][0][l]) / 2 * dx2[l];
+                        if (tri != 3) I += (b[1][2][l] + b[2][1][l]) / 2 * dx3[l];
+                        if (tri != 4) I += (b[0][1][l] + b[1][2][l]) / 2 * dx4[l];
+                        if (tri == 1)
+                            I += (b[0][1][l] + b[0][0][l]) / 2 * dx5[l] + (b[1][0][l] + b[0][0][l]) / 2 * dx6[l];
+                        if (tri == 2)
+                            I += (b[1][0][l] + b[2][0][l]) / 2 * dx5[l] + (b[2][1][l] + b[2][0][l]) / 2 * dx6[l];
+                        if (tri == 3)
+                            I += (b[2][1][l] + b[2][2][l]) / 2 * dx5[l] + (b[1][2][l] + b[2][2][l]) / 2 * dx6[l];
+                        if (tri == 4)
+                            I += (b[1][2][l] + b[0][2][l]) / 2 * dx5[l] + (b[0][1][l] + b[0][2][l]) / 2 * dx6[l];
+                    }
+                    {
+                        R c12[3], c23[3], c34[3], c41[3], c56[3];
+                        cross3(dx1, dx2, c12);
+                        cross3(dx2, dx3, c23);
+                        cross3(dx3, dx4, c34);
+                        cross3(dx4, dx1, c41);
+                        if (tri > 0) cross3(dx5, dx6, c56);
+                        II_[pl] = I;
+                        for (l = 0; l < 3; l++) {
+                            NA[pl][l] = (c12[l] + c23[l] + c34[l] + c41[l]) / 4;
+                            if (tri > 0) NA[pl][l] += c56[l] / 2;
+                        }
+                    }
+                }
+                detN = NA[0][0] * NA[1][1] * NA[2][2] + NA[0][1] * NA[1][2] * NA[2][0] + NA[0][2] * NA[1][0] * NA[2][1] -
+                       NA[0][0] * NA[1][2] * NA[2][1] - NA[0][1] * NA[1][0] * NA[2][2] - NA[0][2] * NA[1][1] * NA[2][0];
+                detN1 = 1 / detN;
+                NA1[0][0] = (NA[1][1] * NA[2][2] - NA[1][2] * NA[2][1]) * detN1;
+                NA1[0][1] = (NA[0][2] * NA[2][1] - NA[0][1] * NA[2][2]) * detN1;
+                NA1[0][2] = (NA[0][1] * NA[1][2] - NA[0][2] * NA[1][1]) * detN1;
+                NA1[1][0] = (NA[1][2] * NA[2][0] - NA[1][0] * NA[2][2]) * detN1;
+                NA1[1][1] = (NA[0][0] * NA[2][2] - NA[0][2] * NA[2][0]) * detN1;
+                NA1[1][2] = (NA[0][2] * NA[1][0] - NA[0][0] * NA[1][2]) * detN1;
+                NA1[2][0] = (NA[1][0] * NA[2][1] - NA[1][1] * NA[2][0]) * detN1;
+                NA1[2][1] = (NA[0][1] * NA[2][0] - NA[0][0] * NA[2][1]) * detN1;
+                NA1[2][2] = (NA[0][0] * NA[1][1] - NA[0][1] * NA[1][0]) * detN1;
+                for (l = 0; l < 3; l++) {
+                    R Jl = 0;
+                    for (m = 0; m < 3; m++) Jl += NA1[l][m] * II_[m];
+                    s->J[3 * II(p, i, j, k) + l] = Jl;
+                }
+            }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Finite-difference current, JClassic src/current.cu:10-218                */
 /* ------------------------------------------------------------------------ */
 
@@ -1057,6 +1203,7 @@ void orc_refresh_fields(orc_state* s) {
     set_b_bound(s);
     if (s->p.jClassic) j_classic(s);
     else if (s->p.jOct) j_stokes4th(s);
+    else if (s->p.jQuint) j_stokes_quint(s);
     else j_stokes(s);
 }
 

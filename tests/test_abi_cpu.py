@@ -125,7 +125,7 @@ def test_create_rejects_unsupported_options():
     h = C.c_void_p()
     assert lib.gm_create(p, C.byref(h)) == -1
     p = configs.braid2(8, 8, 8)
-    p.set_str("jMethod", "StokesQuint")
+    p.set_str("jMethod", "Stokes2nd")
     assert lib.gm_create(p, C.byref(h)) == -1
 
 

@@ -70,7 +70,7 @@ def test_stages_match_oracle(name):
 @pytest.mark.parametrize("name", ["braid_f64", "braid_f32", "tied_f64", "press_f64", "classic_tied_f64",
                                   "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64",
                                   "classic_press_tied_f64", "classic_inertia_tied_f64", "jxbaver_f64", "oct_f64",
-                                  "oct_tied_f64", "oct_f32"])
+                                  "oct_tied_f64", "oct_f32", "quint_f64", "quint_tied_f64"])
 def test_stages_match_reference_kernels(name):
     stage_by_stage(cases.make(name), RefLauncher)
 
@@ -261,3 +261,38 @@ def test_nan_in_b0_is_reported():
     with pytest.raises(Exception):
         g.run(5)
     assert g.state()["status"] & 1
+
+
+@pytest.mark.parametrize("method", ["Stokes", "Stokes4th", "StokesQuint", "Classic"])
+def test_currents_on_a_strongly_distorted_grid(method):
+    """B and J at a grid with random displacements of up to 0.45 spacings per
+    component (some cells fold): the currents' geometric branches (the
+    quintilateral's corner triangles, taken where a neighbour lies on the far
+    side of a face plane) against the oracle and the reference's own
+    kernels."""
+    p = configs.braid2(17, 12, 17, precision=64)
+    p.xPeri = p.yPeri = p.zPeri = 0
+    p.errMode = 0
+    p.set_str("jMethod", method)
+    p = configs.derive(p)
+    B0, xb = configs.init_state(p)
+    rng = np.random.default_rng(3)
+    x = xb.copy()
+    sp = np.array([p.dx, p.dy, p.dz])
+    x[1:-1, 1:-1, 1:-1] += rng.uniform(-0.45, 0.45, size=x[1:-1, 1:-1, 1:-1].shape) * sp
+    g = Relaxation(p)
+    g.upload(x, B0)
+    g.refresh()
+    f = g.download()
+    o = Oracle(p, B0, x)
+    o.refresh()
+    fo = o.get()
+    r = RefLauncher(p, B0, x)
+    r.refresh()
+    fr = r.get()
+    assert relerr(inner(f["B"]), inner(fo["B"])) < 1e-12
+    assert relerr(f["J"], fo["J"]) < 1e-10
+    assert relerr(fo["J"], fr["J"]) < 1e-10
+    g.close()
+    o.close()
+    r.close()
