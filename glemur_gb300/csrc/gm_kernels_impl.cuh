@@ -1050,8 +1050,10 @@ __global__ void k_j_oct(const __grid_constant__ StageArgs<T> a) {
 // the face neighbours, with a corner triangle's two outer edges in place of one
 // diamond edge where the orientation tests pick one.  The tests are the
 // reference's as written: each later test reads the edge vectors the previous
-// one stored, the third compares with 4 instead of 0, and the first
-// triangle's edges take the B averages of the other edge.
+// one stored, the third compares with 4 instead of 0, the first triangle's
+// edges take the B averages of the other edge, and in the (y, z, x) and
+// (z, x, y) planes the fourth triangle's second edge runs from P(1, 2), not
+// P(0, 2), to P(0, 1) (src/current.cu:995-996, 1104-1105).
 template <typename T>
 __global__ void k_j_quint(const __grid_constant__ StageArgs<T> a) {
     const KP<T>& p = a.p;
@@ -1115,7 +1117,7 @@ __global__ void k_j_quint(const __grid_constant__ StageArgs<T> a) {
                 cross3(dx3, dx4, c);
                 if (dot(c, dx5) < 0 || dot(c, dx6) > 4) {
 #pragma unroll
-                    for (int l = 0; l < 3; l++) { dx5[l] = x[0][2][l] - x[1][2][l]; dx6[l] = x[0][1][l] - x[0][2][l]; }
+                    for (int l = 0; l < 3; l++) { dx5[l] = x[0][2][l] - x[1][2][l]; dx6[l] = x[0][1][l] - (pl == 0 ? x[0][2][l] : x[1][2][l]); }
                     tri = 4;
                 }
             }

@@ -757,10 +757,12 @@ static void j_stokes4th(orc_state* s) {
  * when the orientation tests of current.cu:863-896 pick a corner triangle,
  * that triangle's two outer edges in place of one diamond edge.  The tests
  * are restated as written: each later test looks at the edge vectors the
- * previous one stored, the third compares with 4 instead of 0, and the first
+ * previous one stored, the third compares with 4 instead of 0, the first
  * triangle's edges take the B averages of the other edge (current.cu:919-
- * 922).  Area vector: (1/4) of the diamond's consecutive cross products plus
- * (1/2) of the triangle's; the solve multiplies by 1/det. */
+ * 922), and in the second and third planes the fourth triangle's second edge
+ * runs from P(1, 2), not P(0, 2), to P(0, 1) (current.cu:995-996,
+ * 1104-1105).  Area vector: (1/4) of the diamond's consecutive cross
+ * products plus (1/2) of the triangle's; the solve multiplies by 1/det. */
 static void j_stokes_quint(orc_state* s) {
     const P* p = &s->p;
     static const int ax[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};
@@ -823,7 +825,7 @@ static void j_stokes_quint(orc_state* s) {
                         if (dot3(c, dx5) < 0 || dot3(c, dx6) > 4) {
                             for (l = 0; l < 3; l++) {
                                 dx5[l] = x[0][2][l] - x[1][2][l];
-                                dx6[l] = x[0][1][l] - x[0][2][l];
+                                dx6[l] = x[0][1][l] - (pl == 0 ? x[0][2][l] : x[1][2][l]);
                             }
                             tri = 4;
                         }
