@@ -193,11 +193,8 @@ int main(int argc, char* argv[]) {
     }
     printf("jMethod = %s\n", p.jMethod);
     if (!starts(p.jMethod, "Stokes ") && !starts(p.jMethod, "Classic ") && !starts(p.jMethod, "Stokes4th ") &&
-        !starts(p.jMethod, "StokesQuint ")) {
-        if (starts(p.jMethod, "StokesTri "))
-            printf("error: method for computing J not built in this implementation: %s\n", p.jMethod);
-        else
-            printf("error: invalid method for computing J: %s\n", p.jMethod);
+        !starts(p.jMethod, "StokesQuint ") && !starts(p.jMethod, "StokesTri ")) {
+        printf("error: invalid method for computing J: %s\n", p.jMethod);
         return -1;
     }
     printf("initial B: %s\n", p.bInit);

@@ -59,8 +59,9 @@ int check_params(const gm_params* p) {
     if (p->nx < 3 || p->ny < 3 || p->nz < 3) return gm::fail(GM_EPARAM, "nx, ny, nz must be >= 3");
     if ((long long)p->nx * p->ny * p->nz > (1ll << 31)) return gm::fail(GM_EPARAM, "grid too large");
     if (strncmp(p->jMethod, "Stokes ", 7) != 0 && strncmp(p->jMethod, "Classic ", 8) != 0 &&
-        strncmp(p->jMethod, "Stokes4th ", 10) != 0 && strncmp(p->jMethod, "StokesQuint ", 12) != 0)
-        return gm::fail(GM_EPARAM, "jMethod: the Stokes, Stokes4th, StokesQuint and Classic currents are implemented");
+        strncmp(p->jMethod, "Stokes4th ", 10) != 0 && strncmp(p->jMethod, "StokesQuint ", 12) != 0 &&
+        strncmp(p->jMethod, "StokesTri ", 10) != 0)
+        return gm::fail(GM_EPARAM, "jMethod: the Stokes, Stokes4th, StokesQuint, StokesTri and Classic currents are implemented");
     if (p->pressure && strncmp(p->pMethod, "Classic ", 8) != 0) return gm::fail(GM_EPARAM, "pMethod must be Classic");
     if (p->initShearA != 0 || p->initShearB != 0)
         return gm::fail(GM_EPARAM, "initial-distortion ghost corrections (initShearA/B != 0) are not implemented");
@@ -188,6 +189,7 @@ struct Impl : ImplBase {
         kp.jClassic = strncmp(p->jMethod, "Classic ", 8) == 0;
         kp.jOct = strncmp(p->jMethod, "Stokes4th ", 10) == 0;
         kp.jQuint = strncmp(p->jMethod, "StokesQuint ", 12) == 0;
+        kp.jTri = strncmp(p->jMethod, "StokesTri ", 10) == 0;
         kp.inertia = p->inertia != 0;
         kp.nu = (T)p->nu;
         kp.jxbAver = p->jxbAver != 0 && !p->inertia;   // the reference applies it in the frictional branch only
@@ -447,7 +449,7 @@ struct Impl : ImplBase {
             A.a.TZ = TZ2;
             CUDA_TRY(gmk::launch_stage_tma<T>(A, gp.pressure, grid2, stream));
         } else {
-            if (kp.jxbAver || kp.jOct || kp.jQuint) {
+            if (kp.jxbAver || kp.jOct || kp.jQuint || kp.jTri) {
                 // the averaged Lorentz force reads J and B of this stage at every
                 // point's neighbours, and the octilateral current B at the edge
                 // neighbours with the reference's ghost values (current() before
@@ -457,7 +459,7 @@ struct Impl : ImplBase {
                 CUDA_TRY(gmk::launch_stage<T>(aj, gmk::MODE_DIAG, gp.pressure, grid, block, smem_diag, stream));
                 CUDA_TRY(gmk::launch_export_ghosts<T>(kp, outB, outD, stream));
                 launches += 1 + kp.xPeri + kp.yPeri + kp.zPeri;
-                if (kp.jOct || kp.jQuint) {
+                if (kp.jOct || kp.jQuint || kp.jTri) {
                     CUDA_TRY(kp.jOct ? gmk::launch_j_oct<T>(args(n), stream) : gmk::launch_j_quint<T>(args(n), stream));
                     launches++;
                 }
@@ -718,7 +720,7 @@ struct Impl : ImplBase {
         int rc = read_state();
         if (rc) return rc;
         StageArgs<T> a = args(0);
-        if (kp.jOct || kp.jQuint) {
+        if (kp.jOct || kp.jQuint || kp.jTri) {
             // the octilateral and quintilateral currents need the exported B
             // with its ghosts first; the diagnostic pass then reads J from it
             StageArgs<T> aj = args(0);

@@ -69,6 +69,7 @@ struct KP {
     int jClassic;            // jMethod = "Classic": the finite-difference current (generic kernel only)
     int jOct;                // jMethod = "Stokes4th": J from the octilateral pass (outJ; generic kernel only)
     int jQuint;              // jMethod = "StokesQuint": J from the quintilateral pass (outJ; generic kernel only)
+    int jTri;                // jMethod = "StokesTri": J from the same pass in its triangle-only form
     int inertia;             // the velocity equation (generic kernel only)
     T nu;                    // velocity damping
     int jxbAver;             // neighbour-averaged Lorentz force (generic kernel only)

@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
                 T Bc[3], Jv[3];
 #pragma unroll
                 for (int l = 0; l < 3; l++) Bc[l] = t.b(kc, l, j, i);
-                if ((p.jOct || p.jQuint) && !a.jpass) {
+                if ((p.jOct || p.jQuint || p.jTri) && !a.jpass) {
                     // the octilateral / quintilateral current, computed after the J pass
                     const long long lj = (long long)i + (long long)p.nx * ((long long)j + (long long)p.ny * kc);
                     Jv[0] = a.outJ[3 * lj]; Jv[1] = a.outJ[3 * lj + 1]; Jv[2] = a.outJ[3 * lj + 2];
@@ -1054,6 +1054,20 @@ __global__ void k_j_oct(const __grid_constant__ StageArgs<T> a) {
 // edges take the B averages of the other edge, and in the (y, z, x) and
 // (z, x, y) planes the fourth triangle's second edge runs from P(1, 2), not
 // P(0, 2), to P(0, 1) (src/current.cu:995-996, 1104-1105).
+// With p.jTri, the triangular Stokes current (JStokesTri, src/current.cu:
+// 1202-1681): the same tests, but a plane where they pick a triangle takes that
+// triangle alone (its two outer edges and the reversed diamond edge) as the
+// contour and half the outer edges' cross product as the area vector.  The
+// reference adds that to an area vector it never set (src/current.cu:1420-
+// 1424), and its compiled kernel returns NaN in J wherever a plane takes a
+// triangle; the unset start is NaN here too, so the stage's NaN check stops
+// the step there.
+template <typename T>
+__device__ __forceinline__ T quiet_nan() {
+    if constexpr (sizeof(T) == 8) return __longlong_as_double(0x7ff8000000000000ll);
+    else return __int_as_float(0x7fc00000);
+}
+
 template <typename T>
 __global__ void k_j_quint(const __grid_constant__ StageArgs<T> a) {
     const KP<T>& p = a.p;
@@ -1136,10 +1150,18 @@ __global__ void k_j_quint(const __grid_constant__ StageArgs<T> a) {
                 dx2[l] = x[2][1][l] - x[1][0][l];
                 dx3[l] = x[1][2][l] - x[2][1][l];
                 dx4[l] = x[0][1][l] - x[1][2][l];
-                if (tri != 1) I += (b[1][0][l] + b[0][1][l]) / 2 * dx1[l];
-                if (tri != 2) I += (b[2][1][l] + b[1][0][l]) / 2 * dx2[l];
-                if (tri != 3) I += (b[1][2][l] + b[2][1][l]) / 2 * dx3[l];
-                if (tri != 4) I += (b[0][1][l] + b[1][2][l]) / 2 * dx4[l];
+                if (p.jTri && tri != 0) {
+                    // the triangle's closing edge: the diamond edge reversed
+                    if (tri == 1) I -= (b[1][0][l] + b[0][1][l]) / 2 * dx1[l];
+                    if (tri == 2) I -= (b[2][1][l] + b[1][0][l]) / 2 * dx2[l];
+                    if (tri == 3) I -= (b[1][2][l] + b[2][1][l]) / 2 * dx3[l];
+                    if (tri == 4) I -= (b[0][1][l] + b[1][2][l]) / 2 * dx4[l];
+                } else {
+                    if (tri != 1) I += (b[1][0][l] + b[0][1][l]) / 2 * dx1[l];
+                    if (tri != 2) I += (b[2][1][l] + b[1][0][l]) / 2 * dx2[l];
+                    if (tri != 3) I += (b[1][2][l] + b[2][1][l]) / 2 * dx3[l];
+                    if (tri != 4) I += (b[0][1][l] + b[1][2][l]) / 2 * dx4[l];
+                }
                 if (tri == 1) I += (b[0][1][l] + b[0][0][l]) / 2 * dx5[l] + (b[1][0][l] + b[0][0][l]) / 2 * dx6[l];
                 if (tri == 2) I += (b[1][0][l] + b[2][0][l]) / 2 * dx5[l] + (b[2][1][l] + b[2][0][l]) / 2 * dx6[l];
                 if (tri == 3) I += (b[2][1][l] + b[2][2][l]) / 2 * dx5[l] + (b[1][2][l] + b[2][2][l]) / 2 * dx6[l];
@@ -1154,8 +1176,12 @@ __global__ void k_j_quint(const __grid_constant__ StageArgs<T> a) {
             II[pl] = I;
 #pragma unroll
             for (int l = 0; l < 3; l++) {
-                NA[pl][l] = (c12[l] + c23[l] + c34[l] + c41[l]) / 4;
-                if (tri > 0) NA[pl][l] += c56[l] / 2;
+                if (p.jTri && tri > 0) {
+                    NA[pl][l] = quiet_nan<T>() + c56[l] / 2;
+                } else {
+                    NA[pl][l] = (c12[l] + c23[l] + c34[l] + c41[l]) / 4;
+                    if (tri > 0) NA[pl][l] += c56[l] / 2;
+                }
             }
         }
         const T det = NA[0][0] * NA[1][1] * NA[2][2] + NA[0][1] * NA[1][2] * NA[2][0] + NA[0][2] * NA[1][0] * NA[2][1] -

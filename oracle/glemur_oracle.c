@@ -64,6 +64,7 @@ typedef struct {
     int jClassic;              /* jMethod = "Classic" (else "Stokes")            */
     int jOct;                  /* jMethod = "Stokes4th": octilateral contours    */
     int jQuint;                /* jMethod = "StokesQuint": quintilaterals        */
+    int jTri;                  /* jMethod = "StokesTri": diamonds or triangles   */
     int inertia;               /* the velocity equation (rungeKutta.cu:195-212)  */
     R nu;                      /* velocity damping                               */
     int jxbAver;               /* neighbour-averaged Lorentz force               */
@@ -112,6 +113,7 @@ static void to_P(const gm_params* g, P* p) {
     p->jClassic = strncmp(g->jMethod, "Classic ", 8) == 0;
     p->jOct = strncmp(g->jMethod, "Stokes4th ", 10) == 0;
     p->jQuint = strncmp(g->jMethod, "StokesQuint ", 12) == 0;
+    p->jTri = strncmp(g->jMethod, "StokesTri ", 10) == 0;
     p->inertia = g->inertia != 0;
     p->nu = (R)g->nu;
     p->jxbAver = g->jxbAver != 0;
@@ -762,8 +764,18 @@ static void j_stokes4th(orc_state* s) {
  * 922), and in the second and third planes the fourth triangle's second edge
  * runs from P(1, 2), not P(0, 2), to P(0, 1) (current.cu:995-996,
  * 1104-1105).  Area vector: (1/4) of the diamond's consecutive cross
- * products plus (1/2) of the triangle's; the solve multiplies by 1/det. */
-static void j_stokes_quint(orc_state* s) {
+ * products plus (1/2) of the triangle's; the solve multiplies by 1/det.
+ *
+ * With tri_only set, the triangular Stokes current (JStokesTri,
+ * current.cu:1202-1681): the same tests, but a plane where they pick a
+ * triangle takes that triangle alone, its two outer edges and the reversed
+ * diamond edge (with that edge's B average) as the contour and (1/2) of the
+ * outer edges' cross product as the area vector.  The reference adds that
+ * half cross product to an area vector that nothing set before
+ * (current.cu:1420-1424); its compiled kernel returns NaN in all three
+ * components of J at every point where a plane takes a triangle (measured on
+ * a grid with 618 such points out of 3468), so that unset start is NaN here. */
+static void j_stokes_quint(orc_state* s, int tri_only) {
     const P* p = &s->p;
     static const int ax[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};
     int k;
@@ -845,10 +857,18 @@ static void j_stokes_quint(orc_state* s) {
                         dx2[l] = x[2][1][l] - x[1][0][l];
                         dx3[l] = x[1][2][l] - x[2][1][l];
                         dx4[l] = x[0][1][l] - x[1][2][l];
-                        if (tri != 1) I += (b[1][0][l] + b[0][1][l]) / 2 * dx1[l];
-                        if (tri != 2) I += (b[2][1][l] + b[1][0][l]) / 2 * dx2[l];
-                        if (tri != 3) I += (b[1][2][l] + b[2][1][l]) / 2 * dx3[l];
-                        if (tri != 4) I += (b[0][1][l] + b[1][2][l]) / 2 * dx4[l];
+                        if (tri_only && tri != 0) {
+                            /* the triangle's closing edge: the diamond edge reversed */
+                            if (tri == 1) I -= (b[1][0][l] + b[0][1][l]) / 2 * dx1[l];
+                            if (tri == 2) I -= (b[2][1][l] + b[1][0][l]) / 2 * dx2[l];
+                            if (tri == 3) I -= (b[1][2][l] + b[2][1][l]) / 2 * dx3[l];
+                            if (tri == 4) I -= (b[0][1][l] + b[1][2][l]) / 2 * dx4[l];
+                        } else {
+                            if (tri != 1) I += (b[1][0][l] + b[0][1][l]) / 2 * dx1[l];
+                            if (tri != 2) I += (b[2][1][l] + b[1][0][l]) / 2 * dx2[l];
+                            if (tri != 3) I += (b[1][2][l] + b[2][1][l]) / 2 * dx3[l];
+                            if (tri != 4) I += (b[0][1][l] + b[1][2][l]) / 2 * dx4[l];
+                        }
                         if (tri == 1)
                             I += (b[0][1][l] + b[0][0][l]) / 2 * dx5[l] + (b[1][0][l] + b[0][0][l]) / 2 * dx6[l];
                         if (tri == 2)
@@ -867,8 +887,12 @@ static void j_stokes_quint(orc_state* s) {
                         if (tri > 0) cross3(dx5, dx6, c56);
                         II_[pl] = I;
                         for (l = 0; l < 3; l++) {
-                            NA[pl][l] = (c12[l] + c23[l] + c34[l] + c41[l]) / 4;
-                            if (tri > 0) NA[pl][l] += c56[l] / 2;
+                            if (tri_only && tri > 0) {
+                                NA[pl][l] = (R)NAN + c56[l] / 2;
+                            } else {
+                                NA[pl][l] = (c12[l] + c23[l] + c34[l] + c41[l]) / 4;
+                                if (tri > 0) NA[pl][l] += c56[l] / 2;
+                            }
                         }
                     }
                 }
@@ -1205,7 +1229,8 @@ void orc_refresh_fields(orc_state* s) {
     set_b_bound(s);
     if (s->p.jClassic) j_classic(s);
     else if (s->p.jOct) j_stokes4th(s);
-    else if (s->p.jQuint) j_stokes_quint(s);
+    else if (s->p.jQuint) j_stokes_quint(s, 0);
+    else if (s->p.jTri) j_stokes_quint(s, 1);
     else j_stokes(s);
 }
 

@@ -192,6 +192,7 @@ struct Ref {
     bool classic = false;   // jMethod = "Classic": JClassic instead of JStokes
     bool oct = false;       // jMethod = "Stokes4th": JStokes4th (same shared memory as JStokes)
     bool quint = false;     // jMethod = "StokesQuint": JStokesQuint (same shared memory)
+    bool tri = false;       // jMethod = "StokesTri": JStokesTri (same shared memory)
 };
 Ref S;
 
@@ -207,6 +208,7 @@ const char* kname(const char* base, int prec) {
     else if (b == "JClassic") s = "_Z8JClassic7VarsDeviii";
     else if (b == "JStokes4th") s = "_Z10JStokes4th7VarsDeviii";
     else if (b == "JStokesQuint") s = "_Z12JStokesQuint7VarsDeviii";
+    else if (b == "JStokesTri") s = "_Z10JStokesTri7VarsDeviii";
     else if (b == "gradPClassic") s = "_Z12gradPClassic7VarsDeviii";
     else if (b == "kk") s = "_Z2kk7VarsDeviiii" + r;
     else if (b == "setGridPeriFace") s = "_Z15setGridPeriFaceP" + r + "i";
@@ -414,8 +416,9 @@ int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* 
     S.classic = strncmp(g->jMethod, "Classic ", 8) == 0;
     S.oct = strncmp(g->jMethod, "Stokes4th ", 10) == 0;
     S.quint = strncmp(g->jMethod, "StokesQuint ", 12) == 0;
-    if (strncmp(g->jMethod, "Stokes ", 7) != 0 && !S.classic && !S.oct && !S.quint) {
-        g_err = "only jMethod = Stokes, Stokes4th, StokesQuint or Classic";
+    S.tri = strncmp(g->jMethod, "StokesTri ", 10) == 0;
+    if (strncmp(g->jMethod, "Stokes ", 7) != 0 && !S.classic && !S.oct && !S.quint && !S.tri) {
+        g_err = "only jMethod = Stokes, Stokes4th, StokesQuint, StokesTri or Classic";
         return -1;
     }
     S.prec = g->precision;
@@ -429,7 +432,7 @@ int ref_open(const char* cubin, const gm_params* g, const void* B0, const void* 
     CK(D.ModuleLoad(&S.mod, cubin));
     int rc = 0;
     if ((rc = get_fn(&S.fBJ, "B_JacB0")) || (rc = get_fn(&S.fBound, "updateBbound")) ||
-        (rc = get_fn(&S.fPeri, "setPeriFace")) || (rc = get_fn(&S.fJ, S.classic ? "JClassic" : (S.oct ? "JStokes4th" : (S.quint ? "JStokesQuint" : "JStokes")))) ||
+        (rc = get_fn(&S.fPeri, "setPeriFace")) || (rc = get_fn(&S.fJ, S.classic ? "JClassic" : (S.oct ? "JStokes4th" : (S.quint ? "JStokesQuint" : (S.tri ? "JStokesTri" : "JStokes"))))) ||
         (rc = get_fn(&S.fGradP, "gradPClassic")) || (rc = get_fn(&S.fKK, "kk")) ||
         (rc = get_fn(&S.fGridPeri, "setGridPeriFace")) || (rc = get_fn(&S.fXNS, "xNewStar")) ||
         (rc = get_fn(&S.fMaxBlock, "maxBlock")))

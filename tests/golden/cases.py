@@ -30,6 +30,8 @@ reference's boundary handling:
   included.
 * quint_f64 / quint_tied_f64 -- the quintilateral Stokes current
   (jMethod = "StokesQuint", src/current.cu:737-1199).
+* tri_tied_f64 -- the triangular Stokes current (jMethod = "StokesTri",
+  src/current.cu:1202-1681), every face line-tied.
 """
 from __future__ import annotations
 
@@ -99,6 +101,10 @@ def make(name: str):
             p = _braid((17, 17, 18), 32 if name.endswith("32") else 64)
         p.set_str("jMethod", "Stokes4th")
         return configs.derive(p)
+    if name == "tri_tied_f64":
+        p = _braid((17, 12, 17), 64, peri=(0, 0, 0))
+        p.set_str("jMethod", "StokesTri")
+        return configs.derive(p)
     if name in ("quint_f64", "quint_tied_f64"):
         p = _braid((17, 12, 17), 64, peri=(0, 0, 0)) if name == "quint_tied_f64" else _braid((17, 17, 18), 64)
         p.set_str("jMethod", "StokesQuint")
@@ -123,5 +129,5 @@ def make(name: str):
 NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64", "classic_tied_f64",
          "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64", "classic_press_tied_f64",
          "classic_inertia_tied_f64", "jxbaver_f64", "oct_f64", "oct_tied_f64", "oct_f32", "quint_f64",
-         "quint_tied_f64"]
+         "quint_tied_f64", "tri_tied_f64"]
 N_ACCEPTED = 10

@@ -120,10 +120,7 @@ def test_init_state_matches_oracle(prec):
 
 def test_create_rejects_unsupported_options():
     lib = _abi.load()
-    p = configs.braid2(8, 8, 8)
-    p.set_str("jMethod", "StokesTri")
     h = C.c_void_p()
-    assert lib.gm_create(p, C.byref(h)) == -1
     p = configs.braid2(8, 8, 8)
     p.set_str("jMethod", "Stokes2nd")
     assert lib.gm_create(p, C.byref(h)) == -1

@@ -70,7 +70,8 @@ def test_stages_match_oracle(name):
 @pytest.mark.parametrize("name", ["braid_f64", "braid_f32", "tied_f64", "press_f64", "classic_tied_f64",
                                   "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64",
                                   "classic_press_tied_f64", "classic_inertia_tied_f64", "jxbaver_f64", "oct_f64",
-                                  "oct_tied_f64", "oct_f32", "quint_f64", "quint_tied_f64"])
+                                  "oct_tied_f64", "oct_f32", "quint_f64", "quint_tied_f64",
+                                  "tri_tied_f64"])
 def test_stages_match_reference_kernels(name):
     stage_by_stage(cases.make(name), RefLauncher)
 
@@ -263,13 +264,22 @@ def test_nan_in_b0_is_reported():
     assert g.state()["status"] & 1
 
 
-@pytest.mark.parametrize("method", ["Stokes", "Stokes4th", "StokesQuint", "Classic"])
+def _same_with_nan(a, b, tol):
+    """NaN at the same points, and the finite values within tol."""
+    na, nb = np.isnan(a), np.isnan(b)
+    assert np.array_equal(na, nb), (int(na.sum()), int(nb.sum()))
+    return relerr(np.where(na, 0, a), np.where(nb, 0, b)) < tol
+
+
+@pytest.mark.parametrize("method", ["Stokes", "Stokes4th", "StokesQuint", "StokesTri", "Classic"])
 def test_currents_on_a_strongly_distorted_grid(method):
     """B and J at a grid with random displacements of up to 0.45 spacings per
     component (some cells fold): the currents' geometric branches (the
-    quintilateral's corner triangles, taken where a neighbour lies on the far
-    side of a face plane) against the oracle and the reference's own
-    kernels."""
+    quintilateral's and the triangular current's corner triangles, taken where
+    a neighbour lies on the far side of a face plane) against the oracle and
+    the reference's own kernels.  The reference's triangular current is NaN
+    at every point where a plane takes a triangle (618 of 3468 here); the
+    GPU and the oracle are NaN at the same points."""
     p = configs.braid2(17, 12, 17, precision=64)
     p.xPeri = p.yPeri = p.zPeri = 0
     p.errMode = 0
@@ -291,8 +301,12 @@ def test_currents_on_a_strongly_distorted_grid(method):
     r.refresh()
     fr = r.get()
     assert relerr(inner(f["B"]), inner(fo["B"])) < 1e-12
-    assert relerr(f["J"], fo["J"]) < 1e-10
-    assert relerr(fo["J"], fr["J"]) < 1e-10
+    assert _same_with_nan(f["J"], fo["J"], 1e-10)
+    assert _same_with_nan(fo["J"], fr["J"], 1e-10)
+    if method == "StokesTri":
+        assert np.isnan(fr["J"]).any(-1).sum() == 618
+    else:
+        assert np.isfinite(fr["J"]).all()
     g.close()
     o.close()
     r.close()

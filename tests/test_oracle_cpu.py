@@ -252,6 +252,40 @@ def test_classic_and_stokes_currents_agree_to_truncation_error():
     assert errs[1] < errs[0] / 3.5, errs
 
 
+def test_corner_triangle_currents_on_a_folded_grid():
+    """On a grid with random displacements of up to 0.45 spacings (every face
+    line-tied), the quintilateral and triangular currents leave the diamond
+    only where a plane's orientation tests pick a corner triangle: elsewhere
+    both equal the Stokes current to rounding.  Where a triangle is taken, the
+    quintilateral current is finite, and the triangular one is NaN in all three
+    components, as the reference's kernel returns there (current.cu:1420-1424
+    add to an area vector that nothing set)."""
+    def current(method):
+        p = configs.braid2(17, 12, 17, precision=64)
+        p.xPeri = p.yPeri = p.zPeri = 0
+        p.set_str("jMethod", method)
+        p = configs.derive(p)
+        B0, xb = configs.init_state(p)
+        rng = np.random.default_rng(3)
+        x = xb.copy()
+        sp = np.array([p.dx, p.dy, p.dz])
+        x[1:-1, 1:-1, 1:-1] += rng.uniform(-0.45, 0.45, size=x[1:-1, 1:-1, 1:-1].shape) * sp
+        o = Oracle(p, B0, x)
+        o.refresh()
+        J = o.get()["J"]
+        o.close()
+        return J
+
+    Js, Jq, Jt = current("Stokes"), current("StokesQuint"), current("StokesTri")
+    scale = np.abs(Js).max()
+    tri = np.isnan(Jt).any(-1)
+    assert np.isnan(Jt[tri]).all() and tri.sum() == 618
+    assert np.isfinite(Jq).all()
+    moved = np.abs(Jq - Js).max(-1) > 1e-12 * scale
+    assert np.array_equal(moved, tri)
+    assert np.abs(Jt[~tri] - Js[~tri]).max() < 1e-12 * scale
+
+
 # ---- the velocity equation (inertia = T, src/rungeKutta.cu:195-212) -------
 
 def test_inertia_first_stage_from_rest():
