@@ -122,7 +122,7 @@ class Clocks:
             self.path.parent.mkdir(parents=True, exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -270,6 +270,7 @@ def run_gpu(args):
             torch.cuda.synchronize()
 
     l0 = g.launches
+    a0 = g.state()["nAttempted"]
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -288,7 +289,12 @@ def run_gpu(args):
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = N * 6 * args.steps * ws / (ms / 1e3)
+    # the attempted steps counted on the device: a run that stopped early (its
+    # status done) skips the remaining replays' work, and they do not count
+    ran = st["nAttempted"] - a0
+    if ran != args.steps:
+        print(f"warning: {ran} of {args.steps} timed steps ran (status {st['status']})", file=sys.stderr)
+    value = N * 6 * ran * ws / (ms / 1e3)
 
     # --- roofline of the stage kernel: per-launch time with events -----------
     reps = 3
@@ -352,9 +358,10 @@ def run_gpu(args):
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms / max(ran, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(p, {"attempted": st["nAttempted"], "accepted": st["timeIndex"],
+                                          "timed_steps_ran": ran,
                                           "tile_z": tune["tz"] if tune else None}),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -445,7 +452,7 @@ def run_batch(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
