@@ -204,6 +204,12 @@ int gm_init_state(const gm_params* p, void* B0, void* xb);
 
 /* ---- handle lifecycle (src/memory.cu:10-95, main.cu:181-256) ------------- */
 
+/* Allocate a relaxation for the parameters p (as read from params.in).
+ * Accepted: jMethod "Stokes" (the TMA stage kernel), "Stokes4th",
+ * "StokesQuint", "StokesTri" and "Classic" (current.cu:10-1681, selected as
+ * in current.cu:1685-1712); inertia, jxbAver and the Classic pressure
+ * gradient.  Anything else (another jMethod or pMethod, initShearA/B != 0)
+ * returns GM_EPARAM with the reason in gm_last_error(). */
 int gm_create(const gm_params* p, gm_handle** out);
 int gm_destroy(gm_handle* h);
 /* Use `stream` (a cudaStream_t) for all work of h; NULL selects the handle's
