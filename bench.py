@@ -86,14 +86,9 @@ def peaks():
 
 
 def dist_init():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    if ws > 1:
-        import torch.distributed as dist
-        backend = "nccl"
-        dist.init_process_group(backend)
-        return dist, rank, ws
-    return None, rank, ws
+    """(dist, rank, world_size): NCCL under torchrun; replicas, no exchange."""
+    from glemur_gb300 import replicas
+    return replicas.init("nccl")
 
 
 class Clocks:
@@ -285,16 +280,14 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     launches = g.launches - l0
     st = g.state()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    from glemur_gb300 import replicas
+    ms = replicas.max_over_ranks(dist, ms)        # the slowest replica's time
     # the attempted steps counted on the device: a run that stopped early (its
     # status done) skips the remaining replays' work, and they do not count
     ran = st["nAttempted"] - a0
     if ran != args.steps:
         print(f"warning: {ran} of {args.steps} timed steps ran (status {st['status']})", file=sys.stderr)
-    value = N * 6 * ran * ws / (ms / 1e3)
+    value = N * 6 * replicas.sum_over_ranks(dist, ran) / (ms / 1e3)
 
     # --- roofline of the stage kernel: per-launch time with events -----------
     reps = 3
@@ -342,10 +335,7 @@ def run_gpu(args):
     t1 = time.perf_counter()
     barrier()
     e2e_s = t1 - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.max_over_ranks(dist, e2e_s)
     e2e_value = N * 6 * args.steps * ws / e2e_s
     h2d = (xb.nbytes + B0.nbytes) / args.steps
     d2h = (xb.nbytes + 40) / args.steps + 40
@@ -383,10 +373,12 @@ def run_gpu(args):
 def run_batch(args):
     """--workload batch64: the batched configuration (see the module docstring)."""
     import torch
-    from glemur_gb300 import BatchRelaxation, Relaxation, configs
+    from glemur_gb300 import BatchRelaxation, Relaxation, configs, replicas
     dist, rank, ws = dist_init()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    ps = [configs.random_braid(1000 + i, precision=32) for i in range(64)]
+    # the 64 cases, split over the ranks (case i on rank i mod N)
+    mine = replicas.shard(64, rank, ws)
+    ps = [configs.random_braid(1000 + i, precision=32) for i in mine]
     inits = [configs.init_state(p) for p in ps]
     Ns = [p.nx * p.ny * p.nz for p in ps]
     b = BatchRelaxation(ps)
@@ -399,6 +391,8 @@ def run_batch(args):
         b.upload(c, xb, B0)
     l0 = b.launches()
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as ck:
         t0 = time.perf_counter()
         out = b.run(args.batch_cycles, args.batch_residual, pointwise=False, check_every=10)
@@ -406,11 +400,16 @@ def run_batch(args):
         wall = time.perf_counter() - t0
     launches = b.launches() - l0
     att = [o["attempted"] for o in out]
-    work = sum(N * 6 * a for N, a in zip(Ns, att))
+    my_work = sum(N * 6 * a for N, a in zip(Ns, att))
+    # the job: work summed over the ranks, time of the slowest rank
+    work = replicas.sum_over_ranks(dist, my_work)
+    wall = replicas.max_over_ranks(dist, wall)
     value = work / wall
-    secs = sorted(o["seconds"] for o in out)
-    conv = sum(o["converged"] for o in out)
-    folded = sum(1 for o in out if not o["converged"] and o["status"] & 4)
+    secs = sorted(replicas.gather_lists(dist, [o["seconds"] for o in out]))
+    conv = int(replicas.sum_over_ranks(dist, sum(o["converged"] for o in out)))
+    folded = int(replicas.sum_over_ranks(dist, sum(1 for o in out if not o["converged"] and o["status"] & 4)))
+    total_att = int(replicas.sum_over_ranks(dist, sum(att)))
+    launches = int(replicas.sum_over_ranks(dist, launches))
     b.close()
     # the same cases, one after another, same attempted steps, single-case path
     seq_t = 0.0
@@ -426,26 +425,31 @@ def run_batch(args):
         g.state()
         seq_t += time.perf_counter() - t1
         g.close()
+    seq_t = replicas.max_over_ranks(dist, seq_t)
     if rank == 0:
         shapes = {}
-        for p in ps:
+        for i in range(64):
+            p = configs.random_braid(1000 + i, precision=32)
             k = f"{p.nx}x{p.ny}x{p.nz}"
             shapes[k] = shapes.get(k, 0) + 1
         line = {
             "metric": "cell-RK-stages/s (64 batched random braids, each to weighted residual <= R)",
-            "value": value, "unit": UNIT, "n_gpus": 1, "steps": int(sum(att)), "warmup": args.warmup,
-            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "value": value, "unit": UNIT, "n_gpus": ws, "steps": total_att, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batch64: random braids, seeds 1000..1063, 2-8 blobs, sizes drawn from "
                                    "32^3, 48x48x96, 64x64x128, 96x96x192", "shapes": shapes,
                        "residual_target": args.batch_residual, "max_accepted": args.batch_cycles,
-                       "check_every": 10, "parallelism": "single", "tile_z": tune["tzb"] if tune else 32},
+                       "check_every": 10, "tile_z": tune["tzb"] if tune else 32,
+                       "parallelism": "single" if ws == 1 else f"replicas: case i on rank i mod {ws}"},
             "wall_s": wall, "p50_case_s": secs[len(secs) // 2], "p99_case_s": secs[min(len(secs) - 1, int(0.99 * len(secs)))],
-            "converged": conv, "folded_dtmin": folded, "budget_reached": len(out) - conv - folded,
+            "converged": conv, "folded_dtmin": folded, "budget_reached": 64 - conv - folded,
             "sequential_single_case": {"value": work / seq_t, "unit": UNIT, "seconds": seq_t},
             "gpu_launches": launches, "clocks": ck.summary(),
         }
         print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
     return 0
 
 
