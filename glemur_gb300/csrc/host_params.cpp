@@ -31,8 +31,6 @@ void set_str(char* dst, const char* src) {
     dst[GM_STR_LEN - 1] = '\0';
 }
 
-double round_to(double v, int precision) { return precision == 32 ? (double)(float)v : v; }
-
 }  // namespace
 
 extern "C" int gm_params_default(gm_params* p, int precision) {
