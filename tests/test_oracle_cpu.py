@@ -286,6 +286,33 @@ def test_corner_triangle_currents_on_a_folded_grid():
     assert np.abs(Jt[~tri] - Js[~tri]).max() < 1e-12 * scale
 
 
+def test_currents_on_the_folded_grid_match_reference_kernels():
+    """Every current on the folded grid of tests/golden/folded_currents.npz
+    (made by make_folded.py from the reference's own kernels): the oracle's
+    J to 1e-10 for each jMethod, with the triangular current NaN at exactly
+    the reference's 618 points.  This pins the corner-triangle branches of
+    the quintilateral and triangular currents (current.cu:737-1681), which
+    smooth grids never take, without a GPU."""
+    import make_folded
+    z = np.load(GOLDEN / "folded_currents.npz")
+    for m in make_folded.METHODS:
+        p, B0, x = make_folded.folded_case(m)
+        assert np.array_equal(x, z["x"]) and np.array_equal(B0, z["B0"])
+        o = Oracle(p, z["B0"], z["x"])
+        o.refresh()
+        f = o.get()
+        o.close()
+        Jr, Jo = z[f"J_{m}"], f["J"]
+        nr, no = np.isnan(Jr), np.isnan(Jo)
+        assert np.array_equal(nr, no), (m, int(nr.sum()), int(no.sum()))
+        assert relerr(np.where(no, 0, Jo), np.where(nr, 0, Jr)) < 1e-10, m
+        assert relerr(inner(f["B"]), z["B"]) < 1e-12, m
+        if m == "StokesTri":
+            assert nr.any(-1).sum() == 618
+        else:
+            assert not nr.any(), m
+
+
 # ---- the velocity equation (inertia = T, src/rungeKutta.cu:195-212) -------
 
 def test_inertia_first_stage_from_rest():
