@@ -390,6 +390,42 @@ float rexp<float>(float v) { return expf(v); }
 template <>
 double rexp<double>(double v) { return exp(v); }
 
+// initDistortion, src/init.cu:386-420: the grid, ghosts included; B0 refers
+// to the undistorted grid.  "initShearX" shears y by a sine of x, then x by a
+// sine of the sheared y, both growing linearly in z.  PI is a double constant
+// (global.h:17), so the sine's argument and the product are double and only
+// the stored position rounds to the run precision.  "centerShift" moves y by
+// a Gaussian in x, with the constant 5.0804508111226507 (the ghost-plane
+// correction addDist, boundaries.cu:26-29, uses 0.15366 instead).
+template <typename T>
+void init_distortion(const gm_params* g, T* xb) {
+    const bool shear = strncmp(g->initDist, "initShearX ", 11) == 0;
+    const bool shift = strncmp(g->initDist, "centerShift ", 12) == 0;
+    if (!shear && !shift) return;
+    const double kPi = 3.141592653589793;
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const T dx = (T)g->dx, dy = (T)g->dy, dz = (T)g->dz, Ox = (T)g->Ox, Oy = (T)g->Oy, Oz = (T)g->Oz;
+    const T Lx = (T)g->Lx, Ly = (T)g->Ly;
+    const T A = (T)g->initShearA, B = (T)g->initShearB, K = (T)g->initShearK;
+    for (int k = 0; k < nz + 2; k++) {
+        const T z = dz * (T)(k - 1) + Oz;
+        for (int j = 0; j < ny + 2; j++) {
+            const T y = dy * (T)(j - 1) + Oy;
+            for (int i = 0; i < nx + 2; i++) {
+                const T x = dx * (T)(i - 1) + Ox;
+                T* xp = &xb[3 * ((size_t)i + (size_t)(nx + 2) * ((size_t)j + (size_t)(ny + 2) * (size_t)k))];
+                if (shear) {
+                    xp[1] = (T)(xp[1] - A * std::sin(K * 2 * kPi * (x + Ox - dx / 2) / (Lx + dx)) * z);
+                    const T yy = xp[1];
+                    xp[0] = (T)(xp[0] - B * std::sin(K * 2 * kPi * (yy + Oy - dy / 2) / (Ly + dy)) * z);
+                }
+                if (shift)
+                    xp[1] = (T)(xp[1] + A * rexp<T>(-K * x * x) * (1 - y * y) * (rexp<T>(-1 * z + 1) - 5.0804508111226507));
+            }
+        }
+    }
+}
+
 template <typename T>
 int init_state_t(const gm_params* g, T* B0, T* xb) {
     int mode;
@@ -397,7 +433,9 @@ int init_state_t(const gm_params* g, T* B0, T* xb) {
     else if (strncmp(g->bInit, "homZ ", 5) == 0) mode = 1;
     else if (strncmp(g->bInit, "analytic ", 9) == 0) mode = 2;
     else return gm::fail(GM_EPARAM, "gm_init_state: bInit must be blobs, homZ or analytic");
-    if (strncmp(g->initDist, "none ", 5) != 0) return gm::fail(GM_EPARAM, "gm_init_state: only initDist = none is supported");
+    if (strncmp(g->initDist, "none ", 5) != 0 && strncmp(g->initDist, "initShearX ", 11) != 0 &&
+        strncmp(g->initDist, "centerShift ", 12) != 0)
+        return gm::fail(GM_EPARAM, "gm_init_state: initDist must be none, initShearX or centerShift");
     const int nx = g->nx, ny = g->ny, nz = g->nz;
     const T dx = (T)g->dx, dy = (T)g->dy, dz = (T)g->dz, Ox = (T)g->Ox, Oy = (T)g->Oy, Oz = (T)g->Oz;
     const T ampl = (T)g->ampl, ar = (T)g->ar, az = (T)g->az, phi1 = (T)g->phi1;
@@ -432,6 +470,7 @@ int init_state_t(const gm_params* g, T* B0, T* xb) {
             }
         }
     }
+    init_distortion<T>(g, xb);
     // setPeriHost (boundaries.cu:492-528), order z, y, x.  The grid keeps its
     // identity ghosts: the reference's setGridPeriHost changes no in-bounds
     // value (its shifted-component statements fall outside the inner loop).

@@ -199,7 +199,10 @@ int gm_params_read(gm_params* p, const char* path, int precision);
 
 /* Build the initial B0 and grid xb on the host, ghost layers included, as
  * initState + initDistortion + setPeriHost + setGridPeriHost do.  Supports
- * bInit "blobs", "homZ", "analytic" and initDist "none". */
+ * bInit "blobs", "homZ", "analytic" and initDist "none", "initShearX",
+ * "centerShift".  (gm_create still refuses initShearA/B != 0: the
+ * ghost-plane correction of distorted grids, addDist, is not in the stage
+ * kernels.) */
 int gm_init_state(const gm_params* p, void* B0, void* xb);
 
 /* ---- handle lifecycle (src/memory.cu:10-95, main.cu:181-256) ------------- */

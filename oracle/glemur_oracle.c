@@ -186,6 +186,39 @@ static void set_peri_field(const P* p, R* f) {
                 }
 }
 
+/* initDistortion, src/init.cu:386-420: the grid, ghosts included (B0 refers
+ * to the undistorted grid).  "initShearX" shears y by a sine of x and then x
+ * by a sine of the sheared y, both growing linearly in z, in double
+ * arithmetic as PI is a double constant; "centerShift" moves y by a Gaussian
+ * in x, with a constant (5.08...) that differs from addDist's (0.15366). */
+static void init_distortion(const gm_params* g, const P* p, R* xb) {
+    int i, j, k;
+    const int shear = strncmp(g->initDist, "initShearX ", 11) == 0;
+    const int shift = strncmp(g->initDist, "centerShift ", 12) == 0;
+    if (!shear && !shift) return;
+    for (k = 0; k < p->nz + 2; k++) {
+        R z = p->dz * (R)(k - 1) + p->Oz;
+        for (j = 0; j < p->ny + 2; j++) {
+            R y = p->dy * (R)(j - 1) + p->Oy;
+            for (i = 0; i < p->nx + 2; i++) {
+                R x = p->dx * (R)(i - 1) + p->Ox;
+                R* xp = &xb[3 * GI(p, i, j, k)];
+                if (shear) {
+                    R yy;
+                    xp[1] = (R)(xp[1] - p->initShearA * sin(p->initShearK * 2 * PI_D * (x + p->Ox - p->dx / 2) /
+                                                            (p->Lx + p->dx)) * z);
+                    yy = xp[1];
+                    xp[0] = (R)(xp[0] - p->initShearB * sin(p->initShearK * 2 * PI_D * (yy + p->Oy - p->dy / 2) /
+                                                            (p->Ly + p->dy)) * z);
+                }
+                if (shift)
+                    xp[1] = (R)(xp[1] + p->initShearA * REXP(-p->initShearK * x * x) * (1 - y * y) *
+                                            (REXP(-1 * z + 1) - 5.0804508111226507));
+            }
+        }
+    }
+}
+
 int orc_init_state(const gm_params* g, R* B0, R* xb) {
     P p;
     int i, j, k, b;
@@ -195,7 +228,9 @@ int orc_init_state(const gm_params* g, R* B0, R* xb) {
     else if (strncmp(g->bInit, "homZ ", 5) == 0) mode = 1;
     else if (strncmp(g->bInit, "analytic ", 9) == 0) mode = 2;
     else return GM_EPARAM;
-    if (strncmp(g->initDist, "none ", 5) != 0) return GM_EPARAM;
+    if (strncmp(g->initDist, "none ", 5) != 0 && strncmp(g->initDist, "initShearX ", 11) != 0 &&
+        strncmp(g->initDist, "centerShift ", 12) != 0)
+        return GM_EPARAM;
     for (k = 0; k < p.nz + 2; k++) {
         R z = p.dz * (R)(k - 1) + p.Oz;
         for (j = 0; j < p.ny + 2; j++) {
@@ -226,6 +261,7 @@ int orc_init_state(const gm_params* g, R* B0, R* xb) {
             }
         }
     }
+    init_distortion(g, &p, xb);
     /* src/main.cu:168-169.  setGridPeriHost (boundaries.cu:586-634) leaves the
      * in-bounds grid unchanged: its shifted-component statements sit outside
      * the inner loop (missing braces) and only touch indices past the plane
@@ -347,14 +383,16 @@ static void b_jac_b0(orc_state* s) {
 /* Ghost B and detJac, src/boundaries.cu:11-446                             */
 /* ------------------------------------------------------------------------ */
 
-/* addDist, src/boundaries.cu:11-35 */
+/* addDist, src/boundaries.cu:11-35.  PI is a double constant (global.h:17),
+ * so in FP32 the shear's sine argument, the sine and the product are double
+ * and only the assignment to distY / distX rounds. */
 static R add_dist(const P* p, int i, int j, R z, int l) {
     R x = p->dx * (R)i + p->Ox;
     R y = p->dy * (R)j + p->Oy;
     R distX = 0, distY = 0;
     if (p->initDistCode == 0) {
-        distY = -p->initShearA * RSIN((R)(p->initShearK * 2 * PI_D * (x + p->Ox - p->dx / 2) / (p->Lx + p->dx))) * z;
-        distX = -p->initShearB * RSIN((R)(p->initShearK * 2 * PI_D * (distY + y + p->Oy - p->dy / 2) / (p->Ly + p->dy))) * z;
+        distY = (R)(-p->initShearA * sin(p->initShearK * 2 * PI_D * (x + p->Ox - p->dx / 2) / (p->Lx + p->dx)) * z);
+        distX = (R)(-p->initShearB * sin(p->initShearK * 2 * PI_D * (distY + y + p->Oy - p->dy / 2) / (p->Ly + p->dy)) * z);
     }
     if (p->initDistCode == 1) {
         distX = 0;

@@ -118,6 +118,44 @@ def test_init_state_matches_oracle(prec):
     assert np.array_equal(B0[:, 0, :], B0[:, -2, :]) and np.array_equal(B0[:, -1, :], B0[:, 1, :])
 
 
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("dist", ["initShearX", "centerShift"])
+def test_initial_distortion_matches_oracle_and_formula(prec, dist):
+    """initDistortion (src/init.cu:386-420) on the grid, ghosts included: the
+    library and the oracle agree bit for bit, and the displacement follows
+    the formula (restated in numpy, double arithmetic as the reference's
+    double PI makes it; FP32 stores round once).  B0 is unchanged."""
+    p = configs.braid6(20, 16, 24, precision=prec)
+    p.set_str("initDist", dist)
+    p.initShearA, p.initShearB, p.initShearK = 0.3, 0.2, 1.0
+    B0, xb = configs.init_state(p)
+    B0o, xbo = Oracle.init_state(p)
+    assert np.array_equal(B0, B0o) and np.array_equal(xb, xbo)
+    p0 = configs.braid6(20, 16, 24, precision=prec)
+    B00, xb0 = configs.init_state(p0)
+    assert np.array_equal(B0, B00)
+    dt = np.float32 if prec == 32 else np.float64
+    f = lambda v: dt(v)  # noqa: E731  run-precision parameters
+    X, Y, Z = (xb0[..., c] for c in range(3))    # run precision, as REAL x[i], y[j], z[k]
+    if dist == "initShearX":
+        # sums in the run precision, then double from K * 2 * PI on
+        two_k_pi = np.float64(f(p.initShearK) * dt(2)) * np.pi
+        ey = (Y - np.float64(f(p.initShearA)) * np.sin(two_k_pi * (X + f(p.Ox) - f(p.dx) / dt(2)) /
+                                                       np.float64(f(p.Lx) + f(p.dx))) * Z).astype(dt)
+        ex = (X - np.float64(f(p.initShearB)) * np.sin(two_k_pi * (ey + f(p.Oy) - f(p.dy) / dt(2)) /
+                                                       np.float64(f(p.Ly) + f(p.dy))) * Z).astype(dt)
+        ulp = np.spacing(np.abs(xb).max().astype(dt))
+        assert np.abs(xb[..., 1] - ey).max() <= ulp and np.abs(xb[..., 0] - ex).max() <= ulp
+        assert np.array_equal(xb[..., 2], xb0[..., 2])
+    else:
+        X, Y, Z = (a.astype(np.float64) for a in (X, Y, Z))
+        ey = Y + f(p.initShearA) * np.exp(-f(p.initShearK) * X * X) * (1 - Y * Y) * (np.exp(-Z + 1) - 5.0804508111226507)
+        tol = 1e-4 if prec == 32 else 1e-12
+        assert np.abs(xb[..., 1] - ey).max() / np.abs(ey).max() < tol
+        assert np.array_equal(xb[..., 0], xb0[..., 0]) and np.array_equal(xb[..., 2], xb0[..., 2])
+    assert np.abs(xb - xb0).max() > 0.01
+
+
 def test_create_rejects_unsupported_options():
     lib = _abi.load()
     h = C.c_void_p()

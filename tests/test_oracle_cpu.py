@@ -313,6 +313,48 @@ def test_currents_on_the_folded_grid_match_reference_kernels():
             assert not nr.any(), m
 
 
+def test_sheared_initial_grid_ghost_planes_follow_the_shear():
+    """initDist = "initShearX" (src/init.cu:401-407) with the ghost-plane
+    correction addDist (src/boundaries.cu:11-35, 63-107).  The shear is smooth
+    and linear in z, so the line-tied ghost planes' B and Delta equal central
+    differences of the analytically sheared grid: the second ghost plane and
+    the in-plane neighbours at the 16-wide block edges are extrapolated by
+    addDist.  Without the correction the z-derivative would miss the shear
+    (about 0.3 here).  (For "centerShift" the reference's addDist uses the
+    constant 0.15366 where initDistortion uses 5.0805, so its block-edge
+    neighbours leave the grid; the oracle keeps that as written.)"""
+    p = configs.braid6(20, 16, 24, precision=64)
+    p.set_str("initDist", "initShearX")
+    p.initShearA, p.initShearB, p.initShearK = 0.3, 0.2, 1.0
+    p = configs.derive(p)
+    B0, xb = configs.init_state(p)
+    o = Oracle(p, B0, xb)
+    o.refresh()
+    f = o.get()
+    o.close()
+    A, Bs, K = p.initShearA, p.initShearB, p.initShearK
+
+    def sheared(x, y, z):
+        yy = y - A * np.sin(K * 2 * np.pi * (x + p.Ox - p.dx / 2) / (p.Lx + p.dx)) * z
+        xx = x - Bs * np.sin(K * 2 * np.pi * (yy + p.Oy - p.dy / 2) / (p.Ly + p.dy)) * z
+        return np.stack([xx, yy, z + 0 * x], -1)
+
+    I, Jg = np.meshgrid(np.arange(p.nx), np.arange(p.ny), indexing="xy")
+    x, y = p.dx * I + p.Ox, p.dy * Jg + p.Oy
+    for k in (0, p.nz + 1):
+        zg = p.dz * (k - 1) + p.Oz
+        jac = np.stack([(sheared(x + p.dx, y, zg) - sheared(x - p.dx, y, zg)) / (2 * p.dx),
+                        (sheared(x, y + p.dy, zg) - sheared(x, y - p.dy, zg)) / (2 * p.dy),
+                        (sheared(x, y, zg + p.dz) - sheared(x, y, zg - p.dz)) / (2 * p.dz)], -1)
+        det = np.linalg.det(jac)
+        b0 = B0[k, 1:-1, 1:-1]
+        Bn = np.einsum("...la,...a->...l", jac, b0) / det[..., None]
+        Bn[..., 2] = b0[..., 2]                       # B.n = B0.n on the face
+        assert relerr(f["B"][k, 1:-1, 1:-1], Bn) < 1e-12
+        assert np.abs(f["detJac"][k, 1:-1, 1:-1] - det).max() < 1e-12
+        assert np.abs(det - 1).max() > 0.05            # the shear is felt
+
+
 # ---- the velocity equation (inertia = T, src/rungeKutta.cu:195-212) -------
 
 def test_inertia_first_stage_from_rest():
