@@ -91,6 +91,22 @@ def test_namelist_reader(tmp_path):
     assert p32.dt0 == float(np.float32(3e-4))
 
 
+@pytest.mark.parametrize("dist,code", [("none", 0), ("initShearX", 0), ("centerShift", 1)])
+def test_namelist_reader_initial_distortion(tmp_path, dist, code):
+    """initDist and the initShear parameters (namelist start) and the code the
+    Fortran reader derives from initDist (src/readNamelist.f90:256-262)."""
+    f = tmp_path / "params.in"
+    f.write_text(f'&comp nx = 8; ny = 8; nz = 8 /\n&start initDist = "{dist}"; initShearA = 0.25; '
+                 f'initShearB = 0.5; initShearK = 2 /\n&run /\n&io /\n')
+    p = _abi.GmParams()
+    _abi.check(_abi.load().gm_params_read(p, str(f).encode(), 64), "read")
+    assert p.get_str("initDist") == dist and p.initDistCode == code
+    assert (p.initShearA, p.initShearB, p.initShearK) == (0.25, 0.5, 2.0)
+    h = C.c_void_p()
+    assert _abi.load().gm_create(p, C.byref(h)) == -1       # the stage kernels lack addDist
+    assert b"initShear" in _abi.load().gm_last_error()
+
+
 def test_namelist_reader_rejects_unknown_names(tmp_path):
     f = tmp_path / "params.in"
     f.write_text("&comp nx = 4 /\n&start bogus = 1 /\n&run /\n&io /\n")
