@@ -7,6 +7,9 @@
 // fields the relaxation benchmarks use, and the periodic B0 copy
 // setPeriHost (src/boundaries.cu:492-528).
 #include <cctype>
+#include <cerrno>
+#include <climits>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -203,7 +206,7 @@ class Parser {
             if (i < s_.size() && s_[i] == '(') {
                 size_t e = s_.find(')', i);
                 if (e == std::string::npos) { *err = "unterminated index for " + name; return -1; }
-                index = atoi(s_.substr(i + 1, e - i - 1).c_str());
+                if (!parse_int(s_.substr(i + 1, e - i - 1), &index)) { *err = "bad index for " + name; return -1; }
                 i = e + 1;
                 skip_blank(i);
             }
@@ -225,7 +228,13 @@ class Parser {
                 size_t star = t.quoted ? std::string::npos : t.text.find('*');
                 if (star != std::string::npos && star > 0 &&
                     strspn(t.text.c_str(), "0123456789") == star) {
-                    int r = atoi(t.text.substr(0, star).c_str());
+                    // a repeat count r >= 1 that fits the array (checked before
+                    // expanding it, so a huge count cannot run away)
+                    int r = 0;
+                    if (!parse_int(t.text.substr(0, star), &r) || r < 1 || vals.size() + (size_t)r > (size_t)f->count) {
+                        *err = "bad repeat count or too many values for " + name;
+                        return -1;
+                    }
                     Tok v{t.text.substr(star + 1), false};
                     for (int k = 0; k < r; k++) vals.push_back(v);
                 } else {
@@ -243,6 +252,19 @@ class Parser {
     }
 
   private:
+    // a whole decimal integer within the int32 range (an out-of-range value
+    // is an error, as in the Fortran reader)
+    static bool parse_int(const std::string& text, int* out) {
+        const char* c = text.c_str();
+        while (isspace((unsigned char)*c)) c++;
+        char* e = nullptr;
+        errno = 0;
+        const long long v = strtoll(c, &e, 10);
+        while (e && isspace((unsigned char)*e)) e++;
+        if (e == c || *e || errno == ERANGE || v < INT32_MIN || v > INT32_MAX) return false;
+        *out = (int)v;
+        return true;
+    }
     void skip_blank(size_t& i) {
         while (i < s_.size() && isspace((unsigned char)s_[i])) i++;
     }
@@ -292,10 +314,9 @@ class Parser {
         char* base = reinterpret_cast<char*>(p_) + f->off;
         switch (f->kind) {
             case 'i': {
-                char* e = nullptr;
-                long v = strtol(t.text.c_str(), &e, 10);
-                if (t.quoted || *e) { *err = std::string("bad integer for ") + f->name + ": " + t.text; return false; }
-                reinterpret_cast<int32_t*>(base)[k] = (int32_t)v;
+                int v = 0;
+                if (t.quoted || !parse_int(t.text, &v)) { *err = std::string("bad integer for ") + f->name + ": " + t.text; return false; }
+                reinterpret_cast<int32_t*>(base)[k] = v;
                 return true;
             }
             case 'r': {
@@ -304,9 +325,15 @@ class Parser {
                     if (c == 'd' || c == 'D' || c == 'q' || c == 'Q') c = 'e';
                 char* e = nullptr;
                 double d;
+                errno = 0;
                 if (p_->precision == 32) d = (double)strtof(v.c_str(), &e);  // read straight into REAL
                 else d = strtod(v.c_str(), &e);
-                if (t.quoted || *e) { *err = std::string("bad real for ") + f->name + ": " + t.text; return false; }
+                // an overflowing value is an error, as in the Fortran reader
+                const bool overflow = errno == ERANGE && std::isinf(d);
+                if (t.quoted || *e || e == v.c_str() || overflow) {
+                    *err = std::string("bad real for ") + f->name + ": " + t.text;
+                    return false;
+                }
                 reinterpret_cast<double*>(base)[k] = d;
                 return true;
             }

@@ -107,6 +107,32 @@ def test_namelist_reader_initial_distortion(tmp_path, dist, code):
     assert b"initShear" in _abi.load().gm_last_error()
 
 
+@pytest.mark.parametrize("line,ok", [
+    ("blobYc = 10*0.5", True),                    # a repeat count that fills the array
+    ("blobYc = 2147483647*0.0", False),           # refused before it is expanded
+    ("blobYc = 1,2,3,4,5,6,7,8,9,10,11, 2000000000*0", False),
+    ("blobYc = 0*1.0", False),                    # repeat counts are >= 1
+    ("blobXc(11) = 1", False), ("blobXc(0) = 1", False), ("blobXc(99999999999) = 1", False),
+    ("blobXc( 2 ) = 1", True),
+    ("nBlobs = 2147483647", True), ("nBlobs = 2147483648", False), ("nBlobs = 99999999999999999999", False),
+    ("Lx = 1e400", False), ("Lx = 8.d0", True), ("Lx = 1e-400", True),
+])
+def test_namelist_reader_values_at_the_limits(tmp_path, line, ok):
+    """Repeat counts, indices and numbers at and past their limits: an
+    out-of-range integer or index, an overflowing real and a repeat count that
+    runs past the array are errors (as in the Fortran reader), returned at
+    once instead of being truncated or expanded."""
+    f = tmp_path / "params.in"
+    f.write_text(f"&comp nx = 8; ny = 8; nz = 8 /\n&start nBlobs = 2\n    {line}\n/\n&run /\n&io /\n")
+    p = _abi.GmParams()
+    rc = _abi.load().gm_params_read(p, str(f).encode(), 64)
+    assert (rc == 0) == ok, (line, rc, _abi.load().gm_last_error())
+    if line.startswith("blobYc = 10*"):
+        assert list(p.blobYc[:10]) == [0.5] * 10
+    if line.startswith("nBlobs = 2147483647"):
+        assert p.nBlobs == 2147483647
+
+
 def test_namelist_reader_rejects_unknown_names(tmp_path):
     f = tmp_path / "params.in"
     f.write_text("&comp nx = 4 /\n&start bogus = 1 /\n&run /\n&io /\n")
