@@ -134,6 +134,37 @@ def test_restart_reader_errors(lib, tmp_path):
     assert rc == _abi.GM_EIO
 
 
+def test_restart_reader_refuses_truncated_files(lib, tmp_path):
+    """A save or B0 file cut inside the data the restart reads (the header,
+    the positions, the field) is an error, not a partial state."""
+    p = small(64)
+    f = fields(p, 1)
+    save, b0 = tmp_path / "save.vtk", tmp_path / "B0.vtk"
+    _abi.check(lib.gm_io_write_dump(C.byref(p), str(save).encode(), 1.0, 0.1, _abi.ptr(f["xb"]), _abi.ptr(f["B"]),
+                                    _abi.ptr(f["J"]), _abi.ptr(f["D"]), _abi.ptr(f["cv"]), _abi.ptr(f["cx"]),
+                                    _abi.ptr(f["wm"]), None), "write dump")
+    _abi.check(lib.gm_io_write_b0(C.byref(p), str(b0).encode(), _abi.ptr(f["B"])), "write B0")
+    good_s, good_b = save.read_bytes(), b0.read_bytes()
+    xb = np.zeros_like(f["xb"])
+    B0 = np.zeros_like(f["B"])
+    tt, dd = C.c_double(), C.c_double()
+
+    def read():
+        return lib.gm_io_read_state(C.byref(p), str(save).encode(), str(b0).encode(), _abi.ptr(xb), _abi.ptr(B0),
+                                    C.byref(tt), C.byref(dd), None)
+
+    assert read() == 0
+    np.testing.assert_array_equal(xb, f["xb"])
+    npos = good_s.index(b"POINTS")
+    for cut in (0, 200, npos + 40, npos + 40 + f["xb"].nbytes // 2):
+        save.write_bytes(good_s[:cut])
+        assert read() == _abi.GM_EIO, cut
+    save.write_bytes(good_s)
+    for cut in (0, 100, len(good_b) // 2, len(good_b) - 1):
+        b0.write_bytes(good_b[:cut])
+        assert read() == _abi.GM_EIO, cut
+
+
 @pytest.mark.parametrize("precision", [64, 32])
 def test_time_series_lines(lib, precision):
     p = small(precision)
