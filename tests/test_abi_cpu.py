@@ -214,3 +214,18 @@ def test_configs_blob_mapping():
     assert p.blobTwist[0] == float(np.float32(np.sqrt(2) / 2)) and p.blobTwist[1] < 0
     q = configs.braid2()
     assert q.precision == 64 and q.nCycle == 2000 and q.maxError == 1e-5
+
+
+def test_executable_without_a_gpu_stops_before_any_output(tmp_path):
+    """No CPU fallback: on a machine without a CUDA device the glemur
+    executable stops with the reference's message (src/main.cu:49-56) and a
+    non-zero status, before reading params.in or writing anything."""
+    import subprocess
+    n = C.c_int(0)
+    if _abi.load().gm_device_count(C.byref(n)) == 0 and n.value > 0:
+        pytest.skip("a CUDA device is present")
+    exe = Path(__file__).resolve().parents[1] / "glemur_gb300" / "_lib" / "glemur"
+    r = subprocess.run([str(exe)], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0
+    assert "could not locate CUDA devices" in r.stdout or "no CUDA compatible devices" in r.stdout
+    assert list(tmp_path.iterdir()) == []
