@@ -355,6 +355,43 @@ def test_sheared_initial_grid_ghost_planes_follow_the_shear():
         assert np.abs(det - 1).max() > 0.05            # the shear is felt
 
 
+def test_fp32_storage_error_against_fp64():
+    """What FP32 storage costs the relaxation: the six-blob braid at
+    32x32x64 run 500 accepted steps with FP32 storage (FP64 error norm,
+    errMode = 1) and, to the same physical time, in FP64 (positions
+    interpolated linearly in t between the two FP64 steps around it).  The
+    positions then differ by about 3.4e-3 of the largest displacement and the
+    force-free residual by about 0.2 %.  (The GPU's FP32 path matches the
+    oracle's FP32 build per stage to 1e-5, so this is the figure for it.)"""
+    inner_ = lambda a: a[1:-1, 1:-1, 1:-1].astype(np.float64)  # noqa: E731
+    shape = (32, 32, 64)
+    p32 = configs.braid6(*shape, precision=32)
+    p32.errMode = 1
+    p64 = configs.braid6(*shape, precision=64)
+    o32 = Oracle(p32, *configs.init_state(p32))
+    B064, xb64 = configs.init_state(p64)
+    o64 = Oracle(p64, B064, xb64)
+    o32.run(500)
+    t32 = o32.scalars()["t"]
+    x32 = inner_(o32.get()["xb"])
+    prev_t, prev_x = 0.0, inner_(xb64)
+    while o64.scalars()["t"] < t32:
+        prev_t, prev_x = o64.scalars()["t"], inner_(o64.get()["xb"])
+        assert o64.step(1 << 30) >= 0
+    t64, x64 = o64.scalars()["t"], inner_(o64.get()["xb"])
+    w = (t32 - prev_t) / (t64 - prev_t)
+    x64t = (1 - w) * prev_x + w * x64
+    disp = np.abs(x64 - inner_(xb64)).max()
+    o32.refresh()
+    o64.refresh()
+    r32, r64 = o32.reduce()["residual"], o64.reduce()["residual"]
+    o32.close()
+    o64.close()
+    assert disp > 0.5                                   # the grid has moved
+    assert np.abs(x32 - x64t).max() < 6e-3 * disp       # measured 3.4e-3
+    assert abs(r32 - r64) < 5e-3 * r64                  # measured 1.9e-3
+
+
 # ---- the velocity equation (inertia = T, src/rungeKutta.cu:195-212) -------
 
 def test_inertia_first_stage_from_rest():
