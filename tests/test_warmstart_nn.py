@@ -1,5 +1,6 @@
 """The warm-start network: the CPU oracle of its forward and backward pass is
-pinned by finite differences, and the GPU kernels (tensor-core convolutions,
+pinned by finite differences and by an independent torch restatement, and the
+GPU kernels (tensor-core convolutions,
 pooling, upsampling, loss, Adam) are checked against that oracle on the same
 BF16-rounded weights and inputs."""
 import numpy as np
@@ -45,6 +46,58 @@ def test_oracle_gradients_by_finite_differences():
         lm = uo.loss_grad(uo.forward(P, x)["y"], tgt, 1.0)[0]
         b[o] += h
         assert (lp - lm) / (2 * h) == pytest.approx(G[name][1][o], rel=1e-4, abs=1e-7), (name, "bias")
+
+
+def _torch_unet(P, x):
+    """The network restated with torch.nn.functional in float64 on the CPU,
+    independently of the oracle: conv3d on circularly padded x, y and
+    zero-padded z (the oracle's tap t = 9 (dk+1) + 3 (dj+1) + (di+1) is the
+    weight's (t // 9, t // 3 % 3, t % 3) entry), avg_pool3d, nearest
+    upsampling, skips concatenated after the upsampled path."""
+    import torch
+    import torch.nn.functional as F
+    Wt = {n: (torch.tensor(W.transpose(1, 2, 0).reshape(W.shape[1], W.shape[2], 3, 3, 3), requires_grad=True),
+              torch.tensor(b, requires_grad=True)) for n, (W, b) in P.items()}
+
+    def conv(n, a, act=True):
+        a = F.pad(a, (1, 1, 1, 1, 0, 0), mode="circular")
+        a = F.pad(a, (0, 0, 0, 0, 1, 1))
+        y = F.conv3d(a, *Wt[n])
+        return F.relu(y) if act else y
+
+    up = lambda a: F.interpolate(a, scale_factor=2, mode="nearest")  # noqa: E731
+    t = torch.tensor(x.transpose(3, 0, 1, 2)[None].copy())
+    e0 = conv("e0b", conv("e0a", t))
+    e1 = conv("e1b", conv("e1a", F.avg_pool3d(e0, 2)))
+    bb = conv("bb", conv("ba", F.avg_pool3d(e1, 2)))
+    d1 = conv("d1b", conv("d1a", torch.cat([up(bb), e1], 1)))
+    d0 = conv("d0b", conv("d0a", torch.cat([up(d1), e0], 1)))
+    y = conv("head", d0, act=False)
+    return y, Wt
+
+
+def test_oracle_matches_an_independent_torch_network():
+    """Forward output and every layer's weight and bias gradient of the CPU
+    oracle against the torch restatement (autograd) on a 8x8x8 grid."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(1)
+    P = rand_params(rng)
+    x = rng.normal(size=(8, 8, 8, 3))
+    tgt = rng.normal(size=(8, 8, 8, 3))
+    a = uo.forward(P, x)
+    L0, gy = uo.loss_grad(a["y"], tgt, 0.5)
+    G = uo.backward(P, x, a, gy)
+    y, Wt = _torch_unet(P, x)
+    yn = y[0].detach().numpy().transpose(1, 2, 3, 0)
+    assert relerr(a["y"], yn) < 1e-12
+    e = (y[0].permute(1, 2, 3, 0) - torch.tensor(tgt))[1:-1]
+    loss = 0.5 * (e * e).sum()
+    assert abs(float(loss.detach()) - L0) < 1e-10 * abs(L0)
+    loss.backward()
+    for n, (W, b) in Wt.items():
+        gW = W.grad.numpy().reshape(W.shape[0], W.shape[1], 27).transpose(2, 0, 1)
+        assert relerr(G[n][0], gW) < 1e-10, n
+        assert relerr(G[n][1], b.grad.numpy()) < 1e-10, n
 
 
 def bf16(a):
