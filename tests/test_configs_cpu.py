@@ -46,3 +46,14 @@ def test_random_braids_are_reproducible_and_distinct():
     assert bytes(configs.random_braid(18)) != bytes(a)
     p = configs.random_braid(5, shape=(40, 24, 56))
     assert (p.nx, p.ny, p.nz) == (40, 24, 56)
+
+
+def test_warm_start_seed_ranges_are_disjoint():
+    """Training pairs use seeds TRAIN_SEED0 + i (up to the 4096 braids the
+    configuration names), held-out evaluation EVAL_SEED0 + i (256), and the
+    batched bench 1000..1063: no seed is shared."""
+    from glemur_gb300 import train_warmstart as tw
+    train = set(range(tw.TRAIN_SEED0, tw.TRAIN_SEED0 + 4096))
+    held = set(range(tw.EVAL_SEED0, tw.EVAL_SEED0 + 256))
+    bench = set(range(1000, 1064))
+    assert not train & held and not train & bench and not held & bench
