@@ -47,3 +47,25 @@ def test_peak_and_traffic_lookups():
     p = configs.braid6_large(256, 256, 512, precision=32)
     t, src = bench.traffic_per_launch(p)
     assert abs(t - 80.211 * 256 * 256 * 512) < 1e3
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the reference's arithmetic on the host
+    cores) prints one JSON line with the keys the benchmark contract names,
+    on the same metric, unit and workload as the GPU arm."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, str(bench.ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=bench.ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
+    assert d["config"]["grid"] == [128, 128, 256]
