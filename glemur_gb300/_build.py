@@ -4,10 +4,9 @@
   ``include/glemur.h`` (csrc/*.cu with nvcc for sm_103a, csrc/*.cpp with g++),
   statically linked against the CUDA runtime.
 * ``glemur_gb300/_lib/glemur`` -- the drop-in executable (csrc/driver/).
-* ``oracle/_build/liboracle{32,64}.so`` -- the CPU restatement (test
-  infrastructure), built with -ffp-contract=off so x86 and Arm agree.
-* ``oracle/_ref/`` -- where the reference tree exists: the reference's own
-  kernels as cubins; everywhere: the driver-API launcher for them.
+
+The checker (the CPU oracle and the reference-kernel harness) has its own
+recipe, oracle/build.py.
 
 Every step runs in parallel and is skipped when its outputs are newer than
 its inputs.
@@ -26,7 +25,6 @@ PKG = ROOT / "glemur_gb300"
 CSRC = PKG / "csrc"
 LIB_DIR = PKG / "_lib"
 OBJ_DIR = PKG / "_lib" / "obj"
-ORACLE = ROOT / "oracle"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -103,65 +101,12 @@ def build_driver() -> Path | None:
     return exe
 
 
-def build_oracle() -> list[Path]:
-    out_dir = ORACLE / "_build"
-    out_dir.mkdir(parents=True, exist_ok=True)
-    src = ORACLE / "glemur_oracle.c"
-    outs = []
-    cmds = []
-    for bits in (64, 32):
-        so = out_dir / f"liboracle{bits}.so"
-        outs.append(so)
-        if not _newer(so, [src, INCLUDE / "glemur.h"]):
-            cmds.append(["gcc", "-O3", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
-                         "-shared", f"-DORC_BITS={bits}", str(src), "-o", str(so), "-lm"])
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
-        list(ex.map(_run, cmds))
-    return outs
-
-
-def build_reference_harness() -> list[Path]:
-    """The reference's own kernels as cubins (only where the reference tree
-    exists) and the driver-API launcher that runs them."""
-    ref_dir = ORACLE / "_ref"
-    ref_dir.mkdir(parents=True, exist_ok=True)
-    outs = []
-    ref_src = Path(os.environ.get("GLEMUR_REFERENCE_SRC", "/root/reference/src"))
-    wrapper = ORACLE / "ref" / "ref_kernels.cu"
-    if (ref_src / "rungeKutta.cu").exists():
-        deps = [wrapper] + sorted(ref_src.glob("*.cu")) + sorted(ref_src.glob("*.h"))
-        cmds = []
-        # stock build (nvcc default --fmad=true) and, for FP64, a build without
-        # FMA contraction: two builds of the same reference that round differently
-        for prec, variant, extra in ((64, "", []), (32, "", []), (64, "_nofma", ["--fmad=false"])):
-            cub = ref_dir / f"glemur_ref{prec}{variant}.cubin"
-            outs.append(cub)
-            if not _newer(cub, deps):
-                cmds.append([NVCC, "-cubin"] + ARCH + ["-O3", f"-DPRECISION={prec}", "-I" + str(ref_src), "-w"]
-                            + extra + [str(wrapper), "-o", str(cub)])
-        with cf.ThreadPoolExecutor(max_workers=3) as ex:
-            list(ex.map(_run, cmds))
-    launcher_src = ORACLE / "ref" / "ref_launcher.cpp"
-    so = ref_dir / "libref_launcher.so"
-    if not _newer(so, [launcher_src, INCLUDE / "glemur.h"]):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + str(Path(CUDA_HOME) / "include"),
-              str(launcher_src), "-o", str(so), "-ldl"])
-    outs.append(so)
-    return outs
-
-
 def build_all(verbose: bool = False) -> None:
     LIB_DIR.mkdir(parents=True, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
-        f_lib = ex.submit(build_library)
-        f_orc = ex.submit(build_oracle)
-        f_ref = ex.submit(build_reference_harness)
-        lib = f_lib.result()
-        orc = f_orc.result()
-        ref = f_ref.result()
+    lib = build_library()
     exe = build_driver()
     if verbose:
-        for p in [lib, exe, *orc, *ref]:
+        for p in [lib, exe]:
             if p:
                 print("built", p)
 

@@ -23,7 +23,7 @@ def _lib(bits: int) -> C.CDLL:
         return _libs[bits]
     p = BUILD / f"liboracle{bits}.so"
     if not p.exists():
-        raise RuntimeError(f"{p} missing: run the build (glemur_gb300._build.build_oracle)")
+        raise RuntimeError(f"{p} missing: run the build (oracle/build.py)")
     lib = C.CDLL(str(p))
     vp = C.c_void_p
     lib.orc_create.restype = vp
@@ -46,6 +46,9 @@ def _lib(bits: int) -> C.CDLL:
     lib.orc_run.argtypes = [vp, C.c_int, C.c_int, vp]
     lib.orc_run.restype = C.c_int
     lib.orc_reduce.argtypes = [vp, vp]
+    lib.orc_grid_fields.argtypes = [vp, vp, vp, vp]
+    lib.orc_eps_star.argtypes = [vp]
+    lib.orc_eps_star.restype = C.c_double
     lib.orc_real_bits.restype = C.c_int
     assert lib.orc_real_bits() == bits
     _libs[bits] = lib
@@ -151,6 +154,16 @@ class Oracle:
         u = np.ascontiguousarray(u, dtype=self.dtype)
         self.lib.orc_set_u(self.h, _p(u))
 
+    def grid_fields(self):
+        """Per inner point: signed cell volume, convexity flag, minimum wedge
+        product (inner layout (nz, ny, nx))."""
+        out = [np.zeros(self.I, self.dtype) for _ in range(3)]
+        self.lib.orc_grid_fields(self.h, *(_p(a) for a in out))
+        return dict(cellVol=out[0], convexity=out[1], wedgeMin=out[2])
+
+    def eps_star(self):
+        return self.lib.orc_eps_star(self.h)
+
     def reduce(self):
         from glemur_gb300._abi import GmReduction
         r = GmReduction()
@@ -180,6 +193,9 @@ class RefLauncher:
         lib.ref_get_u.argtypes = [C.c_int, vp]
         lib.ref_get_xnew.argtypes = [vp]
         lib.ref_scalars.argtypes = [vp]
+        lib.ref_grid_fields.argtypes = [vp, vp, vp]
+        lib.ref_eps_star.argtypes = [vp]
+        lib.ref_errors.argtypes = [vp, vp]
         lib.ref_last_error.restype = C.c_char_p
         self.lib = lib
         self.p = params
@@ -254,3 +270,21 @@ class RefLauncher:
         x = np.zeros(self.G + (3,), self.dtype)
         self._chk(self.lib.ref_get_xnew(_p(x)), "ref_get_xnew")
         return x
+
+    def grid_fields(self):
+        """dirCellVol, gridConvexity, gridWedgeMin on the current grid
+        (inner layout (nz, ny, nx))."""
+        out = [np.zeros(self.I, self.dtype) for _ in range(3)]
+        self._chk(self.lib.ref_grid_fields(*(_p(a) for a in out)), "ref_grid_fields")
+        return dict(cellVol=out[0], convexity=out[1], wedgeMin=out[2])
+
+    def eps_star(self):
+        v = C.c_double()
+        self._chk(self.lib.ref_eps_star(C.byref(v)), "ref_eps_star")
+        return v.value
+
+    def errors(self):
+        """(errB_1ez, errXb_XbAn) from the reference's kernels."""
+        a, b = C.c_double(), C.c_double()
+        self._chk(self.lib.ref_errors(C.byref(a), C.byref(b)), "ref_errors")
+        return a.value, b.value

@@ -8,7 +8,7 @@
 // host code and not compiled here, so they are defined below with the
 // declarations of src/global.h:168-172.
 //
-// Built only where the reference tree exists (oracle/ref/build_ref.sh); the
+// Built only where the reference tree exists (oracle/build.py); the
 // cubin is loaded by ref_launcher.cpp through the CUDA driver API.
 #include "global.h"
 

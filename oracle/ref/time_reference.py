@@ -2,7 +2,7 @@
 
 Measurement tooling of the oracle directory, not part of the product: it
 drives the cubin built from the reference sources (oracle/_ref, made by
-build_ref.sh) with the launch sequence and host synchronisations of
+oracle/build.py) with the launch sequence and host synchronisations of
 src/main.cu:259-384, through ref_launcher.cpp's ref_time_steps, on the
 128x128x256 FP32 six-blob braid that bench.py times.  One JSON line:
 

@@ -17,7 +17,9 @@ def pytest_configure(config):
 def _built():
     """Build the native parts once per session (no-op when up to date)."""
     from glemur_gb300 import _build
+    from oracle import build as oracle_build
     _build.build_all()
+    oracle_build.build_all()
 
 
 def relerr(a, b):
