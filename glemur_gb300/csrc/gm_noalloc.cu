@@ -2,13 +2,15 @@
 // device allocation.
 //
 // Some callers cannot allocate device memory at the point where they want the
-// relaxation diagnostics: code running inside a captured CUDA graph or a
-// stream-ordered pipeline that must not synchronise (cudaMalloc and cudaFree
-// synchronise the device or are not capturable), a host callback, or a host
-// application whose GPU memory is fully owned by its own pool allocator.
-// gm_reduce_noalloc gives them the reductions of gm_refresh from B, J and
-// detJac arrays they already hold, with the per-plane partial sums kept in a
-// fixed file-scope device array instead of handle-owned scratch.
+// relaxation diagnostics: an application whose GPU memory is owned by its own
+// pool allocator (a framework that reserved the device's memory up front, so a
+// cudaMalloc from a library fails or escapes the pool's accounting), a
+// stream-ordered pipeline that must not stall (cudaFree, and cudaMalloc in
+// places, synchronise the device), or a service with a fixed memory budget
+// that allocates nothing after start-up.  gm_reduce_noalloc gives them the
+// reductions of gm_refresh from B, J and detJac arrays they already hold, with
+// the per-plane partial sums kept in a fixed file-scope device array instead
+// of handle-owned scratch.
 #include <cuda_runtime.h>
 
 #include <float.h>
@@ -30,9 +32,23 @@ enum { S_CROSS = 0, S_JB, S_PW, S_B2W, S_E1, M_JXBB2, M_B, M_J, N_DET };
 __device__ __align__(256) double g_plane_partials[GM_NOALLOC_MAX_PLANES * kFields];
 
 constexpr int kMaxDevices = 64;
-std::once_flag g_once[kMaxDevices];
+// device address of g_plane_partials per device, set by the first successful
+// lookup (a failed lookup is not cached: the next call tries again)
+std::mutex g_setup_mutex;
 double* g_scratch[kMaxDevices] = {nullptr};
-cudaError_t g_setup_err[kMaxDevices] = {cudaSuccess};
+
+// The device address of the scratch array on device `dev` (current).
+cudaError_t scratch_address(int dev, double** out) {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch[dev]) {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_plane_partials);
+        if (e != cudaSuccess) return e;
+        g_scratch[dev] = static_cast<double*>(ptr);
+    }
+    *out = g_scratch[dev];
+    return cudaSuccess;
+}
 
 // One CTA per z-plane: inner points of plane k and, for line-tied faces, the
 // ghost-plane detJac values next to them (the minDetJac of gm_refresh).
@@ -135,25 +151,27 @@ extern "C" int gm_reduce_noalloc(const gm_params* p, const void* B, const void* 
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return gm::fail(GM_EPARAM, "gm_reduce_noalloc: device index out of range");
+    // An error the caller left pending would otherwise be read back below as
+    // this call's launch failure: report it, and leave it pending.
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return gm::fail(GM_ECUDA, std::string("gm_reduce_noalloc: a CUDA error was pending before the call: ") +
+                                      cudaGetErrorString(e));
     // First call on a device: resolve the device address of the scratch array
-    // with that device current.
-    std::call_once(g_once[dev], [dev]() {
-        void* ptr = nullptr;
-        g_setup_err[dev] = cudaGetSymbolAddress(&ptr, g_plane_partials);
-        g_scratch[dev] = static_cast<double*>(ptr);
-    });
-    if (g_setup_err[dev] != cudaSuccess || !g_scratch[dev])
-        return gm::fail(GM_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(g_setup_err[dev]));
+    // with that device current (retried on the next call if it fails).
+    double* scratch = nullptr;
+    e = scratch_address(dev, &scratch);
+    if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const double N = (double)p->nx * p->ny * p->nz;
     if (p->precision == 32)
         k_plane_partials<float><<<p->nz, 256, 0, s>>>((const float*)B, (const float*)J, (const float*)detJac, p->nx,
-                                                       p->ny, p->nz, p->xPeri, p->yPeri, p->zPeri, g_scratch[dev]);
+                                                       p->ny, p->nz, p->xPeri, p->yPeri, p->zPeri, scratch);
     else
         k_plane_partials<double><<<p->nz, 256, 0, s>>>((const double*)B, (const double*)J, (const double*)detJac,
                                                         p->nx, p->ny, p->nz, p->xPeri, p->yPeri, p->zPeri,
-                                                        g_scratch[dev]);
-    k_plane_final<<<1, 32, 0, s>>>(g_scratch[dev], p->nz, N, p->dx * p->dy * p->dz, out);
+                                                        scratch);
+    k_plane_final<<<1, 32, 0, s>>>(scratch, p->nz, N, p->dx * p->dy * p->dz, out);
     e = cudaGetLastError();
     if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("gm_reduce_noalloc launch: ") + cudaGetErrorString(e));
     return GM_OK;

@@ -321,10 +321,11 @@ int gm_download_u(gm_handle* h, int which, void* u);
 /* The reductions of gm_refresh computed from fields the caller already holds
  * on the device, without allocating any device memory.  This entry point has
  * no counterpart in the reference.  It is for callers that cannot allocate at
- * the point where they want diagnostics: code inside a captured CUDA graph or
- * a stream-ordered pipeline (cudaMalloc/cudaFree synchronise or cannot be
- * captured), host callbacks, or applications whose device memory belongs to
- * their own allocator.
+ * the point where they want diagnostics: applications whose device memory
+ * belongs to their own pool allocator (a cudaMalloc from a library fails or
+ * escapes the pool's accounting), stream-ordered pipelines that must not
+ * stall (cudaFree, and cudaMalloc in places, synchronise the device), and
+ * services that allocate nothing after start-up.
  *   B, J, detJac: DEVICE arrays of REAL in the layouts gm_download returns
  *                 (B ghosted AoS, J inner AoS, detJac ghosted scalar).
  *   out:          DEVICE pointer to one gm_reduction; wedgeMin, convex and
@@ -337,9 +338,11 @@ int gm_download_u(gm_handle* h, int which, void* u);
  * rejected with GM_EPARAM.  Each call overwrites every partial it reads, so
  * nothing has to be cleared between calls, but all calls share that array:
  * calls that overlap on the GPU (concurrent streams) race.  The first call on
- * a device looks up the array's device address with that device current;
- * make that first call before any stream capture.  No cudaMalloc, cudaFree or
- * allocating library routine is called. */
+ * a device looks up the array's device address with that device current (a
+ * failed lookup is retried by the next call); make that first call before any
+ * stream capture.  A CUDA error left pending by the caller is reported
+ * (GM_ECUDA) and left pending, and nothing is launched.  No cudaMalloc,
+ * cudaFree or allocating library routine is called. */
 int gm_reduce_noalloc(const gm_params* p, const void* B, const void* J, const void* detJac,
                       gm_reduction* out, void* stream);
 

@@ -1,9 +1,10 @@
 """The allocation-free reduction entry point, gm_reduce_noalloc.
 
 Callers that cannot allocate device memory where they want diagnostics
-(inside graph capture or a no-sync stream pipeline, in host callbacks, or
-under their own allocator) pass fields they already hold; the entry point
-keeps its partial sums in a fixed device array.  Checked through the C-ABI
+(applications whose device memory belongs to their own pool allocator,
+stream pipelines that must not stall on cudaMalloc/cudaFree, services that
+allocate nothing after start-up) pass fields they already hold; the entry
+point keeps its partial sums in a fixed device array.  Checked through the C-ABI
 against gm_refresh on the same state, on two calls in a row."""
 import ctypes as C
 
