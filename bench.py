@@ -173,13 +173,23 @@ def traffic_per_launch(p):
     return float(e["bytes_per_point"]) * n, f"{e.get('source')}, scaled to {n} inner points"
 
 
-def cpu_baseline(p, seconds=20.0):
+def oracle_workload_params(precision=32):
+    """The workload's parameters from the checker's own builder (oracle/params.py),
+    byte-identical to workload_params() but without loading the library."""
+    from oracle import params as op
+    if WORKLOAD == "large":
+        return op.braid6_large(*LARGE_SHAPE, precision=precision)
+    return op.braid6(*SHAPE, precision=precision)
+
+
+def cpu_baseline(seconds=20.0):
     """The oracle (C restatement of the reference arithmetic, all host cores)
-    on a bounded sample of the workload: whole attempted steps on the full grid."""
-    from glemur_gb300 import configs
+    on a bounded sample of the workload: whole attempted steps on the full grid.
+    Parameters and initial state come from the oracle itself."""
     from oracle.pyoracle import Oracle
+    p = oracle_workload_params()
     cores = os.cpu_count() or 1
-    B0, xb = configs.init_state(p)
+    B0, xb = Oracle.init_state(p)
     o = Oracle(p, B0, xb)
     o.step()                      # warm-up (first-touch of the arrays)
     t0 = time.perf_counter()
@@ -197,14 +207,14 @@ def cpu_baseline(p, seconds=20.0):
 
 
 def run_reference(args):
-    """--impl reference: the reference arithmetic on the host cores."""
-    dist, rank, ws = dist_init()
-    if rank != 0:
+    """--impl reference: the reference arithmetic on the host cores.  Nothing
+    of the product library is loaded: parameters, initial state and the
+    relaxation all come from the oracle.  Under torchrun rank 0 alone runs."""
+    if int(os.environ.get("RANK", "0")) != 0:
         return 0
-    from glemur_gb300 import configs
     from oracle.pyoracle import Oracle
-    p = workload_params()
-    B0, xb = configs.init_state(p)
+    p = oracle_workload_params()
+    B0, xb = Oracle.init_state(p)
     o = Oracle(p, B0, xb)
     for _ in range(args.warmup):
         o.step()
@@ -224,8 +234,9 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": n,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / n, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(p, {"impl_note": "reference relaxation arithmetic on host cores (C restatement; "
-                                                  "the reference itself is CUDA-only)"}),
+        "config": workload_config(p),
+        "impl_note": "reference relaxation arithmetic on host cores (C restatement in oracle/; the reference "
+                     "itself is CUDA-only); parameters and initial state from the oracle, no product library loaded",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{n} attempted steps of the full grid (bounded at {budget:.0f} s)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -343,16 +354,16 @@ def run_gpu(args):
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
-        cb = cpu_baseline(p, seconds=args.cpu_seconds)
+        cb = cpu_baseline(seconds=args.cpu_seconds)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / max(ran, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(p, {"attempted": st["nAttempted"], "accepted": st["timeIndex"],
-                                          "timed_steps_ran": ran,
-                                          "tile_z": tune["tz"] if tune else None}),
+            "config": workload_config(p),
+            "run": {"attempted": st["nAttempted"], "accepted": st["timeIndex"], "timed_steps_ran": ran,
+                    "tile_z": tune["tz"] if tune else None},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": peak_kind, "kernel": "k_stage (one RK stage)",

@@ -69,3 +69,18 @@ def test_reference_arm_prints_the_contract_line():
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert d["config"]["grid"] == [128, 128, 256]
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm builds its parameters and initial state with the
+    oracle: the product library is never loaded in that process."""
+    import subprocess
+    import sys
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3'];\n"
+            "try:\n    runpy.run_path('bench.py', run_name='__main__')\nexcept SystemExit:\n    pass\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('LOADED_LIBGLEMUR' if 'libglemur.so' in maps else 'CLEAN')\n"
+            "print('IMPORTED_PACKAGE' if any(m.startswith('glemur_gb300') for m in sys.modules) else 'NO_PACKAGE')")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=bench.ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "CLEAN" in r.stdout and "NO_PACKAGE" in r.stdout, r.stdout[-500:]
