@@ -35,11 +35,13 @@ typedef float R;
 #define REXP expf
 #define RSIN sinf
 #define RSQRT sqrtf
+#define RABS fabsf
 #else
 typedef double R;
 #define REXP exp
 #define RSIN sin
 #define RSQRT sqrt
+#define RABS fabs
 #endif
 
 #define PI_D 3.141592653589793
@@ -1468,6 +1470,88 @@ void orc_reduce(const orc_state* s, gm_reduction* r) {
     r->convex = convex;
     r->errB_1ez = sqrt(e1) / sqrt((double)s->N);
     r->errXb_XbAn = sqrt(e2) / sqrt((double)s->N);
+}
+
+/* Grid-quality fields at the inner points, inner layout i + nx (j + ny k):
+ * - cellVol: the signed volume of the cell towards +x, +y, +z,
+ *   ((x(i+1) - x) x (x(j+1) - x)) . (x(k+1) - x)  (dirCellVol, src/maths.cu:443-493);
+ * - convexity: +1, or -1 where a corner wedge has the wrong orientation
+ *   (gridConvexity, src/maths.cu:573-643);
+ * - wedgeMin: the smallest of the 8 corner wedge products with the sign
+ *   convention of gridWedgeMin (src/maths.cu:497-569).
+ * The last two come from wedge_min_at, which the reductions also use.  Any
+ * output pointer may be NULL. */
+void orc_grid_fields(const orc_state* s, R* cellVol, R* convexity, R* wedgeMin) {
+    const P* p = &s->p;
+    int k;
+#pragma omp parallel for schedule(static)
+    for (k = 0; k < p->nz; k++) {
+        int i, j, l;
+        for (j = 0; j < p->ny; j++)
+            for (i = 0; i < p->nx; i++) {
+                const size_t q = II(p, i, j, k);
+                const R* x = s->xb;
+                const size_t gc = 3 * GI(p, i + 1, j + 1, k + 1);
+                if (cellVol) {
+                    R d1[3], d2[3], d3[3], c[3];
+                    const size_t g1 = 3 * GI(p, i + 2, j + 1, k + 1), g2 = 3 * GI(p, i + 1, j + 2, k + 1),
+                                 g3 = 3 * GI(p, i + 1, j + 1, k + 2);
+                    for (l = 0; l < 3; l++) {
+                        d1[l] = x[g1 + l] - x[gc + l];
+                        d2[l] = x[g2 + l] - x[gc + l];
+                        d3[l] = x[g3 + l] - x[gc + l];
+                    }
+                    cross3(d1, d2, c);
+                    cellVol[q] = dot3(c, d3);
+                }
+                if (convexity || wedgeMin) {
+                    int cv;
+                    const R wm = wedge_min_at(s, i, j, k, &cv);
+                    if (convexity) convexity[q] = (R)cv;
+                    if (wedgeMin) wedgeMin[q] = wm;
+                }
+            }
+    }
+}
+
+/* The force-free parameter eps* (src/maths.cu:203-290, driven by
+ * src/diagnostics.cu:32-47): along the central column i = nx/2, j = ny/2,
+ * a_k = (J.B)/(B.B) in REAL (JB_B2) and z_k the grid's z coordinate; eps* is
+ * the largest sqrt(2) |(a_n - a_p) / (z_n - z_p)| over the pairs with
+ * z_n != z_p (0 for the others), the product formed in double and stored in
+ * REAL, then findDevMax over the nz x nz values (NaN never wins,
+ * src/maths.cu:58-97).  The reference's kernel covers every pair when
+ * nz <= 256 or nz is a multiple of 256, its block size; for other nz its
+ * second block reads shared memory that no thread wrote, and all pairs are
+ * taken here. */
+double orc_eps_star(const orc_state* s) {
+    const P* p = &s->p;
+    const int i = p->nx / 2, j = p->ny / 2, nz = p->nz;
+    R* a = (R*)malloc(sizeof(R) * (size_t)nz);
+    R* z = (R*)malloc(sizeof(R) * (size_t)nz);
+    R m = 0;
+    int n, q;
+    if (!a || !z) {
+        free(a);
+        free(z);
+        return NAN;
+    }
+    for (n = 0; n < nz; n++) {
+        const size_t g = GI(p, i + 1, j + 1, n + 1), l = II(p, i, j, n);
+        const R* Bv = &s->B[3 * g];
+        const R* Jv = &s->J[3 * l];
+        a[n] = dot3(Jv, Bv) / dot3(Bv, Bv);
+        z[n] = s->xb[3 * g + 2];
+    }
+    for (q = 0; q < nz; q++)
+        for (n = 0; n < nz; n++) {
+            R v = 0;
+            if (z[n] != z[q]) v = (R)(1.414213562373095 * (double)RABS((a[n] - a[q]) / (z[n] - z[q])));
+            if (v > m) m = v;
+        }
+    free(a);
+    free(z);
+    return (double)m;
 }
 
 int orc_real_bits(void) { return ORC_BITS; }

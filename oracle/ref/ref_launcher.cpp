@@ -214,6 +214,13 @@ const char* kname(const char* base, int prec) {
     else if (b == "setGridPeriFace") s = "_Z15setGridPeriFaceP" + r + "i";
     else if (b == "xNewStar") s = "_Z8xNewStar7VarsDeviii";
     else if (b == "maxBlock") s = "_Z8maxBlockP" + r + "S_i";
+    else if (b == "dirCellVol") s = "_Z10dirCellVolP" + r + "S_iii";
+    else if (b == "gridConvexity") s = "_Z13gridConvexityP" + r + "S_iii";
+    else if (b == "gridWedgeMin") s = "_Z12gridWedgeMinP" + r + "S_iii";
+    else if (b == "JB_B2") s = "_Z5JB_B2P" + r + "S_S_";
+    else if (b == "epsilonStar") s = "_Z11epsilonStarP" + r + "S_S_i";
+    else if (b == "B_1ez") s = "_Z5B_1ezP" + r + "S_";
+    else if (b == "xb_XbAn") s = "_Z7xb_XbAnP" + r + "S_";
     return s.c_str();
 }
 
@@ -601,6 +608,123 @@ int ref_get_xnew(void* x) {
     SYNC();
     CK(D.MemcpyDtoH(x, S.d.xb_new, 3 * S.NG * S.rs));
     return 0;
+}
+
+// The per-point grid fields of prepareDump (src/diagnostics.cu:154-190):
+// dirCellVol, gridConvexity and gridWedgeMin on the current grid, with the
+// run's block and grid shapes and dynamic shared-memory sizes, copied to the
+// host arrays (inner layout, REAL; any pointer may be NULL).
+int ref_grid_fields(void* cellVol, void* convexity, void* wedgeMin) {
+    const int b0 = S.block[0], b1 = S.block[1], b2 = S.block[2];
+    const size_t vi = S.N * S.rs;
+    CUdeviceptr out = 0;
+    CK(D.MemAlloc(&out, vi));
+    int rc = 0;
+    struct Job { const char* name; void* host; int pad; unsigned smem; };
+    const Job jobs[3] = {
+        {"dirCellVol", cellVol, 1, (unsigned)((3 * (b0 + 1) * (b1 + 1) * (b2 + 1) + b0 * b1 * b2) * S.rs)},
+        {"gridConvexity", convexity, 2, (unsigned)((3 * (b0 + 2) * (b1 + 2) * (b2 + 2) + b0 * b1 * b2) * S.rs)},
+        {"gridWedgeMin", wedgeMin, 2, (unsigned)(3 * (b0 + 2) * (b1 + 2) * (b2 + 2) * S.rs)}};
+    for (const Job& j : jobs) {
+        if (!j.host) continue;
+        CUfunction f;
+        if ((rc = get_fn(&f, j.name))) break;
+        int dX = b0 + j.pad, dY = b1 + j.pad, dZ = b2 + j.pad;
+        CUdeviceptr xb = S.d.xb;
+        void* a[5] = {&xb, &out, &dX, &dY, &dZ};
+        if ((rc = launch(f, dgrid(), dblock(), j.smem, a))) break;
+        if (D.CtxSynchronize() != CUDA_SUCCESS || D.MemcpyDtoH(j.host, out, vi) != CUDA_SUCCESS) {
+            g_err = std::string("ref_grid_fields: ") + j.name;
+            rc = -3;
+            break;
+        }
+    }
+    D.MemFree(out);
+    return rc;
+}
+
+// eps* as src/diagnostics.cu:32-47 computes it: JB_B2, then epsilonStar
+// over the nz x nz pairs, then findDevMax.  The reference's kernel covers
+// every pair only for nz <= 256 or a multiple of 256 (its block size), so
+// other nz are refused.
+int ref_eps_star(double* out) {
+    const int nz = S.gp.nz;
+    if (!(nz <= 256 || nz % 256 == 0)) { g_err = "ref_eps_star: nz must be <= 256 or a multiple of 256"; return -1; }
+    CUfunction fjb, feps;
+    int rc = 0;
+    if ((rc = get_fn(&fjb, "JB_B2")) || (rc = get_fn(&feps, "epsilonStar"))) return rc;
+    CUdeviceptr jb = 0, eps = 0;
+    CK(D.MemAlloc(&jb, (size_t)nz * S.rs));
+    if (D.MemAlloc(&eps, (size_t)nz * nz * S.rs) != CUDA_SUCCESS) { D.MemFree(jb); g_err = "ref_eps_star: alloc"; return -3; }
+    CUdeviceptr B = S.d.B, J = S.d.J, xb = S.d.xb;
+    int dimZ = 256;
+    void* a1[3] = {&B, &J, &jb};
+    void* a2[4] = {&xb, &jb, &eps, &dimZ};
+    const unsigned nb = (unsigned)((nz - 1) / 256 + 1);
+    rc = launch(fjb, Dim{nb, 1, 1}, Dim{256, 1, 1}, 0, a1);
+    if (!rc && D.CtxSynchronize() != CUDA_SUCCESS) { g_err = "ref_eps_star: JB_B2"; rc = -3; }
+    if (!rc) rc = launch(feps, Dim{nb, 1, 1}, Dim{256, 1, 1}, (unsigned)(512 * 2 * S.rs), a2);
+    if (!rc && D.CtxSynchronize() != CUDA_SUCCESS) { g_err = "ref_eps_star: epsilonStar"; rc = -3; }
+    // findDevMax uses the launcher's own scratch, sized for the step's block
+    // maxima: reduce here when the pair count fits it, else on the host
+    if (!rc) {
+        const size_t cnt = (size_t)nz * nz;
+        const size_t nblk = (size_t)S.grid[0] * S.grid[1] * S.grid[2];
+        if (cnt <= nblk) {
+            rc = find_dev_max(eps, (int)cnt, out);
+        } else {
+            std::vector<double> h(cnt);
+            if (S.prec == 64) {
+                if (D.MemcpyDtoH(h.data(), eps, cnt * 8) != CUDA_SUCCESS) rc = -3;
+            } else {
+                std::vector<float> hf(cnt);
+                if (D.MemcpyDtoH(hf.data(), eps, cnt * 4) != CUDA_SUCCESS) rc = -3;
+                for (size_t q = 0; q < cnt; q++) h[q] = hf[q];
+            }
+            double m = 0;   // every value is >= 0; NaN never wins (maxBlock's compare)
+            for (double v : h)
+                if (v > m) m = v;
+            *out = m;
+            if (rc) g_err = "ref_eps_star: copy";
+        }
+    }
+    D.MemFree(jb);
+    D.MemFree(eps);
+    return rc;
+}
+
+// errB_1ez and errXb_XbAn as src/diagnostics.cu:51-71 form them: the
+// kernels' per-block partial sums (B_1ez, xb_XbAn, 256 threads), summed on
+// the host in double, then sqrt(sum) / sqrt(N).
+int ref_errors(double* errB, double* errXb) {
+    CUfunction fb, fx;
+    int rc = 0;
+    if ((rc = get_fn(&fb, "B_1ez")) || (rc = get_fn(&fx, "xb_XbAn"))) return rc;
+    const unsigned nb = (unsigned)((S.N - 1) / 256 + 1);
+    CUdeviceptr part = 0;
+    CK(D.MemAlloc(&part, (size_t)nb * S.rs));
+    double* outs[2] = {errB, errXb};
+    CUfunction fs[2] = {fb, fx};
+    CUdeviceptr src[2] = {S.d.B, S.d.xb};
+    for (int q = 0; q < 2 && !rc; q++) {
+        void* a[2] = {&src[q], &part};
+        rc = launch(fs[q], Dim{nb, 1, 1}, Dim{256, 1, 1}, 0, a);
+        if (rc) break;
+        if (D.CtxSynchronize() != CUDA_SUCCESS) { g_err = "ref_errors: kernel"; rc = -3; break; }
+        double sum = 0;
+        if (S.prec == 64) {
+            std::vector<double> h(nb);
+            if (D.MemcpyDtoH(h.data(), part, (size_t)nb * 8) != CUDA_SUCCESS) { rc = -3; break; }
+            for (double v : h) sum += v;
+        } else {
+            std::vector<float> h(nb);
+            if (D.MemcpyDtoH(h.data(), part, (size_t)nb * 4) != CUDA_SUCCESS) { rc = -3; break; }
+            for (float v : h) sum += v;
+        }
+        *outs[q] = sqrt(sum) / sqrt((double)S.N);
+    }
+    D.MemFree(part);
+    return rc;
 }
 
 void ref_scalars(double* out) {

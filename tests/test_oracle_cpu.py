@@ -448,3 +448,54 @@ def test_inertia_damping_removes_velocity_without_force():
     dx = inner(o.get()["xb"])[..., 0] - inner(xb)[..., 0]
     assert np.allclose(dx, 0.01 * (1 - np.exp(-2.0 * t)) / 2.0, rtol=1e-10, atol=0)
     o.close()
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_diagnostics_match_reference_kernels(precision):
+    """The oracle's per-point grid fields (dirCellVol, gridConvexity,
+    gridWedgeMin), eps* and the analytic-error norms against
+    tests/golden/diagnostics_f{64,32}.npz, made by make_diagnostics.py from
+    the reference's own kernels on a folded grid, a relaxed braid and (FP64)
+    the relaxed analytic field."""
+    from glemur_gb300._abi import GmParams
+    z = np.load(GOLDEN / f"diagnostics_f{precision}.npz")
+    tol = 1e-12 if precision == 64 else 1e-5
+    kinds = ("folded", "braid", "analytic") if precision == 64 else ("folded", "braid")
+    for kind in kinds:
+        p = GmParams.from_buffer_copy(z[f"{kind}_params"].tobytes())
+        o = Oracle(p, z[f"{kind}_B0"], z[f"{kind}_x"])
+        o.refresh()
+        g = o.grid_fields()
+        for key in ("cellVol", "wedgeMin"):
+            assert relerr(g[key], z[f"{kind}_{key}"]) < tol, (kind, key)
+        assert np.array_equal(g["convexity"], z[f"{kind}_convexity"]), kind
+        eps, e1, e2 = z[f"{kind}_scalars"]
+        assert abs(o.eps_star() - eps) <= tol * eps, (kind, o.eps_star(), eps)
+        r = o.reduce()
+        assert abs(r["errB_1ez"] - e1) <= tol * e1, (kind, r["errB_1ez"], e1)
+        if kind == "analytic":
+            assert abs(r["errXb_XbAn"] - e2) <= tol * e2, (kind, r["errXb_XbAn"], e2)
+        if kind == "folded":
+            assert (g["convexity"] < 0).any()
+        o.close()
+
+
+def test_grid_fields_known_answers():
+    """On the identity grid every cell volume is dx dy dz, every cell is
+    convex and every corner wedge is dx dy dz in gridWedgeMin's sign
+    convention; under a uniform shear x += s y the volumes stay dx dy dz."""
+    p = configs.braid2(10, 9, 12, precision=64)
+    p.xPeri = p.yPeri = p.zPeri = 0
+    p = configs.derive(p)
+    B0, xb = configs.init_state(p)
+    v = p.dx * p.dy * p.dz
+    o = Oracle(p, B0, xb)
+    g = o.grid_fields()
+    assert np.allclose(g["cellVol"], v, rtol=1e-12) and np.all(g["convexity"] == 1)
+    assert np.allclose(g["wedgeMin"], v, rtol=1e-12)
+    o.close()
+    xs = xb.copy()
+    xs[..., 0] += 0.3 * xs[..., 1]
+    o = Oracle(p, B0, xs)
+    assert np.allclose(o.grid_fields()["cellVol"], v, rtol=1e-10)
+    o.close()
