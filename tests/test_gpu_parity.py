@@ -6,8 +6,8 @@ Tolerances (max |a-b| / max |b| per field): FP64 1e-12 after one stage
 the first dt updates are driven by rounding noise (the error norm of a
 dt0 = 3e-4 step is ~1e-15 against a true ~1e-18), and from about 1300
 attempts on the braid2 controller is chaotic, so run-level FP64 checks use
-the tolerances measured for two builds that differ only in rounding (see
-test_braid2_fp64_2000_steps_vs_reference_kernels)."""
+the spread measured between two builds of the reference that differ only
+in rounding (see test_braid2_fp64_2000_steps_vs_reference_kernels)."""
 import numpy as np
 import pytest
 
@@ -155,51 +155,107 @@ def test_run_matches_oracle(name):
     assert red["convex"] == ro["convex"]
 
 
-def _ref_state(p, B0, xb, n, variant=""):
+def _ref_trace(p, B0, xb, marks, variant=""):
+    """The reference's own kernels (one build) at each accepted-step mark."""
     r = RefLauncher(p, B0, xb, variant=variant)
-    r.run(n, max_attempts=100000)
-    f, s = r.get(), r.scalars()
-    r.close()
-    return f, s
+    out = []
+    try:
+        for m in marks:
+            r.run(m, max_attempts=100000)
+            out.append((r.get(), r.scalars()))
+    finally:
+        r.close()
+    return out
+
+
+def _lib_trace(p, B0, xb, marks):
+    g = Relaxation(p)
+    g.upload(xb, B0)
+    out, done = [], 0
+    for m in marks:
+        s = g.run(m - done)
+        done = m
+        g.refresh()
+        out.append((g.download(), s))
+    g.close()
+    return out
+
+
+def _field_errs(f, r):
+    return dict(x=relerr(inner(f["xb"]), inner(r["xb"])), B=relerr(inner(f["B"]), inner(r["B"])),
+                J=relerr(f["J"], r["J"]))
+
+
+def run_vs_reference_kernels(precision, marks):
+    """x, B and J of the library after each mark of accepted steps against the
+    reference's stock build, and the spread between the reference's stock
+    and --fmad=false builds (two builds that differ only in rounding) at the
+    same marks.  Returns rows of (mark, ours, spread, attempts)."""
+    p = configs.braid2(precision=precision)
+    p.errMode = 0          # the reference's arithmetic of the error norm and controller
+    p = configs.derive(p)
+    B0, xb = configs.init_state(p)
+    lib = _lib_trace(p, B0, xb, marks)
+    ref = _ref_trace(p, B0, xb, marks)
+    nof = _ref_trace(p, B0, xb, marks, "_nofma")
+    rows = []
+    for m, (fl, sl), (fr, sr), (fn, sn) in zip(marks, lib, ref, nof):
+        assert sl["timeIndex"] == sr["timeIndex"] == sn["timeIndex"] == m
+        ours, spread = _field_errs(fl, fr), _field_errs(fn, fr)
+        att = (sl["nAttempted"], sr["nAttempted"], sn["nAttempted"])
+        print(f"fp{precision} {m:5d} accepted: attempts lib/ref/ref-nofma {att}; library vs reference "
+              + " ".join(f"{k} {v:.2e}" for k, v in ours.items()) + "; reference fma vs nofma "
+              + " ".join(f"{k} {v:.2e}" for k, v in spread.items()))
+        rows.append((m, ours, spread, att))
+    return rows
 
 
 def test_braid2_fp64_2000_steps_vs_reference_kernels():
-    """The 32x32x64 two-blob braid in FP64 (config of 2000 accepted steps)
-    against the reference's own kernels.
+    """The 32x32x64 two-blob braid in FP64, 2000 accepted steps (the
+    configuration the relative-error bound 1e-10 is stated for), against the
+    reference's own kernels.
 
-    x, B and J agree to 1e-10 / 1e-9 / 1e-8 over the first 500 accepted steps.
-    After ~1300 attempts the step-size controller becomes chaotic and any
-    rounding difference grows; at 2000 steps the comparison is against the
-    spread between two builds of the reference itself (stock and
-    --fmad=false): the library must stay within 10x that spread."""
-    p = configs.braid2(precision=64)
-    p.errMode = 0
-    p = configs.derive(p)
-    B0, xb = configs.init_state(p)
-    g = Relaxation(p)
-    g.upload(xb, B0)
-    g.run(500)
-    g.refresh()
-    f = g.download()
-    fr, sr = _ref_state(p, B0, xb, 500)
-    assert relerr(inner(f["xb"]), inner(fr["xb"])) < 1e-10
-    assert relerr(inner(f["B"]), inner(fr["B"])) < 1e-9
-    assert relerr(f["J"], fr["J"]) < 1e-8
-    sg = g.run(1500)
-    g.refresh()
-    f = g.download()
-    fr, sr = _ref_state(p, B0, xb, 2000)
-    fn, sn = _ref_state(p, B0, xb, 2000, variant="_nofma")
-    assert sg["timeIndex"] == sr["timeIndex"] == sn["timeIndex"] == 2000
-    assert abs(sg["nAttempted"] - sr["nAttempted"]) <= max(10, abs(sn["nAttempted"] - sr["nAttempted"]) * 10)
-    for key, tol in (("xb", 1e-6), ("B", 1e-4), ("J", 1e-2)):
-        a = inner(f[key]) if key != "J" else f[key]
-        b = inner(fr[key]) if key != "J" else fr[key]
-        c = inner(fn[key]) if key != "J" else fn[key]
-        spread = relerr(c, b)
-        ours = relerr(a, b)
-        print(f"{key}: library vs reference {ours:.2e}, reference fma vs nofma {spread:.2e}")
-        assert ours < max(10 * spread, 1e-10) or ours < tol
+    While the step-size controllers of the builds agree (every accept and
+    reject equal, through 1000 accepted steps), x and B hold the 1e-10 bound.
+    J is a difference quotient of B and carries the rounding of the grid
+    amplified by 1/d: the reference's own stock and --fmad=false builds differ
+    by 2.2e-10 in J at 500 steps, so for J, and for every field once the
+    controller has become chaotic (after about 1300 attempts a rounding
+    difference flips an accept), the bound is 10x that measured spread.
+    Measured on a GB300: library vs reference at 500 steps x 6.9e-13,
+    B 9.2e-12, J 1.5e-10 (reference vs itself 1.0e-12, 1.4e-11, 2.2e-10); at
+    2000 steps x 4.9e-8, B 2.0e-7, J 4.9e-6 (6.1e-8, 9.2e-6, 2.4e-4)."""
+    rows = run_vs_reference_kernels(64, (100, 500, 1000, 2000))
+    for m, ours, spread, att in rows:
+        if m <= 1000:
+            assert att[0] == att[1] == att[2], ("accept/reject sequences differ", m, att)
+            assert ours["x"] <= 1e-10 and ours["B"] <= 1e-10, (m, ours)
+        if m <= 100:
+            assert ours["J"] <= 1e-10, (m, ours)
+        for k in ("x", "B", "J"):
+            assert ours[k] <= max(1e-10, 10 * spread[k]), (m, k, ours[k], spread[k])
+
+
+def test_braid2_fp32_run_vs_reference_kernels():
+    """The same braid with FP32 storage and the reference's FP32 error norm
+    and controller (errMode 0, dt0 = 3e-4), against the reference's
+    PRECISION=32 kernels.  The FP32 error norm |x_new - x*| is rounding of x
+    (~1e-6) against maxError = 1e-5, so the controller of any two builds
+    diverges within a few tens of steps: the reference's stock and
+    --fmad=false builds already take 28 and 29 attempts to 25 accepted steps.
+    At 10 steps (every accept equal) x and B hold the 1e-5 bound and J stays
+    within the reference's own spread; at every mark each field is within 10x
+    that spread.  Measured: at 10 steps x 6.0e-8, B 3.6e-6, J 7.5e-6
+    (reference vs itself 7.9e-8, 3.8e-6, 7.6e-6); at 2000 steps x 3.1e-5,
+    B 7.0e-4, J 6.5e-3 (3.2e-5, 7.8e-4, 7.3e-3)."""
+    rows = run_vs_reference_kernels(32, (10, 25, 100, 500, 2000))
+    for m, ours, spread, att in rows:
+        if m == 10:
+            assert att[0] == att[1] == att[2], ("accept/reject sequences differ", m, att)
+            assert ours["x"] <= 1e-5 and ours["B"] <= 1e-5, (m, ours)
+            assert ours["J"] <= max(1e-5, 3 * spread["J"]), (m, ours, spread)
+        for k in ("x", "B", "J"):
+            assert ours[k] <= max(1e-5, 10 * spread[k]), (m, k, ours[k], spread[k])
 
 
 def test_fp32_storage_vs_fp64_step():
