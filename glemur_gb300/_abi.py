@@ -139,6 +139,7 @@ SIGNATURES = {
     "gm_download": (C.c_int, [VP, VP, VP, VP, VP]),
     "gm_autotune": (C.c_int, [VP, C.c_int, P(C.c_int), P(C.c_double)]),
     "gm_set_tile_z": (C.c_int, [VP, C.c_int]),
+    "gm_debug_stall": (C.c_int, [VP, C.c_int]),
     "gm_download_k": (C.c_int, [VP, C.c_int, VP]),
     "gm_download_x": (C.c_int, [VP, C.c_int, VP]),
     "gm_upload_u": (C.c_int, [VP, VP]),
@@ -175,6 +176,7 @@ SIGNATURES = {
                                          C.c_int, VP, VP]),
     "gm_nn_warm_grid": (C.c_int, [VP, P(GmParams), C.c_int, VP, VP, VP, VP]),
     "gm_nn_zero": (C.c_int, [VP, C.c_size_t, VP]),
+    "gm_nn_debug_stall": (C.c_int, [C.c_int]),
     "gm_device_count": (C.c_int, [P(C.c_int)]),
     "gm_set_device": (C.c_int, [C.c_int]),
     "gm_io_write_cuda_info": (C.c_int, [C.c_char_p, C.c_int, C.c_long]),

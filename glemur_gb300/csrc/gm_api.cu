@@ -63,8 +63,7 @@ int check_params(const gm_params* p) {
         strncmp(p->jMethod, "StokesTri ", 10) != 0)
         return gm::fail(GM_EPARAM, "jMethod: the Stokes, Stokes4th, StokesQuint, StokesTri and Classic currents are implemented");
     if (p->pressure && strncmp(p->pMethod, "Classic ", 8) != 0) return gm::fail(GM_EPARAM, "pMethod must be Classic");
-    if (p->initShearA != 0 || p->initShearB != 0)
-        return gm::fail(GM_EPARAM, "initial-distortion ghost corrections (initShearA/B != 0) are not implemented");
+    if (p->initDistCode != 0 && p->initDistCode != 1) return gm::fail(GM_EPARAM, "initDistCode must be 0 or 1");
     if (!(p->dx > 0 && p->dy > 0 && p->dz > 0)) return gm::fail(GM_EPARAM, "dx, dy, dz must be > 0 (call gm_params_derive)");
     if (p->errMode != 0 && p->errMode != 1) return gm::fail(GM_EPARAM, "errMode must be 0 or 1");
     if (p->stageKernel != 0 && p->stageKernel != 1) return gm::fail(GM_EPARAM, "stageKernel must be 0 or 1");
@@ -91,10 +90,12 @@ struct ImplBase {
     virtual int step(gm_step_result* r) = 0;
     virtual int autotune(int trials, int* tz, double* ms) = 0;
     virtual int set_tile_z(int tz) = 0;
+    virtual int debug_stall(int on) = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     int64_t launches = 0;
     bool uploaded = false;
+    bool stall_on = false;   // gm_debug_stall
 };
 
 template <typename T>
@@ -112,6 +113,7 @@ struct Impl : ImplBase {
     T* KU[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     T* B0 = nullptr;
     T* B0s = nullptr;           // B0 scaled for the algebraic B formula
+    T* shear_tab = nullptr;     // initially distorted grid: the z ghost planes' corrected positions
     T* outB = nullptr;
     T* outJ = nullptr;
     T* outD = nullptr;
@@ -146,7 +148,7 @@ struct Impl : ImplBase {
         if (graph) cudaGraphDestroy(graph);
         void* ptrs[] = {X[0], X[1], XS[0], XS[1], K[0], K[1], K[2], K[3], K[4], B0, B0s, outB, outJ,
                         outD, stage_buf, eps, eps_col, st, log, part, red, U[0], U[1], US[0], US[1],
-                        KU[0], KU[1], KU[2], KU[3], KU[4]};
+                        KU[0], KU[1], KU[2], KU[3], KU[4], shear_tab};
         for (void* q : ptrs)
             if (q) cudaFree(q);
         if (h_st) cudaFreeHost(h_st);
@@ -201,6 +203,9 @@ struct Impl : ImplBase {
         kp.maxError = (double)(T)p->maxError;
         kp.dtMin = (double)(T)p->dtMin;
         kp.ar = p->ar; kp.az = p->az; kp.phi1 = p->phi1;
+        kp.shear = p->initShearA != 0 || p->initShearB != 0;
+        kp.initDistCode = p->initDistCode;
+        kp.shA = (T)p->initShearA; kp.shB = (T)p->initShearB; kp.shK = (T)p->initShearK;
         kp.wantXbAn = p->redErrXb_XbAn != 0;
         kp.nTs = p->nTs;
         kp.dtDump = (T)p->dtDump;
@@ -245,6 +250,10 @@ struct Impl : ImplBase {
         }
         if ((rc = alloc((void**)&B0, NP * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&B0s, NP * sizeof(T)))) return rc;
+        if (kp.shear) {
+            if ((rc = alloc((void**)&shear_tab, (size_t)20 * nx * ny * sizeof(T)))) return rc;
+            kp.shearTab = shear_tab;
+        }
         if ((rc = alloc((void**)&outB, 3 * NG * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outJ, 3 * N * sizeof(T)))) return rc;
         if ((rc = alloc((void**)&outD, NG * sizeof(T)))) return rc;
@@ -396,6 +405,7 @@ struct Impl : ImplBase {
         a.st = st;
         a.log = log;
         a.n = n;
+        a.stall = stall_on ? 1 : 0;
         a.TZ = TZ;
         a.outB = outB; a.outJ = outJ; a.outD = outD;
         a.part = part;
@@ -417,6 +427,11 @@ struct Impl : ImplBase {
             CUDA_TRY(gmk::launch_images<T>(kp, b, stream));
         }
         launches += 10;
+        if (kp.shear) {
+            // the line-tied z ghost planes of the uploaded grid, with addDist
+            CUDA_TRY(gmk::launch_shear_table<T>(kp, X[0], shear_tab, stream));
+            launches++;
+        }
         if (kp.inertia) {
             // uInit = "nil": zero velocity (the reference allocates uu with
             // malloc and leaves it unset, memory.cu:33-35, init.cu:362-364)
@@ -580,6 +595,15 @@ struct Impl : ImplBase {
         if (rc != GM_OK) return rc;
         if (tz_out) *tz_out = best_tz;
         if (ms_out) *ms_out = best_ms / trials;
+        return GM_OK;
+    }
+
+    int debug_stall(int on) override {
+        if (!use_tma) return gm::fail(GM_EPARAM, "gm_debug_stall: the run does not use the TMA stage kernel");
+        stall_on = on != 0;
+        // the step graph holds the launch arguments: capture it again
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
         return GM_OK;
     }
 
@@ -1214,6 +1238,11 @@ int gm_run(gm_handle* h, int nCycle, gm_state* out) {
 int gm_run_events(gm_handle* h, int nCycle, gm_state* out) {
     if (!h) return gm::fail(GM_EPARAM, "null handle");
     return h->impl->run_events(nCycle, out);
+}
+
+int gm_debug_stall(gm_handle* h, int on) {
+    if (!h) return gm::fail(GM_EPARAM, "null handle");
+    return h->impl->debug_stall(on);
 }
 
 int gm_grid_fields(gm_handle* h, void* cellVol, void* convexity, void* wedgeMin) {

@@ -83,6 +83,10 @@ struct KP {
     T cmcT[6];               // c - c* in the run precision
     T inv8dxdydz;            // 1 / (8 dx dy dz): det(a, b, c) -> Delta
     double ar, az, phi1;     // analytic-field parameters (distance-to-analytic diagnostic)
+    int shear;               // initShearA or initShearB != 0: addDist on the line-tied z ghost planes
+    int initDistCode;        // 0: initShearX, 1: centerShift (src/readNamelist.f90)
+    T shA, shB, shK;         // initShearA, initShearB, initShearK
+    const T* shearTab;       // with shear: the z ghost planes' corrected positions (k_shear_table)
     int wantXbAn;
     int nTs;                 // output cadences (main.cu:355-377)
     T dtDump, dtSave;
@@ -118,6 +122,8 @@ struct StageArgs {
     int n;                   // stage index 0..5
     int TZ;                  // planes per CTA
     int jpass;               // diagnostic mode on the stage's own input grid (the J pass of jxbAver)
+    int stall;               // failure-detection test (gm_debug_stall): the TMA stage kernel withholds the
+                             // copies of each tile's first position planes
     // diagnostic mode outputs (reference layout) and partials
     T* outB;                 // ghosted AoS
     T* outJ;                 // inner AoS
@@ -152,6 +158,8 @@ template <typename T>
 cudaError_t launch_images(const KP<T>& p, T* soa, cudaStream_t s);
 template <typename T>
 cudaError_t launch_scale_b0(const KP<T>& p, const T* B0, T* B0s, cudaStream_t s);
+template <typename T>
+cudaError_t launch_shear_table(const KP<T>& p, const T* X, T* tab, cudaStream_t s);
 template <typename T>
 cudaError_t launch_pack_k(const KP<T>& p, const T* k, T* aos, cudaStream_t s);
 template <typename T>

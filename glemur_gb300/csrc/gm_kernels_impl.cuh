@@ -95,7 +95,27 @@ __device__ __forceinline__ void b_interior(const KP<T>& p, const Tile<T, NB>& t,
 // plane shifted by the grid spacing; in-plane neighbours at the edges of the
 // reference's 16x16 launch blocks are the own position shifted by the
 // spacing (boundaries.cu:72-109, 212-237, 340-365); B.n = B0.n.
-template <typename T, class TileT>
+// addDist, src/boundaries.cu:11-35: the initial distortion at inner column
+// (i, j) and height z, component l (0: x, 1: y).  PI is a double constant, so
+// in FP32 the sine's argument, the sine and the products are double and only
+// the assignment to distX / distY rounds; the centerShift form takes exp in
+// REAL and subtracts the double constant 0.15366.
+template <typename T>
+__device__ __forceinline__ T add_dist(const KP<T>& p, int i, int j, T z, int l) {
+    const T x = p.dx * (T)i + p.Ox;
+    const T y = p.dy * (T)j + p.Oy;
+    T distX = 0, distY = 0;
+    if (p.initDistCode == 0) {
+        distY = (T)(-p.shA * sin(p.shK * (T)2 * 3.141592653589793 * (x + p.Ox - p.dx / (T)2) / (p.Lx + p.dx)) * z);
+        distX = (T)(-p.shB * sin(p.shK * (T)2 * 3.141592653589793 * (distY + y + p.Oy - p.dy / (T)2) / (p.Ly + p.dy)) *
+                    z);
+    } else {
+        distY = (T)(p.shA * exp(-p.shK * x * x) * ((T)1 - y * y) * (exp((T)-1 * z + (T)1) - 0.15366));
+    }
+    return l == 0 ? distX : distY;
+}
+
+template <typename T, bool SHEAR = true, class TileT>
 __device__ __forceinline__ void b_face(const KP<T>& p, const TileT& t, const T* __restrict__ B0, int a, int i,
                                        int j, int k, T Bv[3], T* D) {
     const int u = (a == 0) ? 1 : 0;
@@ -141,6 +161,18 @@ __device__ __forceinline__ void b_face(const KP<T>& p, const TileT& t, const T* 
     }
     if (eLv) Lv[v] = X1[v] - d3[v];
     if (eRv) Rv[v] = X1[v] + d3[v];
+    if (SHEAR && a == 2 && p.shear) {
+        // an initially distorted grid: the outer ghost plane and the neighbours
+        // extrapolated at the 16-wide block edges carry the distortion
+        // (src/boundaries.cu:65-107).  The line-tied ghost planes do not move,
+        // so these positions are constants of the run (k_shear_table).
+        const T* tb = p.shearTab + 10 * ((long long)side * p.nx * p.ny + (long long)j * p.nx + i);
+        Xo[0] = tb[0]; Xo[1] = tb[1];
+        if (eLu) { Lu[0] = tb[2]; Lu[1] = tb[3]; }
+        if (eRu) { Ru[0] = tb[4]; Ru[1] = tb[5]; }
+        if (eLv) { Lv[0] = tb[6]; Lv[1] = tb[7]; }
+        if (eRv) { Rv[0] = tb[8]; Rv[1] = tb[9]; }
+    }
     T jac[3][3];
 #pragma unroll
     for (int l = 0; l < 3; l++) {
@@ -774,6 +806,19 @@ __global__ void __launch_bounds__(256) k_stage(const __grid_constant__ StageArgs
 template <typename T>
 __device__ __forceinline__ void control_one(const KP<T>& p, DevState* st, double* log) {
     if (st->done) return;
+    if (st->status & (GM_ST_TIMEOUT | GM_ST_ALIGN)) {
+        // a stage of this step gave up a bounded wait or failed its alignment
+        // check: its outputs are incomplete, so the step is neither accepted
+        // nor used to adapt dt, and the run stops
+        st->maxDeltaBits = 0ull;
+        st->nAttempted++;
+        st->nRejected++;
+        st->lastAccepted = 0;
+        st->event = 0;
+        st->done = 1;
+        st->status |= GM_ST_DONE;
+        return;
+    }
     const double md = __longlong_as_double((long long)st->maxDeltaBits);
     st->maxDeltaBits = 0ull;
     st->maxDelta = md;
@@ -914,6 +959,38 @@ __global__ void k_images(const KP<T> p, T* __restrict__ soa) {
 }
 
 // B0 scaled for the algebraic B formula: (4 dy dz B0x, 4 dx dz B0y, 4 dx dy B0z)
+// The positions the line-tied z ghost planes' B formula uses on an initially
+// distorted grid (updateBbound's face-2 branch, src/boundaries.cu:63-107),
+// for every inner column (i, j) of both z faces: the outer plane (x, y) and
+// the four in-plane neighbours extrapolated at the reference's 16-wide block
+// edges (x, y each), in the reference's order of operations, with addDist in
+// device arithmetic as the reference evaluates it.  The ghost planes are fixed,
+// so this runs once per upload.  tab[10 ((side ny + j) nx + i) + q].
+template <typename T>
+__global__ void k_shear_table(const KP<T> p, const T* __restrict__ X, T* __restrict__ tab) {
+    const long long n = 2ll * p.nx * p.ny;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % p.nx), j = (int)((q / p.nx) % p.ny), side = (int)(q / ((long long)p.nx * p.ny));
+        const int k = side ? p.nz : -1;
+        T X1[3];
+        for (int l = 0; l < 3; l++)
+            X1[l] = X[l * p.cs + (i + 2) + (long long)p.px * ((j + 2) + (long long)p.py * (k + 2))];
+        const T sg = (T)(2 * side - 1);
+        const T zs = p.dz * sg + p.Oz + p.Lz * (T)side;
+        const T zo = (T)2 * p.dz * sg + p.Oz + p.Lz * (T)side;
+        T* t = tab + 10 * q;
+        for (int l = 0; l < 2; l++) t[l] = X1[l] - add_dist(p, i, j, X1[2], l) + add_dist(p, i, j, zo, l);
+        t[2] = X1[0] - p.dx - add_dist(p, i, j, zs, 0) + add_dist(p, i - 1, j, zs, 0);
+        t[3] = X1[1] - add_dist(p, i, j, zs, 1) + add_dist(p, i - 1, j, zs, 1);
+        t[4] = X1[0] + p.dx - add_dist(p, i, j, zs, 0) + add_dist(p, i + 1, j, zs, 0);
+        t[5] = X1[1] - add_dist(p, i, j, zs, 1) + add_dist(p, i + 1, j, zs, 1);
+        t[6] = X1[0] - add_dist(p, i, j, zs, 0) + add_dist(p, i, j - 1, zs, 0);
+        t[7] = X1[1] - p.dy - add_dist(p, i, j, zs, 1) + add_dist(p, i, j - 1, zs, 1);
+        t[8] = X1[0] - add_dist(p, i, j, zs, 0) + add_dist(p, i, j + 1, zs, 0);
+        t[9] = X1[1] + p.dy - add_dist(p, i, j, zs, 1) + add_dist(p, i, j + 1, zs, 1);
+    }
+}
+
 template <typename T>
 __global__ void k_scale_b0(const KP<T> p, const T* __restrict__ B0, T* __restrict__ B0s) {
     const T w0 = 4 * p.dy * p.dz, w1 = 4 * p.dx * p.dz, w2 = 4 * p.dx * p.dy;
@@ -1430,6 +1507,12 @@ cudaError_t launch_unpack(const KP<T>& p, const T* aos, T* soa, cudaStream_t s) 
 }
 
 template <typename T>
+cudaError_t launch_shear_table(const KP<T>& p, const T* X, T* tab, cudaStream_t s) {
+    k_shear_table<T><<<nblk(2ll * p.nx * p.ny), 256, 0, s>>>(p, X, tab);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_scale_b0(const KP<T>& p, const T* B0, T* B0s, cudaStream_t s) {
     k_scale_b0<T><<<nblk(p.cs), 256, 0, s>>>(p, B0, B0s);
     return cudaGetLastError();
@@ -1511,6 +1594,7 @@ cudaError_t launch_eps_star(const KP<T>& p, const T* B, const T* J, const T* X, 
     template cudaError_t launch_pack<T>(const KP<T>&, const T*, T*, cudaStream_t);                                \
     template cudaError_t launch_images<T>(const KP<T>&, T*, cudaStream_t);                                        \
     template cudaError_t launch_scale_b0<T>(const KP<T>&, const T*, T*, cudaStream_t);                            \
+    template cudaError_t launch_shear_table<T>(const KP<T>&, const T*, T*, cudaStream_t);                         \
     template cudaError_t launch_pack_k<T>(const KP<T>&, const T*, T*, cudaStream_t);                              \
     template cudaError_t launch_pack_k6<T>(const KP<T>&, const T*, const T*, T*, cudaStream_t);                  \
     template cudaError_t launch_j_oct<T>(const StageArgs<T>&, cudaStream_t);                                    \

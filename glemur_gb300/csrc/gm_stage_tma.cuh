@@ -237,7 +237,9 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     const StageArgs<T>& a = A.a;
     const KP<T>& p = a.p;
     DevState* st = a.st;
-    if (st->done) return true;
+    // a stopped run, or an earlier stage of this step that gave up a wait or
+    // failed its alignment check: nothing to compute
+    if (st->done || (st->status & (GM_ST_TIMEOUT | GM_ST_ALIGN))) return true;
 
     T* xs = reinterpret_cast<T*>(base);                                   // XR position slots
     T* b0r = reinterpret_cast<T*>(base + L::OFF_B0);                       // 2 B0s slots
@@ -352,19 +354,32 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
     };
     // ring positions relative to plane kk, from one modulo per iteration
     auto xring = [&](int m, int back) { int s = m - back; s += s < 0 ? XR : 0; return xs + s * SLOT; };
+    // the face formula at x / y face points (no initial-distortion terms: those
+    // concern the z faces only) and at the z ghost planes
     auto face_b = [&](int face, int i, int j, int kb, T Bv[3]) {
         Tile<T, 4, XR, 20> tl;
         tl.xs = xs;
         tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = S::HYR;
         tl.slot = SLOT;
         T D;
-        b_face<T>(p, tl, a.B0, face, i, j, kb, Bv, &D);
+        b_face<T, false>(p, tl, a.B0, face, i, j, kb, Bv, &D);
+    };
+    auto face_bz = [&](int i, int j, int kb, T Bv[3]) {
+        Tile<T, 4, XR, 20> tl;
+        tl.xs = xs;
+        tl.i0 = i0; tl.j0 = j0; tl.HX = HX2; tl.HY = S::HYR;
+        tl.slot = SLOT;
+        T D;
+        b_face<T, true>(p, tl, a.B0, 2, i, j, kb, Bv, &D);
     };
 
     // copies issued / completed so far (the producer): position planes
     // k0-2 .. kend+1, B0s planes k0-1 .. kend, k planes k0 .. kend-1
     if (producer) {
-        for (int q = k0 - 2; q <= min(k0 + 1, kend + 1); q++) issue_x(q);
+        // failure-detection test (a.stall): the first position planes are
+        // withheld, so the bounded waits for them run out
+        if (!a.stall)
+            for (int q = k0 - 2; q <= min(k0 + 1, kend + 1); q++) issue_x(q);
         ctl->x_iss = min(k0 + 1, kend + 1);
         ctl->x_done = k0 - 3;
         issue_b0(k0 - 1);
@@ -439,7 +454,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgsTMA<T>& A, int bx, int
                     }
                 } else if (!zPeri) {
                     // line-tied ghost plane: only the own columns are needed
-                    if (own[r]) face_b(2, ic, jc[r], kb, Bv[r]);
+                    if (own[r]) face_bz(ic, jc[r], kb, Bv[r]);
                 } else {
                     // periodic image plane: only the own columns are needed
                     if (own[r]) b_point<T, PC>(xm, x0, xq, ox1[r], s0, Bv[r], An[r], &Rn[r]);
@@ -663,7 +678,7 @@ template <typename T, bool PRESS, int NS>
 __global__ void __launch_bounds__(TX * TY2, sizeof(T) == 4 ? (stage_rows<T, PRESS>() == 1 ? GM_STAGE_MINB : 2) : 2)
     k_stage_tma(const __grid_constant__ StageArgsTMA<T> A) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    if (A.a.st->done) return;
+    if (A.a.st->done || (A.a.st->status & (GM_ST_TIMEOUT | GM_ST_ALIGN))) return;
     constexpr int R = stage_rows<T, PRESS>();
     unsigned char* base = stage_smem_setup<T, PRESS, NS, R>(smraw);
     stage_tile<T, PRESS, NS, R>(A, blockIdx.x, blockIdx.y, blockIdx.z, base);

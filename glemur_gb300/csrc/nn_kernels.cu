@@ -86,7 +86,9 @@ struct ConvArgs {
     int relu;
     int nx, ny, nz, xper, yper;
     int Kc, Np;                              // padded input channels (multiple of 16), padded outputs
+    int Nt;                                  // output channels per CTA (multiple of 16; blockIdx.y picks the slice)
     int* status;
+    int stall;                               // failure-detection test: wait on an mbarrier nothing arrives on
 };
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
@@ -107,18 +109,23 @@ __device__ __forceinline__ uint4 gather8(const ConvArgs& a, int i, int j, int k,
     return z;
 }
 
-// One CTA: 128 consecutive voxels x all Np output channels, accumulated over
-// the 27 taps.  The A tile (128 voxels x Kc input channels at the tap's
-// offset) and the tap's B tile (Np x Kc weights) are gathered into one of two
+// One CTA: 128 consecutive voxels x one slice of Nt output channels
+// (blockIdx.y; all Np when they fit), accumulated over the 27 taps.  The A
+// tile (128 voxels x Kc input channels at the tap's offset) and the tap's B
+// tile (the slice's weights, Nn x Kc) are gathered into one of two
 // shared-memory stages while the tensor cores work on the other.
 __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
     extern __shared__ __align__(128) unsigned char sm[];
-    const int Kc = a.Kc, Np = a.Np;
-    const int aBytes = 128 * Kc * 2, bBytes = Np * Kc * 2;
+    const int Kc = a.Kc;
+    const int n0 = blockIdx.y * a.Nt;                 // first output channel of the slice
+    const int Np = min(a.Nt, a.Np - n0);              // channels of this slice (a multiple of 16)
+    const int aBytes = 128 * Kc * 2, bBytes = a.Nt * Kc * 2;
     unsigned char* stA[2] = {sm, sm + aBytes};
     unsigned char* stB[2] = {sm + 2 * aBytes, sm + 2 * aBytes + bBytes};
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * aBytes + 2 * bBytes);   // 2 stages
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+    // mbarriers: one per stage (MMA commits) and one that nothing arrives on
+    // (the failure-detection test waits on it)
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * aBytes + 2 * bBytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long long V = (long long)a.nx * a.ny * a.nz;
     const long long v = (long long)blockIdx.x * 128 + tid;
@@ -131,6 +138,7 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
     if (tid == 0) {
         mbar_init_tc(&bars[0]);
         mbar_init_tc(&bars[1]);
+        mbar_init_tc(&bars[2]);
     }
     if (warp == 0) tmem_alloc(tslot, ncols);
     tc_fence_before();
@@ -139,13 +147,21 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
     const uint32_t tbase = *tslot;
     const uint32_t id = idesc_bf16(128, Np);
     uint32_t ph[2] = {0, 0};
-    bool ok = true;
+    bool pend[2] = {false, false};   // a commit on bars[s] not yet waited for
+    // failure-detection test: a bounded wait that runs out before any MMA
+    bool ok = a.stall ? mbar_wait_tc(&bars[2], 0, 1u << 10) : true;
     for (int t = 0; t < 27; t++) {
         const int s = t & 1;
         // the MMAs of tap t-2 read this stage: wait for them
-        if (t >= 2) {
+        if (pend[s]) {
             if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
             ph[s] ^= 1;
+            pend[s] = false;
+        }
+        // after a wait ran out no thread writes a stage and no MMA is issued
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
         }
         const int dk = t / 9 - 1, dj = (t / 3) % 3 - 1, di = t % 3 - 1;
         // A: row tid = this thread's voxel, Kc channels in 16-byte chunks
@@ -153,8 +169,8 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
             const uint4 q = valid ? gather8(a, vi + di, vj + dj, vk + dk, c) : make_uint4(0, 0, 0, 0);
             *reinterpret_cast<uint4*>(stA[s] + kmajor_off(tid, c, Kc)) = q;
         }
-        // B: the tap's Np x Kc weights
-        const __nv_bfloat16* Wt = a.W + (size_t)t * Np * Kc;
+        // B: the slice's Np x Kc weights of the tap
+        const __nv_bfloat16* Wt = a.W + ((size_t)t * a.Np + n0) * Kc;
         for (int e = tid; e < Np * Kc / 8; e += 128) {
             const int r = e / (Kc / 8), c = (e % (Kc / 8)) * 8;
             *reinterpret_cast<uint4*>(stB[s] + kmajor_off(r, c, Kc)) =
@@ -172,11 +188,16 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
             }
             mma_commit(&bars[s]);
         }
+        pend[s] = true;
     }
-    // the commits of taps 26 (stage 0) and 25 (stage 1) are still unwaited
-    if (!mbar_wait_tc(&bars[26 & 1], ph[26 & 1])) ok = false;
-    ph[26 & 1] ^= 1;
-    if (!mbar_wait_tc(&bars[25 & 1], ph[25 & 1])) ok = false;
+    // the commits not yet waited for (taps 25 and 26, or those in flight when
+    // a wait ran out): bounded waits before the accumulator is read or freed
+    for (int s = 0; s < 2; s++)
+        if (pend[s]) {
+            if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
+            ph[s] ^= 1;
+        }
+    ok = __syncthreads_and(ok);
     tc_fence_after();
     if (ok) {
         for (int c0 = 0; c0 < Np; c0 += 16) {
@@ -186,7 +207,7 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
                 const long long vv = v;
 #pragma unroll
                 for (int q = 0; q < 16; q++) {
-                    const int c = c0 + q;
+                    const int c = n0 + c0 + q;
                     if (c >= a.co) break;
                     float y = acc[q] + (a.bias ? a.bias[c] : 0.f);
                     if (a.relu) y = fmaxf(y, 0.f);
@@ -215,11 +236,13 @@ struct WgradArgs {
     int Kin;                                 // padded input channels (multiple of 16, <= 256)
     int vchunk;                              // voxels per CTA (multiple of 64)
     int* status;
+    int stall;                               // failure-detection test: wait on an mbarrier nothing arrives on
 };
 
 // dW[t][o][i] += sum_v dout[v][o] in[v + off(t)][i] over a voxel chunk, on the
-// tensor cores: M = 128 rows (output channels, zero-padded), N = Kin input
-// channels, K = voxels in steps of 64.  grid = (chunks, 27).
+// tensor cores: M = 128 rows (output channels 128 blockIdx.z .., zero-padded),
+// N = Kin input channels, K = voxels in steps of 64.
+// grid = (chunks, 27, output-channel tiles of 128).
 __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
     extern __shared__ __align__(128) unsigned char sm[];
     constexpr int KV = 64;                                   // voxels per K step
@@ -227,10 +250,13 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
     const int aBytes = 128 * KV * 2, bBytes = Kin * KV * 2;
     unsigned char* stA[2] = {sm, sm + aBytes};
     unsigned char* stB[2] = {sm + 2 * aBytes, sm + 2 * aBytes + bBytes};
+    // mbarriers: one per stage (MMA commits) and one that nothing arrives on
+    // (the failure-detection test waits on it)
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * aBytes + 2 * bBytes);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int t = blockIdx.y;
+    const int mo = 128 * blockIdx.z;                 // first output channel of this CTA's rows
     const int dk = t / 9 - 1, dj = (t / 3) % 3 - 1, di = t % 3 - 1;
     const long long V = (long long)a.nx * a.ny * a.nz;
     const long long v0 = (long long)blockIdx.x * a.vchunk;
@@ -240,6 +266,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
     if (tid == 0) {
         mbar_init_tc(&bars[0]);
         mbar_init_tc(&bars[1]);
+        mbar_init_tc(&bars[2]);
     }
     if (warp == 0) tmem_alloc(tslot, ncols);
     tc_fence_before();
@@ -248,12 +275,21 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
     const uint32_t tbase = *tslot;
     const uint32_t id = idesc_bf16(128, Kin);
     uint32_t ph[2] = {0, 0};
-    bool ok = true;
+    bool pend[2] = {false, false};   // a commit on bars[s] not yet waited for
+    // failure-detection test: a bounded wait that runs out before any MMA
+    bool ok = a.stall ? mbar_wait_tc(&bars[2], 0, 1u << 10) : true;
+    int issued = 0;                  // K steps whose MMAs were issued
     for (int st = 0; st < nsteps; st++) {
         const int s = st & 1;
-        if (st >= 2) {
+        if (pend[s]) {
             if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
             ph[s] ^= 1;
+            pend[s] = false;
+        }
+        // after a wait ran out no thread writes a stage and no MMA is issued
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
         }
         // voxel rows of this step: thread pairs split the 64 voxels
         const int r = tid & 63, half = tid >> 6;
@@ -265,10 +301,11 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
             vj = (int)((v / a.nx) % a.ny);
             vk = (int)(v / ((long long)a.nx * a.ny));
         }
-        // A[o][r] = dout[v][o], o < 128 (zero beyond co): half 0 writes o < 64, half 1 o >= 64
+        // A[o][r] = dout[v][mo + o], o < 128 (zero beyond co): half 0 writes
+        // o < 64, half 1 o >= 64
         for (int o = half * 64; o < half * 64 + 64; o++) {
             __nv_bfloat16 x = __float2bfloat16_rn(0.f);
-            if (valid && o < a.co) x = a.dout[v * a.ldd + o];
+            if (valid && mo + o < a.co) x = a.dout[v * a.ldd + mo + o];
             *reinterpret_cast<__nv_bfloat16*>(stA[s] + kmajor_off(o, r, KV)) = x;
         }
         // B[i][r] = in[v + off][i]
@@ -294,19 +331,20 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
             }
             mma_commit(&bars[s]);
         }
+        pend[s] = true;
+        issued++;
     }
-    if (nsteps >= 1) {
-        const int sl = (nsteps - 1) & 1;
-        if (!mbar_wait_tc(&bars[sl], ph[sl])) ok = false;
-        ph[sl] ^= 1;
-    }
-    if (nsteps >= 2) {
-        const int sp = (nsteps - 2) & 1;
-        if (!mbar_wait_tc(&bars[sp], ph[sp])) ok = false;
-    }
+    // the commits not yet waited for: bounded waits before the accumulator is
+    // read or freed
+    for (int s = 0; s < 2; s++)
+        if (pend[s]) {
+            if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
+            ph[s] ^= 1;
+        }
+    ok = __syncthreads_and(ok);
     tc_fence_after();
-    const int o = 32 * warp + lane;                      // this thread's row = output channel
-    if (ok && nsteps > 0) {
+    const int o = mo + 32 * warp + lane;                 // this thread's row: output channel mo + row
+    if (ok && issued > 0) {
         for (int c0 = 0; c0 < Kin; c0 += 16) {
             float acc[16];
             tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, acc);
@@ -619,12 +657,28 @@ static int check_view_align(const void* p, int ld, const char* what) {
     return GM_OK;
 }
 
+namespace {
+// failure-detection test hook (gm_nn_debug_stall): read when a convolution is launched
+int g_nn_stall = 0;
+}  // namespace
+
+int gm_nn_debug_stall(int on) {
+    g_nn_stall = on ? 1 : 0;
+    return GM_OK;
+}
+
 int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c2, const void* W, const float* bias,
                void* out, int ldo, int co, const void* mask, int ldm, int relu, int nx, int ny, int nz, int xper,
                int yper, int Kc, int Np, int* status, void* stream) {
     if (!in1 || !W || !out || !status) return gm::fail(GM_EPARAM, "gm_nn_conv: null argument");
     if (Kc % 16 || Kc < 16 || Kc > 256 || Np % 16 || Np < 16 || Np > 256 || c1 + (in2 ? c2 : 0) > Kc || co > Np ||
-        c1 % 8 || (size_t)2 * (128 + Np) * Kc * 2 + 32 > 200 * 1024)
+        c1 % 8)
+        return gm::fail(GM_EPARAM, "gm_nn_conv: channel counts out of range");
+    // output channels per CTA: all of them when both stages fit the shared
+    // memory, else the widest multiple of 16 that fits (slices in blockIdx.y)
+    int Nt = Np;
+    while (Nt > 16 && (size_t)2 * (128 + Nt) * Kc * 2 + 32 > 200 * 1024) Nt -= 16;
+    if ((size_t)2 * (128 + Nt) * Kc * 2 + 32 > 200 * 1024)
         return gm::fail(GM_EPARAM, "gm_nn_conv: channel counts out of range");
     int rc;
     if ((rc = check_view_align(in1, ld1, "gm_nn_conv in1")) || (rc = check_view_align(in2, ld2, "gm_nn_conv in2")))
@@ -635,12 +689,14 @@ int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c
     a.W = (const __nv_bfloat16*)W; a.bias = bias;
     a.out = (__nv_bfloat16*)out; a.ldo = ldo; a.co = co;
     a.mask = (const __nv_bfloat16*)mask; a.ldm = ldm; a.relu = relu;
-    a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper; a.Kc = Kc; a.Np = Np; a.status = status;
-    const size_t smem = (size_t)2 * (128 + Np) * Kc * 2 + 32;
+    a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper; a.Kc = Kc; a.Np = Np; a.Nt = Nt; a.status = status;
+    a.stall = g_nn_stall;
+    const size_t smem = (size_t)2 * (128 + Nt) * Kc * 2 + 32;
     cudaError_t e = cudaFuncSetAttribute(gmnn::k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
     const long long V = (long long)nx * ny * nz;
-    gmnn::k_conv<<<(unsigned)((V + 127) / 128), 128, smem, (cudaStream_t)stream>>>(a);
+    const dim3 grid((unsigned)((V + 127) / 128), (unsigned)((Np + Nt - 1) / Nt));
+    gmnn::k_conv<<<grid, 128, smem, (cudaStream_t)stream>>>(a);
     e = cudaGetLastError();
     return e == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, std::string("k_conv: ") + cudaGetErrorString(e));
 }
@@ -650,7 +706,7 @@ int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1
                      int* status, void* stream) {
     if (!dout || !in1 || !dW || !status) return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: null argument");
     if (Kin % 16 || Kin < 16 || Kin > 256 || c1 + (in2 ? c2 : 0) > Kin || ci > c1 + (in2 ? c2 : 0) || ci < 1 ||
-        co > 128 || co < 1 || vchunk % 64 || vchunk < 64 || c1 % 8)
+        co > 256 || co < 1 || vchunk % 64 || vchunk < 64 || c1 % 8)
         return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: channel counts or chunk out of range");
     int rc;
     if ((rc = check_view_align(in1, ld1, "gm_nn_conv_wgrad in1")) || (rc = check_view_align(in2, ld2, "gm_nn_conv_wgrad in2")))
@@ -661,11 +717,12 @@ int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1
     a.in2 = (const __nv_bfloat16*)in2; a.ld2 = ld2; a.c2 = in2 ? c2 : 0;
     a.dW = dW; a.ci = ci; a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper; a.Kin = Kin; a.vchunk = vchunk;
     a.status = status;
+    a.stall = g_nn_stall;
     const size_t smem = (size_t)2 * (128 + Kin) * 64 * 2 + 32;
     cudaError_t e = cudaFuncSetAttribute(gmnn::k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
     const long long V = (long long)nx * ny * nz;
-    const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), 27);
+    const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), 27, (unsigned)((co + 127) / 128));
     gmnn::k_conv_wgrad<<<grid, 128, smem, (cudaStream_t)stream>>>(a);
     e = cudaGetLastError();
     return e == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, std::string("k_conv_wgrad: ") + cudaGetErrorString(e));

@@ -49,8 +49,8 @@ __device__ __forceinline__ void mbar_init_tc(uint64_t* bar) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait_tc(uint64_t* bar, uint32_t parity) {
-    for (unsigned it = 0; it < kTcWaitLimit; it++) {
+__device__ __forceinline__ bool mbar_wait_tc(uint64_t* bar, uint32_t parity, unsigned limit = kTcWaitLimit) {
+    for (unsigned it = 0; it < limit; it++) {
         uint32_t ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"

@@ -290,6 +290,17 @@ int gm_autotune(gm_handle* h, int trials, int* tz, double* ms);
  * only), e.g. to repeat a depth gm_autotune chose; the step graph is
  * recaptured.  No counterpart in the reference. */
 int gm_set_tile_z(gm_handle* h, int tz);
+/* Failure-detection test hook (no counterpart in the reference, which has no
+ * bounded waits).  While `on` is non-zero, the TMA stage kernel's copy
+ * producer withholds the copies of each tile's first position planes, so
+ * every CTA's bounded wait for them (2^22 polls each) runs out: the CTA
+ * records GM_ST_TIMEOUT in the status word, waits (bounded) for the copies
+ * it did issue and returns; the step is neither accepted nor used to adapt
+ * dt, and the run stops with GM_ETIMEOUT.  No copy is left in flight and no
+ * wait is unbounded; the device context stays usable.  The step graph is
+ * recaptured.  GM_EPARAM when the run does not use the TMA stage kernel.
+ * Off by default. */
+int gm_debug_stall(gm_handle* h, int on);
 
 /* Stage increments k_0..k_4 of the last step (inner AoS in the reference kk
  * layout src/rungeKutta.cu:236: 3*nx*ny*nz values each, or 6*nx*ny*nz with
@@ -409,13 +420,15 @@ int gm_nn_tc_gemm_check(const void* A, const void* B, float* D, int N, int K, in
  *   relu, then times (mask[v][o] > 0) if mask; the input is the concatenation
  *   of the views in1 (c1 channels, c1 a multiple of 8) and in2 (c2); W is
  *   BF16 [27][Np][Kc] (Kc >= c1 + c2 and Np >= co multiples of 16, <= 256).
- *   With W flipped in t and transposed it is the input gradient. */
+ *   With W flipped in t and transposed it is the input gradient.  A CTA takes
+ *   128 voxels and all Np outputs, or a slice of them when the two operand
+ *   stages would not fit its shared memory. */
 int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c2, const void* W, const float* bias,
                void* out, int ldo, int co, const void* mask, int ldm, int relu, int nx, int ny, int nz, int xper,
                int yper, int Kc, int Np, int* status, void* stream);
 /* dW[t][o][i] += sum_v dout[v][o] in[v + off(t)][i] (FP32, i < ci), on the
  * tensor cores over voxel chunks of vchunk (a multiple of 64); Kin >= c1 + c2
- * a multiple of 16 <= 256, co <= 128. */
+ * a multiple of 16 <= 256, co <= 256 (output channels in tiles of 128). */
 int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1, int c1, const void* in2, int ld2,
                      int c2, float* dW, int ci, int nx, int ny, int nz, int xper, int yper, int Kin, int vchunk,
                      int* status, void* stream);
@@ -467,6 +480,13 @@ int gm_nn_warm_grid(const float* d, const gm_params* p, int passes, const void* 
                     void* stream);
 /* Zero `bytes` bytes of device memory (cudaMemsetAsync). */
 int gm_nn_zero(void* p, size_t bytes, void* stream);
+/* Failure-detection test hook for the tensor-core convolutions (no
+ * counterpart in the reference): while `on` is non-zero (process-wide, read
+ * at each launch of gm_nn_conv / gm_nn_conv_wgrad), every CTA first waits on
+ * an mbarrier that nothing arrives on, with a limit of 2^10 polls; the wait
+ * runs out before any MMA is issued, the CTA frees its tensor memory and sets
+ * *status = 1, and its output is left unwritten.  Off by default. */
+int gm_nn_debug_stall(int on);
 
 /* Number of CUDA devices and selection of the device the calling thread
  * uses (the cudaGetDeviceCount / cudaSetDevice of src/main.cu:47-80). */

@@ -32,6 +32,11 @@ reference's boundary handling:
   (jMethod = "StokesQuint", src/current.cu:737-1199).
 * tri_tied_f64 -- the triangular Stokes current (jMethod = "StokesTri",
   src/current.cu:1202-1681), every face line-tied.
+* shear_f64 / shear_f32 -- an initially sheared grid (initDist =
+  "initShearX", src/init.cu:401-407): the line-tied z ghost planes carry the
+  addDist correction (src/boundaries.cu:11-35, 63-107).
+* centershift_tied_f64 (checked live against the reference's kernels, no
+  fixture) -- initDist = "centerShift" on a small all-line-tied box.
 """
 from __future__ import annotations
 
@@ -109,6 +114,23 @@ def make(name: str):
         p = _braid((17, 12, 17), 64, peri=(0, 0, 0)) if name == "quint_tied_f64" else _braid((17, 17, 18), 64)
         p.set_str("jMethod", "StokesQuint")
         return configs.derive(p)
+    if name in ("shear_f64", "shear_f32"):
+        p = _braid((17, 17, 18), 64 if name.endswith("64") else 32)
+        p.set_str("initDist", "initShearX")
+        p.initDistCode = 0
+        p.initShearA, p.initShearB, p.initShearK = p.rnd(0.05), p.rnd(0.03), 1.0
+        return configs.derive(p)
+    if name == "centershift_tied_f64":
+        p = configs.braid2(17, 17, 12, precision=64)
+        p.xPeri = p.yPeri = p.zPeri = 0
+        p.Lx, p.Ly, p.Lz = 2.0, 2.0, 4.0
+        p.Ox, p.Oy, p.Oz = -1.0, -1.0, 0.0
+        configs.set_blobs(p, [(0.3, 0.0, 1.5, 1.0, 0.5, 0.8), (-0.3, 0.0, 2.5, -1.0, 0.5, 0.8)])
+        p.errMode = 0
+        p.set_str("initDist", "centerShift")
+        p.initDistCode = 1
+        p.initShearA, p.initShearB, p.initShearK = 0.02, 0.0, 1.0
+        return configs.derive(p)
     if name == "analytic_f64":
         p = configs.defaults(64)
         p.nx, p.ny, p.nz = 16, 16, 16
@@ -129,5 +151,5 @@ def make(name: str):
 NAMES = ["braid_f64", "braid_f32", "tied_f64", "zperi_f64", "press_f64", "analytic_f64", "classic_tied_f64",
          "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64", "classic_press_tied_f64",
          "classic_inertia_tied_f64", "jxbaver_f64", "oct_f64", "oct_tied_f64", "oct_f32", "quint_f64",
-         "quint_tied_f64", "tri_tied_f64"]
+         "quint_tied_f64", "tri_tied_f64", "shear_f64", "shear_f32"]
 N_ACCEPTED = 10

@@ -102,9 +102,13 @@ def test_namelist_reader_initial_distortion(tmp_path, dist, code):
     _abi.check(_abi.load().gm_params_read(p, str(f).encode(), 64), "read")
     assert p.get_str("initDist") == dist and p.initDistCode == code
     assert (p.initShearA, p.initShearB, p.initShearK) == (0.25, 0.5, 2.0)
+    # the parameter check accepts initially distorted grids (the ghost planes
+    # carry addDist); without a GPU gm_create stops later, at the device
     h = C.c_void_p()
-    assert _abi.load().gm_create(p, C.byref(h)) == -1       # the stage kernels lack addDist
-    assert b"initShear" in _abi.load().gm_last_error()
+    rc = _abi.load().gm_create(p, C.byref(h))
+    assert rc != -1 and b"initShear" not in _abi.load().gm_last_error()
+    if rc == 0:
+        _abi.load().gm_destroy(h)
 
 
 @pytest.mark.parametrize("line,ok", [

@@ -62,7 +62,7 @@ def stage_by_stage(p, ref):
     r.close()
 
 
-@pytest.mark.parametrize("name", cases.NAMES)
+@pytest.mark.parametrize("name", cases.NAMES + ["centershift_tied_f64"])
 def test_stages_match_oracle(name):
     stage_by_stage(cases.make(name), Oracle)
 
@@ -71,7 +71,7 @@ def test_stages_match_oracle(name):
                                   "classic_tied_f32", "inertia_f64", "inertia_f32", "inertia_press_f64",
                                   "classic_press_tied_f64", "classic_inertia_tied_f64", "jxbaver_f64", "oct_f64",
                                   "oct_tied_f64", "oct_f32", "quint_f64", "quint_tied_f64",
-                                  "tri_tied_f64"])
+                                  "tri_tied_f64", "shear_f64", "shear_f32", "centershift_tied_f64"])
 def test_stages_match_reference_kernels(name):
     stage_by_stage(cases.make(name), RefLauncher)
 
