@@ -228,11 +228,12 @@ def warm_start_comparison():
     (inference, grid build, validity check) included, with min Delta of each
     run.  Runs after the timed region."""
     from glemur_gb300 import train_warmstart as tw
-    from glemur_gb300.warmstart import UNet, WEIGHTS, load_weights, n_params
+    from glemur_gb300.warmstart import UNet, WEIGHTS, load_weights, n_params, weights_width
     if not WEIGHTS.exists():
         return None
-    net = UNet(tw.SHAPE, seed=0)
-    net.load_state_dict(load_weights())
+    w = load_weights()
+    net = UNet(tw.SHAPE, seed=0, wb=weights_width(w))
+    net.load_state_dict(w)
     seeds = [tw.EVAL_SEED0 + s for s in WARM_SEEDS]
     rows = tw.evaluate(net, seeds, WARM_RESIDUAL, WARM_MAX_ATTEMPTS, log=lambda m: None)
     net.check_status()
@@ -246,7 +247,7 @@ def warm_start_comparison():
     return {"residual": f"|J||B|-weighted sum|JxB| / sum|J||B| <= {WARM_RESIDUAL} (the unweighted point mean "
                         "levels off near 0.19 on these braids, and 1e-2 is not reached before the grid folds, "
                         "in the reference's kernels too)",
-            "grid": list(tw.SHAPE), "seeds": seeds, "network_parameters": n_params(),
+            "grid": list(tw.SHAPE), "seeds": seeds, "network_parameters": n_params(weights_width(w)),
             "weights": str(WEIGHTS.relative_to(ROOT)), "plain_s": tp, "warm_s": tws,
             "speedup_total": tp / tws if tws > 0 else None,
             "accepted": sum(r["accepted"] for r in rows), "cases": per}

@@ -25,7 +25,7 @@ import time
 import numpy as np
 
 from . import BatchRelaxation, Relaxation, configs
-from .warmstart import UNet, load_weights, n_params, save_weights
+from .warmstart import WB, UNet, load_weights, n_params, save_weights, weights_width
 
 SHAPE = (64, 64, 128)
 TRAIN_SEED0 = 100000      # training seeds TRAIN_SEED0 + i
@@ -309,7 +309,7 @@ def evaluate_large(weights, residual, max_attempts, factor=2, log=print):
     g.state()
     tp, ap, rp0, mdp, okp = time_to_residual(g, p, xb0, B0, residual, max_attempts)
     cshape = (p.nx // factor, p.ny // factor, p.nz // factor)
-    net = UNet(cshape, seed=0)
+    net = UNet(cshape, seed=0, wb=weights_width(weights))
     net.load_state_dict(weights)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -345,6 +345,83 @@ def evaluate_large(weights, residual, max_attempts, factor=2, log=print):
     return row
 
 
+def evaluate_batched(net, seeds, residual, max_cycles, smooth=2, chunk=64, log=print):
+    """Held-out seeds in batches of `chunk` cases: every case of a batch is
+    relaxed together by the batched plain path (one persistent launch per
+    stage), first from the identity grid, then from the network's grid (built
+    on the device; a grid with min Delta <= 0 is replaced by the identity
+    grid).  Per case: attempts to the residual target, the residual at the
+    start, min Delta of the warm grid; per batch: the wall time of the plain
+    run and of the warm run, the latter including inference, grid builds,
+    uploads and validity checks."""
+    import torch
+    from . import _abi
+    lib = _abi.load()
+    rows, batches = [], []
+    for i0 in range(0, len(seeds), chunk):
+        ss = seeds[i0:i0 + chunk]
+        ps = [case(s) for s in ss]
+        inits = [configs.init_state(p) for p in ps]
+        b = BatchRelaxation(ps)
+        for c, (B0, xb) in enumerate(inits):
+            b.upload(c, xb, B0)
+        b.steps_async(2)            # capture the step graph outside the timed runs
+        b.state(0)
+        for c, (B0, xb) in enumerate(inits):
+            b.upload(c, xb, B0)
+        res0p = [b.refresh(c)["residual"] for c in range(len(ps))]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        outp = b.run(max_cycles, residual, pointwise=False, check_every=10)
+        torch.cuda.synchronize()
+        tp = time.perf_counter() - t0
+        # warm start: inference and grid build on the device, then the same run
+        t0 = time.perf_counter()
+        acc, mind, res0w = [], [], []
+        for c, (p, (B0, xb0)) in enumerate(zip(ps, inits)):
+            B0d = torch.from_numpy(B0).cuda()
+            xw = DeviceWarmGrid(p, xb0).build(net, B0d, smooth)
+            torch.cuda.synchronize()
+            _abi.check(lib.gm_batch_upload(b.h, c, _abi.VP(xw.data_ptr()), _abi.VP(B0d.data_ptr()), 0.0, p.dt0),
+                       "gm_batch_upload")
+            r = b.refresh(c)
+            ok = r["minDetJac"] > 0
+            if not ok:
+                b.upload(c, xb0, B0)
+                r = b.refresh(c)
+            acc.append(ok)
+            mind.append(r["minDetJac"])
+            res0w.append(r["residual"])
+        torch.cuda.synchronize()
+        t_net = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        outw = b.run(max_cycles, residual, pointwise=False, check_every=10)
+        torch.cuda.synchronize()
+        tw = time.perf_counter() - t0 + t_net
+        b.close()
+        for q, s in enumerate(ss):
+            rows.append(dict(seed=s, plain_attempts=outp[q]["attempted"], plain_reached=bool(outp[q]["converged"]),
+                             plain_res0=res0p[q], warm_attempts=outw[q]["attempted"],
+                             warm_reached=bool(outw[q]["converged"]), warm_res0=res0w[q], accepted=acc[q],
+                             warm_minDet=mind[q]))
+        batches.append(dict(cases=len(ss), plain_s=tp, warm_s=tw, warm_start_s=t_net))
+        log(f"eval batch {i0 // chunk}: {len(ss)} cases, plain {tp:.1f} s, warm {tw:.1f} s "
+            f"(warm start {t_net:.1f} s), accepted {sum(acc)}")
+    both = [r for r in rows if r["plain_reached"] and r["warm_reached"]]
+    att = [r["plain_attempts"] / max(r["warm_attempts"], 1) for r in both]
+    tp = sum(x["plain_s"] for x in batches)
+    tw = sum(x["warm_s"] for x in batches)
+    summary = dict(cases=len(rows), accepted=sum(r["accepted"] for r in rows),
+                   plain_reached=sum(r["plain_reached"] for r in rows),
+                   warm_reached=sum(r["warm_reached"] for r in rows), both_reached=len(both),
+                   plain_s=tp, warm_s=tw, speedup_total=tp / tw if tw > 0 else None,
+                   attempts_ratio_median=float(np.median(att)) if att else None,
+                   plain_res0_median=float(np.median([r["plain_res0"] for r in rows])),
+                   warm_res0_median=float(np.median([r["warm_res0"] for r in rows])),
+                   min_delta_warm=float(min(r["warm_minDet"] for r in rows)))
+    return dict(summary=summary, batches=batches, rows=rows)
+
+
 def summarize(rows):
     both = [r for r in rows if r["plain_reached"] and r["warm_reached"]]
     sp = [r["plain_s"] / r["warm_s"] for r in both]
@@ -373,15 +450,20 @@ def main(argv=None):
     ap.add_argument("--large", action="store_true", help="also evaluate the 256x256x512 pressure case")
     ap.add_argument("--smooth", default="2", help="comma-separated box-filter passes to evaluate")
     ap.add_argument("--tta", default="1", help="comma-separated numbers of input translations to average")
+    ap.add_argument("--wb", type=int, default=WB, help="bottleneck channels of a network trained here")
+    ap.add_argument("--eval-batched", type=int, default=0,
+                    help="also evaluate this many held-out seeds with the batched path")
     a = ap.parse_args(argv)
     global SHAPE
     SHAPE = tuple(int(v) for v in a.shape.split(","))
     log = lambda m: print(m, flush=True)
-    net = UNet(SHAPE, seed=7)
-    log(f"U-Net: {n_params()} parameters")
-    report = dict(shape=SHAPE, residual=a.residual, params=n_params())
-    if a.weights:
-        net.load_state_dict(load_weights(a.weights))
+    w = load_weights(a.weights) if a.weights else None
+    wb = weights_width(w) if w is not None else a.wb
+    net = UNet(SHAPE, seed=7, wb=wb)
+    log(f"U-Net: {n_params(wb)} parameters")
+    report = dict(shape=SHAPE, residual=a.residual, params=n_params(wb), wb=wb)
+    if w is not None:
+        net.load_state_dict(w)
     else:
         t0 = time.perf_counter()
         data = make_data([TRAIN_SEED0 + i for i in range(a.train)], a.residual, a.max_cycles, log)
@@ -402,6 +484,10 @@ def main(argv=None):
         log(f"{key((sm, tt))}: " + json.dumps(report[key((sm, tt))]["summary"]))
     best = min(variants, key=lambda v: -(report[key(v)]["summary"]["speedup_total"] or 0))
     report.update(best_variant=key(best), summary=report[key(best)]["summary"])
+    if a.eval_batched:
+        report["batched"] = evaluate_batched(net, [EVAL_SEED0 + a.eval + i for i in range(a.eval_batched)],
+                                             a.residual, a.max_cycles, smooth=best[0], log=log)
+        log("batched: " + json.dumps(report["batched"]["summary"]))
     if a.large:
         report["large"] = evaluate_large(net.state_dict(), a.residual, 4 * a.max_cycles, log=log)
     log(json.dumps(report["summary"]))

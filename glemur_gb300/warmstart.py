@@ -7,9 +7,11 @@ accumulation in tensor memory), pooling, upsampling, the loss and Adam.
 torch only allocates the buffers.
 
 Network (3 levels, base width 24): two convolutions per level on the way
-down (24, 48, 96 channels, 2x2x2 mean pooling between levels), nearest
+down (24, 48 and wb channels, 2x2x2 mean pooling between levels), nearest
 upsampling and concatenation with the skip on the way up (48, 24 channels),
-and a 3x3x3 head to 3 channels: the displacement in grid spacings.  Padding
+and a 3x3x3 head to 3 channels: the displacement in grid spacings.  The
+bottleneck width wb is 192 for networks trained here (1.79 M parameters; 96
+gives 0.80 M); a weights file records it in the shapes of its arrays.  Padding
 is periodic in x, y and zero in z.  The displacement of the first and last
 z-planes is imposed to be zero, and a predicted grid whose cells are not all
 positive (min Delta <= 0) is rejected in favour of the identity grid.
@@ -28,12 +30,22 @@ from ._abi import check
 
 WEIGHTS = Path(__file__).resolve().parent / "weights" / "unet_64x64x128.npz"
 
-# name, input channels of the weights, output channels, ReLU
-LAYERS = [("e0a", 3, 24, True), ("e0b", 24, 24, True), ("e1a", 24, 48, True), ("e1b", 48, 48, True),
-          ("ba", 48, 96, True), ("bb", 96, 96, True), ("d1a", 144, 48, True), ("d1b", 48, 48, True),
-          ("d0a", 72, 24, True), ("d0b", 24, 24, True), ("head", 24, 3, False)]
-# channels of the buffer view each layer reads (the input is stored with 8 channels)
-VIEW_IN = {"e0a": 8, "d1a": 144, "d0a": 72}
+WB = 192   # bottleneck channels of a network trained here
+
+
+def layers(wb=WB):
+    """(name, input channels of the weights, output channels, ReLU) per layer."""
+    return [("e0a", 3, 24, True), ("e0b", 24, 24, True), ("e1a", 24, 48, True), ("e1b", 48, 48, True),
+            ("ba", 48, wb, True), ("bb", wb, wb, True), ("d1a", wb + 48, 48, True), ("d1b", 48, 48, True),
+            ("d0a", 72, 24, True), ("d0b", 24, 24, True), ("head", 24, 3, False)]
+
+
+LAYERS = layers()
+
+
+def view_in(wb=WB):
+    """Channels of the buffer view each layer reads (the input is stored with 8 channels)."""
+    return {"e0a": 8, "d1a": wb + 48, "d0a": 72}
 
 
 def r16(n):
@@ -44,8 +56,13 @@ def r8(n):
     return (n + 7) // 8 * 8
 
 
-def n_params():
-    return sum(27 * ci * co + co for _, ci, co, _ in LAYERS)
+def n_params(wb=WB):
+    return sum(27 * ci * co + co for _, ci, co, _ in layers(wb))
+
+
+def weights_width(d):
+    """Bottleneck width of a weights dictionary (load_weights)."""
+    return int(d["bb.W"].shape[1])
 
 
 def bf16_bits(a):
@@ -67,9 +84,9 @@ def load_weights(path=None):
 
 
 class _Layer:
-    def __init__(self, name, ci, co, relu, rng, torch, dev):
+    def __init__(self, name, ci, co, relu, rng, torch, dev, view):
         self.name, self.ci, self.co, self.relu = name, ci, co, relu
-        self.view = VIEW_IN.get(name, ci)
+        self.view = view
         self.kin, self.npo = r16(self.view), r16(co)          # forward conv: K, padded outputs
         self.kco, self.npi = r16(co), r16(self.view)          # input-gradient conv
         f32 = dict(dtype=torch.float32, device=dev)
@@ -86,7 +103,7 @@ class _Layer:
 class UNet:
     """The network on one grid shape (nx, ny, nz divisible by 4)."""
 
-    def __init__(self, shape, seed=0, xper=True, yper=True, device="cuda"):
+    def __init__(self, shape, seed=0, xper=True, yper=True, device="cuda", wb=WB):
         import torch
         self.torch = torch
         self.lib = _abi.load()
@@ -97,16 +114,18 @@ class UNet:
         self.xper, self.yper = int(xper), int(yper)
         self.dev = device
         rng = np.random.default_rng(seed)
-        self.layers = {n: _Layer(n, ci, co, r, rng, torch, device) for n, ci, co, r in LAYERS}
+        self.wb = wb
+        vin = view_in(wb)
+        self.layers = {n: _Layer(n, ci, co, r, rng, torch, device, vin.get(n, ci)) for n, ci, co, r in layers(wb)}
         self.V = [nx * ny * nz, nx * ny * nz // 8, nx * ny * nz // 64]
         self.dims = [(nx, ny, nz), (nx // 2, ny // 2, nz // 2), (nx // 4, ny // 4, nz // 4)]
         bf = dict(dtype=torch.bfloat16, device=device)
         A = {}
         for name, lvl, ch in [("X0", 0, 8), ("E0a", 0, 24), ("CAT0", 0, 72), ("P1", 1, 24), ("E1a", 1, 48),
-                              ("CAT1", 1, 144), ("P2", 2, 48), ("Ba", 2, 96), ("Bb", 2, 96), ("D1a", 1, 48),
+                              ("CAT1", 1, wb + 48), ("P2", 2, 48), ("Ba", 2, wb), ("Bb", 2, wb), ("D1a", 1, 48),
                               ("D1b", 1, 48), ("D0a", 0, 24), ("D0b", 0, 24), ("Y", 0, 8),
                               ("dY", 0, 8), ("dD0b", 0, 24), ("dD0a", 0, 24), ("dCAT0", 0, 72), ("dD1b", 1, 48),
-                              ("dD1a", 1, 48), ("dCAT1", 1, 144), ("dBb", 2, 96), ("dBa", 2, 96), ("dP2", 2, 48),
+                              ("dD1a", 1, 48), ("dCAT1", 1, wb + 48), ("dBb", 2, wb), ("dBa", 2, wb), ("dP2", 2, 48),
                               ("dE1a", 1, 48), ("dP1", 1, 24), ("dE0a", 0, 24)]:
             A[name] = torch.zeros((self.V[lvl], ch), **bf)
         self.A = A
@@ -173,11 +192,12 @@ class UNet:
         self._conv(Ls["e0b"], v("E0a"), v("CAT0", 48), 24, 0, True)
         self._pool(v("CAT0", 48), v("P1"), 24, 0)
         self._conv(Ls["e1a"], v("P1"), v("E1a"), 48, 1, True)
-        self._conv(Ls["e1b"], v("E1a"), v("CAT1", 96), 48, 1, True)
-        self._pool(v("CAT1", 96), v("P2"), 48, 1)
-        self._conv(Ls["ba"], v("P2"), v("Ba"), 96, 2, True)
-        self._conv(Ls["bb"], v("Ba"), v("Bb"), 96, 2, True)
-        self._up(v("Bb"), v("CAT1"), 96, 1)
+        wb = self.wb
+        self._conv(Ls["e1b"], v("E1a"), v("CAT1", wb), 48, 1, True)
+        self._pool(v("CAT1", wb), v("P2"), 48, 1)
+        self._conv(Ls["ba"], v("P2"), v("Ba"), wb, 2, True)
+        self._conv(Ls["bb"], v("Ba"), v("Bb"), wb, 2, True)
+        self._up(v("Bb"), v("CAT1"), wb, 1)
         self._conv(Ls["d1a"], v("CAT1"), v("D1a"), 48, 1, True)
         self._conv(Ls["d1b"], v("D1a"), v("D1b"), 48, 1, True)
         self._up(v("D1b"), v("CAT0"), 48, 0)
@@ -217,20 +237,21 @@ class UNet:
         self._conv(L, v("dD1b"), v("dD1a"), 48, 1, False, mask=v("D1a"), backward=True)
         L = Ls["d1a"]
         self._wgrad(L, v("dD1a"), v("CAT1"), 1)
-        self._conv(L, v("dD1a"), v("dCAT1"), 144, 1, False, backward=True)
-        self._up(v("dCAT1"), v("dBb"), 96, 1, backward=True)
-        self._relu_bwd(v("dBb"), v("Bb"), 96, 2)
+        wb = self.wb
+        self._conv(L, v("dD1a"), v("dCAT1"), wb + 48, 1, False, backward=True)
+        self._up(v("dCAT1"), v("dBb"), wb, 1, backward=True)
+        self._relu_bwd(v("dBb"), v("Bb"), wb, 2)
         L = Ls["bb"]
         self._wgrad(L, v("dBb"), v("Ba"), 2)
-        self._conv(L, v("dBb"), v("dBa"), 96, 2, False, mask=v("Ba"), backward=True)
+        self._conv(L, v("dBb"), v("dBa"), wb, 2, False, mask=v("Ba"), backward=True)
         L = Ls["ba"]
         self._wgrad(L, v("dBa"), v("P2"), 2)
         self._conv(L, v("dBa"), v("dP2"), 48, 2, False, backward=True)
-        self._pool(v("dP2"), v("dCAT1", 96), 48, 1, backward=True, accumulate=True)
-        self._relu_bwd(v("dCAT1", 96), v("CAT1", 96), 48, 1)
+        self._pool(v("dP2"), v("dCAT1", wb), 48, 1, backward=True, accumulate=True)
+        self._relu_bwd(v("dCAT1", wb), v("CAT1", wb), 48, 1)
         L = Ls["e1b"]
-        self._wgrad(L, v("dCAT1", 96), v("E1a"), 1)
-        self._conv(L, v("dCAT1", 96), v("dE1a"), 48, 1, False, mask=v("E1a"), backward=True)
+        self._wgrad(L, v("dCAT1", wb), v("E1a"), 1)
+        self._conv(L, v("dCAT1", wb), v("dE1a"), 48, 1, False, mask=v("E1a"), backward=True)
         L = Ls["e1a"]
         self._wgrad(L, v("dE1a"), v("P1"), 1)
         self._conv(L, v("dE1a"), v("dP1"), 24, 1, False, backward=True)

@@ -20,10 +20,11 @@ MAX_ATTEMPTS = 12000
 
 def test_warm_start_reaches_residual_sooner():
     from glemur_gb300 import train_warmstart as tw
-    from glemur_gb300.warmstart import UNet, WEIGHTS, load_weights
+    from glemur_gb300.warmstart import UNet, WEIGHTS, load_weights, weights_width
     assert WEIGHTS.exists(), f"missing trained weights {WEIGHTS}"
-    net = UNet(tw.SHAPE, seed=0)
-    net.load_state_dict(load_weights())
+    w = load_weights()
+    net = UNet(tw.SHAPE, seed=0, wb=weights_width(w))
+    net.load_state_dict(w)
     rows = tw.evaluate(net, [tw.EVAL_SEED0 + s for s in SEEDS], RESIDUAL, MAX_ATTEMPTS, log=lambda m: None)
     net.check_status()
     for r in rows:

@@ -16,7 +16,10 @@ def rand_params(rng, scale=1.0):
 
 
 def test_param_count():
-    assert 750_000 < n_params() < 850_000
+    """About 2 M parameters at base width 24 with a 192-channel bottleneck;
+    a 96-channel bottleneck has 0.8 M."""
+    assert 1_700_000 < n_params() < 1_900_000
+    assert 750_000 < n_params(96) < 850_000
 
 
 def test_oracle_gradients_by_finite_differences():
@@ -158,10 +161,11 @@ def test_gpu_network_matches_oracle():
         d = net.dims[lvl]
         a_ = net.A[name][:, c0:c0 + c].float().cpu().numpy().astype(np.float64)
         return a_.reshape(d[2], d[1], d[0], c)
+    wb = net.wb
     pairs = {"head": (("dY", 0, 3, 0), ("D0b", 0, 24, 0)), "d0b": (("dD0b", 0, 24, 0), ("D0a", 0, 24, 0)),
              "d0a": (("dD0a", 0, 24, 0), ("CAT0", 0, 72, 0)), "d1b": (("dD1b", 0, 48, 1), ("D1a", 0, 48, 1)),
-             "d1a": (("dD1a", 0, 48, 1), ("CAT1", 0, 144, 1)), "bb": (("dBb", 0, 96, 2), ("Ba", 0, 96, 2)),
-             "ba": (("dBa", 0, 96, 2), ("P2", 0, 48, 2)), "e1b": (("dCAT1", 96, 48, 1), ("E1a", 0, 48, 1)),
+             "d1a": (("dD1a", 0, 48, 1), ("CAT1", 0, wb + 48, 1)), "bb": (("dBb", 0, wb, 2), ("Ba", 0, wb, 2)),
+             "ba": (("dBa", 0, wb, 2), ("P2", 0, 48, 2)), "e1b": (("dCAT1", wb, 48, 1), ("E1a", 0, 48, 1)),
              "e1a": (("dE1a", 0, 48, 1), ("P1", 0, 24, 1)), "e0b": (("dCAT0", 48, 24, 0), ("E0a", 0, 24, 0)),
              "e0a": (("dE0a", 0, 24, 0), ("X0", 0, 3, 0))}
     for name, (dspec, ispec) in pairs.items():
@@ -171,15 +175,15 @@ def test_gpu_network_matches_oracle():
         assert frob(g[name][0], dW) < 3e-3, (name, "W kernel", frob(g[name][0], dW))
         assert frob(g[name][1], db) < 3e-3, (name, "b kernel", frob(g[name][1], db))
     # forward convolutions and input gradients, layer by layer, from GPU buffers
-    fwd = {"e0b": ("E0a", 0, 24, 0, "CAT0", 48, 24), "d1a": ("CAT1", 0, 144, 1, "D1a", 0, 48),
-           "bb": ("Ba", 0, 96, 2, "Bb", 0, 96), "d0a": ("CAT0", 0, 72, 0, "D0a", 0, 24)}
+    fwd = {"e0b": ("E0a", 0, 24, 0, "CAT0", 48, 24), "d1a": ("CAT1", 0, wb + 48, 1, "D1a", 0, 48),
+           "bb": ("Ba", 0, wb, 2, "Bb", 0, wb), "d0a": ("CAT0", 0, 72, 0, "D0a", 0, 24)}
     for name, (iname, i0, ic, lvl, oname, o0, oc) in fwd.items():
         ref = uo.relu(uo.conv(buf(iname, i0, ic, lvl), *P[name]))
         assert frob(buf(oname, o0, oc, lvl), ref) < 1e-2, (name, "forward kernel")
-    # input gradient of d1a (the 144-channel concatenation), before the pool / ReLU updates
-    # of its skip part: the up part (channels 0..95) is untouched afterwards
-    dcat1 = uo.conv_bwd(buf("CAT1", 0, 144, 1), P["d1a"][0], buf("dD1a", 0, 48, 1))[0]
-    assert frob(buf("dCAT1", 0, 96, 1), dcat1[..., :96]) < 1e-2, "input-gradient kernel"
+    # input gradient of d1a (the wb + 48 channel concatenation), before the pool / ReLU
+    # updates of its skip part: the up part (channels 0..wb-1) is untouched afterwards
+    dcat1 = uo.conv_bwd(buf("CAT1", 0, wb + 48, 1), P["d1a"][0], buf("dD1a", 0, 48, 1))[0]
+    assert frob(buf("dCAT1", 0, wb, 1), dcat1[..., :wb]) < 1e-2, "input-gradient kernel"
 
 
 @pytest.mark.gpu
@@ -241,11 +245,12 @@ def test_gpu_warm_grid_matches_host_build(smooth):
     import torch
     from glemur_gb300 import configs
     from glemur_gb300.train_warmstart import DeviceWarmGrid, warm_grid
-    from glemur_gb300.warmstart import UNet, load_weights
+    from glemur_gb300.warmstart import UNet, load_weights, weights_width
     p = configs.random_braid(900003, shape=(64, 64, 128), precision=32)
     B0, xb0 = configs.init_state(p)
-    net = UNet((64, 64, 128), seed=0)
-    net.load_state_dict(load_weights())
+    w = load_weights()
+    net = UNet((64, 64, 128), seed=0, wb=weights_width(w))
+    net.load_state_dict(w)
     host = warm_grid(net, p, B0, smooth)
     dev = DeviceWarmGrid(p, xb0).build(net, torch.from_numpy(B0).cuda(), smooth).cpu().numpy()
     net.check_status()
