@@ -87,115 +87,157 @@ struct ConvArgs {
     int nx, ny, nz, xper, yper;
     int Kc, Np;                              // padded input channels (multiple of 16), padded outputs
     int Nt;                                  // output channels per CTA (multiple of 16; blockIdx.y picks the slice)
+    int Kch;                                 // input channels per pipeline step (min(Kc, kConvKc), multiple of 16)
     int* status;
     int stall;                               // failure-detection test: wait on an mbarrier nothing arrives on
 };
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// 16 bytes (8 channels starting at channel c) of voxel (i, j, k) of the
-// concatenated input, zero outside the z range and beyond the channels.
-__device__ __forceinline__ uint4 gather8(const ConvArgs& a, int i, int j, int k, int c) {
-    uint4 z = make_uint4(0, 0, 0, 0);
-    if (k < 0 || k >= a.nz) return z;
-    if (!a.xper && (i < 0 || i >= a.nx)) return z;
-    if (!a.yper && (j < 0 || j >= a.ny)) return z;
-    i = wrap(i, a.nx);
-    j = wrap(j, a.ny);
-    const long long v = (long long)i + (long long)a.nx * (j + (long long)a.ny * k);
-    if (c < a.c1) return *reinterpret_cast<const uint4*>(a.in1 + v * a.ld1 + c);
-    c -= a.c1;
-    if (c < a.c2) return *reinterpret_cast<const uint4*>(a.in2 + v * a.ld2 + c);
-    return z;
+// Pipeline of the convolution: a step is one tap and one chunk of up to
+// kConvKc input channels (Kch = min(Kc, kConvKc), so that narrow layers keep
+// small stages and many CTAs per SM); kConvStages steps of operands are in
+// flight.
+constexpr int kConvKc = 64;
+constexpr int kConvStages = 4;
+
+// 16-byte asynchronous copy global -> shared (cp.async, L2 only), or 16 zero
+// bytes when !valid (source size 0: nothing is read from src).
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sm_addr(dst)), "l"(src),
+                 "r"(valid ? 16 : 0)
+                 : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // One CTA: 128 consecutive voxels x one slice of Nt output channels
-// (blockIdx.y; all Np when they fit), accumulated over the 27 taps.  The A
-// tile (128 voxels x Kc input channels at the tap's offset) and the tap's B
-// tile (the slice's weights, Nn x Kc) are gathered into one of two
-// shared-memory stages while the tensor cores work on the other.
+// (blockIdx.y; all Np when they fit), accumulated over the 27 taps.  The
+// operands of a step (the tap's A tile: 128 voxels x one chunk of input
+// channels at the tap's offset; and its B tile: the slice's weights for that
+// chunk) are copied straight into shared memory with cp.async, kConvStages
+// steps ahead, while one thread issues the tensor-core MMAs of the current
+// step; a stage is refilled once the MMAs that read it have committed.
 __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
     extern __shared__ __align__(128) unsigned char sm[];
-    const int Kc = a.Kc;
+    constexpr int S = kConvStages;
+    const int Kc = a.Kc, KCH = a.Kch;
     const int n0 = blockIdx.y * a.Nt;                 // first output channel of the slice
     const int Np = min(a.Nt, a.Np - n0);              // channels of this slice (a multiple of 16)
-    const int aBytes = 128 * Kc * 2, bBytes = a.Nt * Kc * 2;
-    unsigned char* stA[2] = {sm, sm + aBytes};
-    unsigned char* stB[2] = {sm + 2 * aBytes, sm + 2 * aBytes + bBytes};
+    const int aBytes = 128 * KCH * 2, bBytes = a.Nt * KCH * 2;
+    unsigned char* stA = sm;                          // S stages of A, then S stages of B
+    unsigned char* stB = sm + S * aBytes;
     // mbarriers: one per stage (MMA commits) and one that nothing arrives on
     // (the failure-detection test waits on it)
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * aBytes + 2 * bBytes);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + S * (aBytes + bBytes));
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + S + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
     const long long V = (long long)a.nx * a.ny * a.nz;
     const long long v = (long long)blockIdx.x * 128 + tid;
     const bool valid = v < V;
     const int vi = valid ? (int)(v % a.nx) : 0;
     const int vj = valid ? (int)((v / a.nx) % a.ny) : 0;
     const int vk = valid ? (int)(v / ((long long)a.nx * a.ny)) : 0;
+    const int nk = (Kc + KCH - 1) / KCH;             // channel chunks per tap
+    const int T = 27 * nk;                           // steps
     uint32_t ncols = 32;
     while ((int)ncols < Np) ncols <<= 1;
-    if (tid == 0) {
-        mbar_init_tc(&bars[0]);
-        mbar_init_tc(&bars[1]);
-        mbar_init_tc(&bars[2]);
-    }
+    if (tid == 0)
+        for (int q = 0; q <= S; q++) mbar_init_tc(&bars[q]);
     if (warp == 0) tmem_alloc(tslot, ncols);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *tslot;
     const uint32_t id = idesc_bf16(128, Np);
-    uint32_t ph[2] = {0, 0};
-    bool pend[2] = {false, false};   // a commit on bars[s] not yet waited for
-    // failure-detection test: a bounded wait that runs out before any MMA
-    bool ok = a.stall ? mbar_wait_tc(&bars[2], 0, 1u << 10) : true;
-    for (int t = 0; t < 27; t++) {
-        const int s = t & 1;
-        // the MMAs of tap t-2 read this stage: wait for them
-        if (pend[s]) {
-            if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
-            ph[s] ^= 1;
-            pend[s] = false;
-        }
-        // after a wait ran out no thread writes a stage and no MMA is issued
-        if (!__syncthreads_and(ok)) {
-            ok = false;
-            break;
-        }
+
+    // the copies of step q into stage q % S
+    auto issue = [&](int q) {
+        const int st = q % S;
+        const int t = q / nk, kc0 = (q % nk) * KCH, kcw = min(KCH, Kc - kc0);
         const int dk = t / 9 - 1, dj = (t / 3) % 3 - 1, di = t % 3 - 1;
-        // A: row tid = this thread's voxel, Kc channels in 16-byte chunks
-        for (int c = 0; c < Kc; c += 8) {
-            const uint4 q = valid ? gather8(a, vi + di, vj + dj, vk + dk, c) : make_uint4(0, 0, 0, 0);
-            *reinterpret_cast<uint4*>(stA[s] + kmajor_off(tid, c, Kc)) = q;
+        // A: row tid = this thread's voxel at the tap's offset
+        int i = vi + di, j = vj + dj;
+        const int k = vk + dk;
+        bool in = valid && k >= 0 && k < a.nz && (a.xper || (i >= 0 && i < a.nx)) && (a.yper || (j >= 0 && j < a.ny));
+        i = wrap(i, a.nx);
+        j = wrap(j, a.ny);
+        const long long u = in ? (long long)i + (long long)a.nx * (j + (long long)a.ny * k) : 0;
+        unsigned char* dA = stA + st * aBytes;
+        for (int c = 0; c < kcw; c += 8) {
+            const int cc = kc0 + c;
+            const __nv_bfloat16* src = a.in1;
+            bool ok8 = in;
+            if (cc < a.c1) src = a.in1 + u * a.ld1 + cc;
+            else if (cc - a.c1 < a.c2) src = a.in2 + u * a.ld2 + (cc - a.c1);
+            else ok8 = false;
+            cp_async16(dA + kmajor_off(tid, c, KCH), ok8 ? src : a.in1, ok8);
         }
-        // B: the slice's Np x Kc weights of the tap
-        const __nv_bfloat16* Wt = a.W + ((size_t)t * a.Np + n0) * Kc;
-        for (int e = tid; e < Np * Kc / 8; e += 128) {
-            const int r = e / (Kc / 8), c = (e % (Kc / 8)) * 8;
-            *reinterpret_cast<uint4*>(stB[s] + kmajor_off(r, c, Kc)) =
-                *reinterpret_cast<const uint4*>(Wt + (size_t)r * Kc + c);
+        // B: the slice's Np x kcw weights of the tap
+        const __nv_bfloat16* Wt = a.W + ((size_t)t * a.Np + n0) * Kc + kc0;
+        unsigned char* dB = stB + st * bBytes;
+        const int cpr = kcw / 8;                     // 16-byte chunks per row
+        for (int e = tid; e < Np * cpr; e += 128) {
+            const int r = e / cpr, c = (e % cpr) * 8;
+            cp_async16(dB + kmajor_off(r, c, KCH), Wt + (size_t)r * Kc + c, true);
         }
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        if (tid == 0) {
-            for (int kk = 0; kk < Kc / 16; kk++) {
-                const uint64_t ad = smem_desc(sm_addr(stA[s]) + kk * 256, 128, (uint32_t)Kc * 16);
-                const uint64_t bd = smem_desc(sm_addr(stB[s]) + kk * 256, 128, (uint32_t)Kc * 16);
-                mma_bf16(tbase, ad, bd, id, t > 0 || kk > 0);
+    };
+
+    uint32_t ph[S];
+    bool pend[S];                    // a commit on bars[s] not yet waited for
+    for (int q = 0; q < S; q++) { ph[q] = 0; pend[q] = false; }
+    // failure-detection test: a bounded wait that runs out before any MMA
+    bool ok = a.stall ? mbar_wait_tc(&bars[S], 0, 1u << 10) : true;
+    if (__syncthreads_and(ok)) {
+        for (int q = 0; q < S - 1; q++) {
+            if (q < T) issue(q);
+            cp_async_commit();
+        }
+        for (int q = 0; q < T; q++) {
+            // refill the stage of step q + S - 1: the MMAs of step q - 1 read it
+            const int qn = q + S - 1;
+            if (qn < T) {
+                const int sn = qn % S;
+                if (pend[sn]) {
+                    if (!mbar_wait_tc(&bars[sn], ph[sn])) ok = false;
+                    ph[sn] ^= 1;
+                    pend[sn] = false;
+                }
             }
-            mma_commit(&bars[s]);
+            // after a wait ran out no thread copies into a stage and no MMA is issued
+            if (!__syncthreads_and(ok)) {
+                ok = false;
+                break;
+            }
+            if (qn < T) issue(qn);
+            cp_async_commit();
+            cp_async_wait<S - 1>();                  // step q's copies have landed
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            const int s = q % S;
+            if (tid == 0) {
+                const int kcw = min(KCH, Kc - (q % nk) * KCH);
+                for (int kk = 0; kk < kcw / 16; kk++) {
+                    const uint64_t ad = smem_desc(sm_addr(stA + s * aBytes) + kk * 256, 128, (uint32_t)KCH * 16);
+                    const uint64_t bd = smem_desc(sm_addr(stB + s * bBytes) + kk * 256, 128, (uint32_t)KCH * 16);
+                    mma_bf16(tbase, ad, bd, id, q > 0 || kk > 0);
+                }
+                mma_commit(&bars[s]);
+            }
+            pend[s] = true;
         }
-        pend[s] = true;
     }
-    // the commits not yet waited for (taps 25 and 26, or those in flight when
-    // a wait ran out): bounded waits before the accumulator is read or freed
-    for (int s = 0; s < 2; s++)
-        if (pend[s]) {
-            if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
-            ph[s] ^= 1;
+    // the copies still in flight, and the commits not yet waited for: bounded
+    // waits before the accumulator is read or freed
+    cp_async_wait_all();
+    for (int q = 0; q < S; q++)
+        if (pend[q]) {
+            if (!mbar_wait_tc(&bars[q], ph[q])) ok = false;
+            ph[q] ^= 1;
         }
     ok = __syncthreads_and(ok);
     tc_fence_after();
@@ -225,6 +267,19 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
 }
 
 // ---- convolution: weight gradient --------------------------------------------
+
+// Transpose of an 8 x 8 block of 16-bit values: in[r] holds elements (r, 0..7),
+// out[c] receives elements (0..7, c).  Word m of out[c] pairs rows 2m and
+// 2m + 1 of column c, taken from word c / 2 of those rows.
+__device__ __forceinline__ void transpose8x8(const uint4 in[8], uint4 out[8]) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(in);
+    uint32_t* o = reinterpret_cast<uint32_t*>(out);
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+            o[c * 4 + m] = __byte_perm(w[(2 * m) * 4 + c / 2], w[(2 * m + 1) * 4 + c / 2], (c & 1) ? 0x7632 : 0x5410);
+}
 
 struct WgradArgs {
     const __nv_bfloat16* dout; int ldd, co;  // upstream gradient (co channels)
@@ -291,33 +346,65 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
             ok = false;
             break;
         }
-        // voxel rows of this step: thread pairs split the 64 voxels
-        const int r = tid & 63, half = tid >> 6;
-        const long long v = v0 + (long long)st * KV + r;
-        const bool valid = v < V && v - v0 < a.vchunk;
-        int vi = 0, vj = 0, vk = 0;
-        if (valid) {
-            vi = (int)(v % a.nx);
-            vj = (int)((v / a.nx) % a.ny);
-            vk = (int)(v / ((long long)a.nx * a.ny));
+        // The operands move in 8 x 8 blocks: 8 voxels (rows 8 rg .. 8 rg + 7 of
+        // the step, the same for every block of this thread) by 8 channels,
+        // loaded as 8 rows of 16 bytes, transposed in registers and stored as
+        // 8 rows of 16 bytes of the K-major tile (K = voxel).
+        const int rg = tid & 7;
+        int vA[8], vB[8];            // the voxels for dout, and at the tap's offset for the input (-1: zero)
+        {
+            // the block's 8 voxels are consecutive: with nx a multiple of 8 they
+            // share j and k, so one decomposition serves all of them
+            const int vb = (int)(v0 + (long long)st * KV) + rg * 8;
+            const int nxy = a.nx * a.ny;
+            int i0 = vb % a.nx, j0 = (vb / a.nx) % a.ny, k0 = vb / nxy;
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int v = vb + u;
+                vA[u] = vB[u] = -1;
+                if (v < V && v - v0 < a.vchunk) {
+                    if (a.nx % 8) { i0 = v % a.nx; j0 = (v / a.nx) % a.ny; k0 = v / nxy; }
+                    const int iu = (a.nx % 8 ? i0 : i0 + u);
+                    vA[u] = v;
+                    const int i = iu + di, j = j0 + dj, k = k0 + dk;
+                    if (k >= 0 && k < a.nz && (a.xper || (i >= 0 && i < a.nx)) && (a.yper || (j >= 0 && j < a.ny)))
+                        vB[u] = wrap(i, a.nx) + a.nx * (wrap(j, a.ny) + a.ny * k);
+                }
+            }
         }
-        // A[o][r] = dout[v][mo + o], o < 128 (zero beyond co): half 0 writes
-        // o < 64, half 1 o >= 64
-        for (int o = half * 64; o < half * 64 + 64; o++) {
-            __nv_bfloat16 x = __float2bfloat16_rn(0.f);
-            if (valid && mo + o < a.co) x = a.dout[v * a.ldd + mo + o];
-            *reinterpret_cast<__nv_bfloat16*>(stA[s] + kmajor_off(o, r, KV)) = x;
-        }
-        // B[i][r] = in[v + off][i]
-        ConvArgs g;
-        g.in1 = a.in1; g.ld1 = a.ld1; g.c1 = a.c1; g.in2 = a.in2; g.ld2 = a.ld2; g.c2 = a.c2;
-        g.nx = a.nx; g.ny = a.ny; g.nz = a.nz; g.xper = a.xper; g.yper = a.yper;
-        for (int c = half * 8; c < Kin; c += 16) {
-            uint4 q = valid ? gather8(g, vi + di, vj + dj, vk + dk, c) : make_uint4(0, 0, 0, 0);
-            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
+        const uint4 z4 = make_uint4(0, 0, 0, 0);
+        // A[o][r] = dout[v_r][mo + o] (zero beyond co): one block per thread;
+        // blocks wholly beyond co are zero and written in the first use of
+        // each stage only
+        if (mo + (tid >> 3) * 8 < a.co || st < 2) {
+            const int og = tid >> 3, o0 = mo + og * 8;
+            uint4 rows[8], cols[8];
 #pragma unroll
             for (int u = 0; u < 8; u++)
-                *reinterpret_cast<__nv_bfloat16*>(stB[s] + kmajor_off(c + u, r, KV)) = e[u];
+                rows[u] = (vA[u] >= 0 && o0 < a.co)
+                              ? *reinterpret_cast<const uint4*>(a.dout + (size_t)vA[u] * a.ldd + o0) : z4;
+            transpose8x8(rows, cols);
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+                *reinterpret_cast<uint4*>(stA[s] + kmajor_off(og * 8 + c, rg * 8, KV)) = o0 + c < a.co ? cols[c] : z4;
+        }
+        // B[i][r] = in[v_r + off][i]
+        for (int e = tid; e < (Kin / 8) * 8; e += 128) {
+            const int c0 = (e >> 3) * 8;
+            uint4 rows[8], cols[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                rows[u] = z4;
+                if (vB[u] >= 0) {
+                    if (c0 < a.c1) rows[u] = *reinterpret_cast<const uint4*>(a.in1 + (size_t)vB[u] * a.ld1 + c0);
+                    else if (c0 - a.c1 < a.c2)
+                        rows[u] = *reinterpret_cast<const uint4*>(a.in2 + (size_t)vB[u] * a.ld2 + (c0 - a.c1));
+                }
+            }
+            transpose8x8(rows, cols);
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+                *reinterpret_cast<uint4*>(stB[s] + kmajor_off(c0 + c, rg * 8, KV)) = cols[c];
         }
         fence_async_smem();
         tc_fence_before();
@@ -674,12 +761,14 @@ int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c
     if (Kc % 16 || Kc < 16 || Kc > 256 || Np % 16 || Np < 16 || Np > 256 || c1 + (in2 ? c2 : 0) > Kc || co > Np ||
         c1 % 8)
         return gm::fail(GM_EPARAM, "gm_nn_conv: channel counts out of range");
-    // output channels per CTA: all of them when both stages fit the shared
-    // memory, else the widest multiple of 16 that fits (slices in blockIdx.y)
+    // output channels per CTA: all of them when the operand stages fit the
+    // shared memory, else the widest multiple of 16 that fits (slices in
+    // blockIdx.y)
+    const int Kch = Kc < gmnn::kConvKc ? Kc : gmnn::kConvKc;
+    auto conv_smem = [Kch](int nt) { return (size_t)gmnn::kConvStages * (128 + nt) * Kch * 2 + 64; };
     int Nt = Np;
-    while (Nt > 16 && (size_t)2 * (128 + Nt) * Kc * 2 + 32 > 200 * 1024) Nt -= 16;
-    if ((size_t)2 * (128 + Nt) * Kc * 2 + 32 > 200 * 1024)
-        return gm::fail(GM_EPARAM, "gm_nn_conv: channel counts out of range");
+    while (Nt > 16 && conv_smem(Nt) > 200 * 1024) Nt -= 16;
+    if (conv_smem(Nt) > 200 * 1024) return gm::fail(GM_EPARAM, "gm_nn_conv: channel counts out of range");
     int rc;
     if ((rc = check_view_align(in1, ld1, "gm_nn_conv in1")) || (rc = check_view_align(in2, ld2, "gm_nn_conv in2")))
         return rc;
@@ -689,9 +778,9 @@ int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c
     a.W = (const __nv_bfloat16*)W; a.bias = bias;
     a.out = (__nv_bfloat16*)out; a.ldo = ldo; a.co = co;
     a.mask = (const __nv_bfloat16*)mask; a.ldm = ldm; a.relu = relu;
-    a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper; a.Kc = Kc; a.Np = Np; a.Nt = Nt; a.status = status;
+    a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper; a.Kc = Kc; a.Np = Np; a.Nt = Nt; a.Kch = Kch; a.status = status;
     a.stall = g_nn_stall;
-    const size_t smem = (size_t)2 * (128 + Nt) * Kc * 2 + 32;
+    const size_t smem = conv_smem(Nt);
     cudaError_t e = cudaFuncSetAttribute(gmnn::k_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
     const long long V = (long long)nx * ny * nz;
@@ -706,7 +795,7 @@ int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1
                      int* status, void* stream) {
     if (!dout || !in1 || !dW || !status) return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: null argument");
     if (Kin % 16 || Kin < 16 || Kin > 256 || c1 + (in2 ? c2 : 0) > Kin || ci > c1 + (in2 ? c2 : 0) || ci < 1 ||
-        co > 256 || co < 1 || vchunk % 64 || vchunk < 64 || c1 % 8)
+        co > 256 || co < 1 || vchunk % 64 || vchunk < 64 || c1 % 8 || (long long)nx * ny * nz >= (1ll << 31))
         return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: channel counts or chunk out of range");
     int rc;
     if ((rc = check_view_align(in1, ld1, "gm_nn_conv_wgrad in1")) || (rc = check_view_align(in2, ld2, "gm_nn_conv_wgrad in2")))
