@@ -295,3 +295,53 @@ class UNet:
     def check_status(self):
         if int(self.status.item()) != 0:
             raise _abi.GlemurError("a tensor-core completion wait gave up (status set)")
+
+
+def time_passes(shape=(64, 64, 128), wb=WB, reps=10, seed=1):
+    """Mean wall time (CUDA events) of a forward pass and of a forward +
+    backward pass of the network on random inputs, after three warm-up
+    passes; then one more forward + backward inside cudaProfilerStart/Stop,
+    so that a profiler started with profiling off captures exactly that pass."""
+    import torch
+    nx, ny, nz = shape
+    net = UNet(shape, seed=seed, wb=wb)
+    rng = np.random.default_rng(seed)
+    X0 = np.zeros((nx * ny * nz, 8), np.float32)
+    X0[:, :3] = rng.normal(size=(nx * ny * nz, 3))
+    net.A["X0"].copy_(torch.from_numpy(X0).to(torch.bfloat16))
+    tgt = torch.from_numpy(rng.normal(size=(nx * ny * nz, 3)).astype(np.float32)).cuda()
+    scale = 1.0 / (nx * ny * nz * 3)
+
+    def fb():
+        net.zero_grad()
+        net.forward()
+        net.backward(tgt, scale)
+
+    for _ in range(3):
+        fb()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    for name, fn in (("forward_backward_ms", fb), ("forward_ms", net.forward)):
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = e0.elapsed_time(e1) / reps
+    net.check_status()
+    torch.cuda.profiler.start()
+    fb()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="time the warm-start network's passes on random inputs")
+    ap.add_argument("--shape", default="64,64,128")
+    ap.add_argument("--wb", type=int, default=WB)
+    a = ap.parse_args()
+    print(json.dumps(time_passes(tuple(int(v) for v in a.shape.split(",")), a.wb)))
