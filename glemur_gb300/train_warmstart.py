@@ -448,6 +448,8 @@ def main(argv=None):
     ap.add_argument("--weights", default="", help="evaluate these weights instead of training")
     ap.add_argument("--shape", default="64,64,128", help="grid (nx,ny,nz), each divisible by 4")
     ap.add_argument("--large", action="store_true", help="also evaluate the 256x256x512 pressure case")
+    ap.add_argument("--large-residual", type=float, default=0.0,
+                    help="residual target of the large case (default: --residual)")
     ap.add_argument("--smooth", default="2", help="comma-separated box-filter passes to evaluate")
     ap.add_argument("--tta", default="1", help="comma-separated numbers of input translations to average")
     ap.add_argument("--wb", type=int, default=WB, help="bottleneck channels of a network trained here")
@@ -475,22 +477,23 @@ def main(argv=None):
                       loss_last=hist[-1][2] if hist else None)
         if a.out:
             save_weights(net.state_dict(), a.out)
-    variants = [(int(s), int(q)) for s in a.smooth.split(",") for q in a.tta.split(",")]
+    variants = [(int(s), int(q)) for s in a.smooth.split(",") for q in a.tta.split(",")] if a.eval > 0 else []
     key = lambda v: f"smooth{v[0]}" + (f"_tta{v[1]}" if v[1] > 1 else "")
     for sm, tt in variants:
         rows = evaluate(net, [EVAL_SEED0 + i for i in range(a.eval)], a.residual, a.max_cycles, log, smooth=sm,
                         tta=tt)
         report[key((sm, tt))] = dict(summary=summarize(rows), rows=rows)
         log(f"{key((sm, tt))}: " + json.dumps(report[key((sm, tt))]["summary"]))
-    best = min(variants, key=lambda v: -(report[key(v)]["summary"]["speedup_total"] or 0))
-    report.update(best_variant=key(best), summary=report[key(best)]["summary"])
+    best = min(variants, key=lambda v: -(report[key(v)]["summary"]["speedup_total"] or 0)) if variants else (2, 1)
+    if variants:
+        report.update(best_variant=key(best), summary=report[key(best)]["summary"])
     if a.eval_batched:
         report["batched"] = evaluate_batched(net, [EVAL_SEED0 + a.eval + i for i in range(a.eval_batched)],
                                              a.residual, a.max_cycles, smooth=best[0], log=log)
         log("batched: " + json.dumps(report["batched"]["summary"]))
     if a.large:
-        report["large"] = evaluate_large(net.state_dict(), a.residual, 4 * a.max_cycles, log=log)
-    log(json.dumps(report["summary"]))
+        report["large"] = evaluate_large(net.state_dict(), a.large_residual or a.residual, 4 * a.max_cycles, log=log)
+    log(json.dumps(report.get("summary")))
     if a.report:
         with open(a.report, "w") as f:
             json.dump(report, f, indent=1)

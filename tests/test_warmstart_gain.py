@@ -7,8 +7,8 @@ check) in its time.  The held-out seeds lie outside the training range; every pr
 grid must be accepted (no folded cell).  The predicted grid starts at a
 higher residual than the identity grid (its small grid-scale errors show up
 as current), but its displacement is close to the relaxed one, so it needs
-far fewer attempts: on these seeds 1100 / 2100 / 1100 against 3900 / 5050 /
-2650, and 2x less wall time over 32 held-out seeds."""
+far fewer attempts: on these seeds 1150 / 2050 / 950 against 3900 / 5050 /
+2650, and 2.1x less total wall time over 256 held-out seeds."""
 import pytest
 
 pytestmark = pytest.mark.gpu
