@@ -25,11 +25,12 @@ cores: the reference is CUDA-only, so its CPU form is the C restatement in
 oracle/ (OpenMP over all cores) on the same workload, with parameters and
 initial state from the oracle (the product library is not loaded).
 
-Besides the timed region, the braid6 line carries three baselines and
-comparisons, each run after the timed region: cpu_baseline (the oracle on
-the host cores, a bounded sample), ref_cuda (the reference's own kernels,
-compiled from its sources, on the same GPU and workload) and warm_start
-(plain against warm-started time to residual on three held-out braids).
+Besides the timed region, the braid6 line carries baselines and comparisons,
+each run after the timed region: cpu_baseline (the oracle on the host cores,
+a bounded sample), ref_cuda (the reference's own kernels, compiled from its
+sources, on the same GPU and workload), warm_start (plain against
+warm-started time to residual on three held-out braids) and batched (the
+64-case batched configuration).
 """
 from __future__ import annotations
 
@@ -162,6 +163,69 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML (read-only queries)
+    about every millisecond in a thread during the timed region, so that a
+    timed region of a few milliseconds still has samples.  Falls back to
+    nvidia-smi (Clocks) when NVML cannot be loaded."""
+
+    # clock-event reason bits of nvml.h
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, gpu_index=0, period_s=0.001):
+        import ctypes as C
+        self.C = C
+        self.idx, self.period = gpu_index, period_s
+        self.samples = []
+        self.lib = None
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return
+            h = C.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(gpu_index), C.byref(h)) != 0:
+                return
+            self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            mx = C.c_uint()
+            self.max_mhz = float(mx.value) if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0 else None
+            self.lib, self.h = lib, h
+        except Exception:
+            self.lib = None
+
+    def _run(self):
+        C = self.C
+        mhz, rs = C.c_uint(), C.c_ulonglong()
+        while not self.stop:
+            ok1 = self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0     # NVML_CLOCK_SM
+            ok2 = self.reasons_fn(self.h, C.byref(rs)) == 0
+            if ok1 and ok2:
+                self.samples.append((float(mhz.value), int(rs.value)))
+            time.sleep(self.period)
+
+    def __enter__(self):
+        import threading
+        self.stop = False
+        self.thread = None
+        if self.lib is not None:
+            self.thread = threading.Thread(target=self._run, daemon=True)
+            self.thread.start()
+        return self
+
+    def __exit__(self, *a):
+        if self.thread is not None:
+            self.stop = True
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.samples:
+            return None
+        reasons = sorted({n for _, r in self.samples for bit, n in self.REASONS.items() if r & bit})
+        return {"sm_mhz": statistics.median(m for m, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.samples), "sampler": "nvml, ~1 ms"}
+
+
 def traffic_per_launch(p):
     """DRAM bytes per stage launch from the committed ncu summary, if any."""
     f = ROOT / "profiles" / "stage_kernel_traffic.json"
@@ -251,6 +315,44 @@ def warm_start_comparison():
             "weights": str(WEIGHTS.relative_to(ROOT)), "plain_s": tp, "warm_s": tws,
             "speedup_total": tp / tws if tws > 0 else None,
             "accepted": sum(r["accepted"] for r in rows), "cases": per}
+
+
+def batched_comparison(residual=0.2, max_accepted=3000):
+    """The batched configuration on this GPU, after the timed region: 64
+    seeded random braids of uneven sizes (seeds 1000..1063, drawn as
+    configs.random_braid) in one persistent launch per RK stage, each case
+    until its weighted force-free residual reaches `residual`, its dt falls
+    to dtMin, or `max_accepted` accepted steps.  Aggregate cell-RK-stages/s
+    and the p50 / p99 wall time per case (`--workload batch64` runs the same
+    with the single-case comparison)."""
+    import torch
+    from glemur_gb300 import BatchRelaxation, configs
+    ps = [configs.random_braid(1000 + i, precision=32) for i in range(64)]
+    inits = [configs.init_state(p) for p in ps]
+    b = BatchRelaxation(ps)
+    for c, (B0, xb) in enumerate(inits):
+        b.upload(c, xb, B0)
+    tune = b.autotune(2)
+    b.steps_async(3)
+    b.state(0)
+    for c, (B0, xb) in enumerate(inits):
+        b.upload(c, xb, B0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = b.run(max_accepted, residual, pointwise=False, check_every=10)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    b.close()
+    work = sum(p.nx * p.ny * p.nz * 6 * o["attempted"] for p, o in zip(ps, out))
+    secs = sorted(o["seconds"] for o in out)
+    return {"value": work / wall, "unit": UNIT, "wall_s": wall, "cases": 64,
+            "p50_case_s": secs[len(secs) // 2], "p99_case_s": secs[min(len(secs) - 1, int(0.99 * len(secs)))],
+            "converged": int(sum(o["converged"] for o in out)),
+            "folded_dtmin": int(sum(1 for o in out if not o["converged"] and o["status"] & 4)),
+            "residual_target": f"|J||B|-weighted residual <= {residual}", "max_accepted": max_accepted,
+            "tile_z": tune["tzb"], "what": "64 random braids (seeds 1000..1063) of 32^3, 48x48x96, 64x64x128 and "
+                                          "96x96x192 cells, one persistent launch per RK stage under a CUDA graph, "
+                                          "run after the timed region"}
 
 
 def reference_cuda_baseline(steps, warmup):
@@ -353,7 +455,7 @@ def run_gpu(args):
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    with Clocks(local) as ck:
+    with Clocks(local) as ck, NvmlClocks(local) as nk:
         with torch.cuda.stream(stream):
             e0.record(stream)
         g.steps_async(args.steps)
@@ -434,6 +536,9 @@ def run_gpu(args):
     warm = None
     if rank == 0 and not args.no_warm_start and WORKLOAD == "braid6":
         warm = warm_start_comparison()
+    batched = None
+    if rank == 0 and not args.no_batched and WORKLOAD == "braid6":
+        batched = batched_comparison(args.batch_residual, args.batch_cycles)
 
     if rank == 0:
         line = {
@@ -451,13 +556,14 @@ def run_gpu(args):
             "cpu_baseline": cb,
             "ref_cuda": ref_cuda,
             "warm_start": warm,
+            "batched": batched,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "note": "one relaxation job through the C-ABI from pinned host buffers: the grid and B0 "
                             "uploaded once, the step state (t, dt, maxDelta, counts) read back after every "
                             "step, the final grid downloaded once; per-step bytes are those copies divided "
                             "by the steps (the grid stays on the device between steps)"},
             "gpu_launches": launches,
-            "clocks": ck.summary(),
+            "clocks": nk.summary() or ck.summary(),
         }
         print(json.dumps(line))
     g.close()
@@ -558,6 +664,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference's own kernels")
     ap.add_argument("--no-warm-start", action="store_true", help="skip the warm-start comparison")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-case batched run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the cost model's tile depth")
     ap.add_argument("--tile-z", type=int, default=0, help="set the stage kernel's z-chunk depth (no autotuning)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)

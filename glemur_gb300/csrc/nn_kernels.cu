@@ -268,178 +268,181 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
 
 // ---- convolution: weight gradient --------------------------------------------
 
-// Transpose of an 8 x 8 block of 16-bit values: in[r] holds elements (r, 0..7),
-// out[c] receives elements (0..7, c).  Word m of out[c] pairs rows 2m and
-// 2m + 1 of column c, taken from word c / 2 of those rows.
-__device__ __forceinline__ void transpose8x8(const uint4 in[8], uint4 out[8]) {
-    const uint32_t* w = reinterpret_cast<const uint32_t*>(in);
-    uint32_t* o = reinterpret_cast<uint32_t*>(out);
-#pragma unroll
-    for (int c = 0; c < 8; c++)
-#pragma unroll
-        for (int m = 0; m < 4; m++)
-            o[c * 4 + m] = __byte_perm(w[(2 * m) * 4 + c / 2], w[(2 * m + 1) * 4 + c / 2], (c & 1) ? 0x7632 : 0x5410);
+// dW[t][o][i] = sum_v dout[v][o] in[v + off(t)][i] as one GEMM per voxel chunk
+// with the 27 taps stacked along M: row m = t Cp + i (Cp = ci rounded up to 8),
+// column n = output channel o (N = co rounded up to 16), K = voxels.  Both
+// operands are read as they lie in the channels-last buffers: 16 bytes are 8
+// channels of one voxel, which is one row of a core matrix of the MN-major
+// operand layout, so a copy goes straight from global to shared memory
+// (cp.async) with no transpose.
+//
+// MN-major, no swizzle: a step of kWgKV voxels of an operand with R rows (M or
+// N) is kWgKV / 16 slices of 16 voxels, one per MMA (K = 16); slice s holds
+// R / 8 x 2 core matrices of 128 bytes (8 voxels x 8 channels), core (rb, h) at
+// s R 32 + rb 256 + h 128 bytes.  So neighbouring core matrices along the rows
+// are 256 bytes apart (the descriptor's stride-dimension offset) and along K
+// 128 bytes apart (its leading-dimension offset).  Read with the two offsets
+// exchanged, every address would still fall inside the slice.
+constexpr int kWgKV = 64;
+constexpr int kWgStages = 4;
+
+__device__ __forceinline__ uint32_t mn_off(int rb, int w, int R) {
+    return (uint32_t)((w >> 4) * R * 32 + rb * 256 + (w & 15) * 16);
 }
 
 struct WgradArgs {
-    const __nv_bfloat16* dout; int ldd, co;  // upstream gradient (co channels)
+    const __nv_bfloat16* dout; int ldd, co;  // upstream gradient (channels up to co rounded to 8 readable)
     const __nv_bfloat16* in1; int ld1, c1;   // forward input views
     const __nv_bfloat16* in2; int ld2, c2;
     float* dW;                               // [27][co][ci] FP32, accumulated with atomics
-    int ci;                                  // input channels of the weights (<= c1 + c2)
+    int ci, Cp;                              // input channels of the weights; rows per tap (ci rounded to 8)
+    int N;                                   // MMA columns: co rounded up to 16
     int nx, ny, nz, xper, yper;
-    int Kin;                                 // padded input channels (multiple of 16, <= 256)
-    int vchunk;                              // voxels per CTA (multiple of 64)
+    int vchunk;                              // voxels per CTA (multiple of kWgKV)
     int* status;
     int stall;                               // failure-detection test: wait on an mbarrier nothing arrives on
 };
 
-// dW[t][o][i] += sum_v dout[v][o] in[v + off(t)][i] over a voxel chunk, on the
-// tensor cores: M = 128 rows (output channels 128 blockIdx.z .., zero-padded),
-// N = Kin input channels, K = voxels in steps of 64.
-// grid = (chunks, 27, output-channel tiles of 128).
+// grid = (voxel chunks, row tiles of 128 stacked (tap, channel) rows).  The
+// operands of a step (kWgKV voxels: the tile's rows of the input at their taps'
+// offsets, and the upstream gradient) are copied kWgStages steps ahead while
+// one thread issues the MMAs of the current step; a stage is refilled once the
+// MMAs that read it have committed.
 __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
     extern __shared__ __align__(128) unsigned char sm[];
-    constexpr int KV = 64;                                   // voxels per K step
-    const int Kin = a.Kin;
-    const int aBytes = 128 * KV * 2, bBytes = Kin * KV * 2;
-    unsigned char* stA[2] = {sm, sm + aBytes};
-    unsigned char* stB[2] = {sm + 2 * aBytes, sm + 2 * aBytes + bBytes};
+    constexpr int S = kWgStages, KV = kWgKV;
+    const int N = a.N;
+    const int aBytes = 128 * KV * 2, bBytes = N * KV * 2;
+    unsigned char* stA = sm;                          // S stages of A, then S stages of B
+    unsigned char* stB = sm + S * aBytes;
     // mbarriers: one per stage (MMA commits) and one that nothing arrives on
     // (the failure-detection test waits on it)
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + 2 * aBytes + 2 * bBytes);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + S * (aBytes + bBytes));
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + S + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int t = blockIdx.y;
-    const int mo = 128 * blockIdx.z;                 // first output channel of this CTA's rows
-    const int dk = t / 9 - 1, dj = (t / 3) % 3 - 1, di = t % 3 - 1;
-    const long long V = (long long)a.nx * a.ny * a.nz;
-    const long long v0 = (long long)blockIdx.x * a.vchunk;
-    const int nsteps = (int)((min(V - v0, (long long)a.vchunk) + KV - 1) / KV);
-    uint32_t ncols = 32;
-    while ((int)ncols < Kin) ncols <<= 1;
-    if (tid == 0) {
-        mbar_init_tc(&bars[0]);
-        mbar_init_tc(&bars[1]);
-        mbar_init_tc(&bars[2]);
+    const int m0 = 128 * blockIdx.y;                  // first stacked row of this CTA
+    const int V = a.nx * a.ny * a.nz;                 // < 2^31 (checked by the host)
+    const int v0 = blockIdx.x * a.vchunk;
+    const int nv = min(V - v0, a.vchunk);             // voxels of this chunk
+    const int T = (nv + KV - 1) / KV;                 // steps
+    const int w = tid & (KV - 1);                     // this thread's voxel within a step
+    const int cpb = a.Cp >> 3;                        // 8-channel groups per tap
+    // this thread's 8 row blocks of A (rb = tid / 64 + 2 r): tap and first channel
+    int tr[8], cr[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const int g = (m0 >> 3) + (tid >> 6) + 2 * r;
+        tr[r] = g / cpb;
+        cr[r] = (g - tr[r] * cpb) * 8;
     }
+    uint32_t ncols = 32;
+    while ((int)ncols < N) ncols <<= 1;
+    if (tid == 0)
+        for (int q = 0; q <= S; q++) mbar_init_tc(&bars[q]);
     if (warp == 0) tmem_alloc(tslot, ncols);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *tslot;
-    const uint32_t id = idesc_bf16(128, Kin);
-    uint32_t ph[2] = {0, 0};
-    bool pend[2] = {false, false};   // a commit on bars[s] not yet waited for
+    // A and B both MN-major (transpose bits 15 and 16)
+    const uint32_t id = idesc_bf16(128, N) | (1u << 15) | (1u << 16);
+
+    // the copies of step q into stage q % S
+    auto issue = [&](int q) {
+        const int st = q % S;
+        const int vl = q * KV + w;
+        const bool vin = vl < nv;
+        const int v = v0 + (vin ? vl : 0);
+        const int i = v % a.nx, j = (v / a.nx) % a.ny, k = v / (a.nx * a.ny);
+        unsigned char* dA = stA + st * aBytes;
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            const int t = tr[r], c = cr[r];
+            const int ii = i + t % 3 - 1, jj = j + (t / 3) % 3 - 1, kk = k + t / 9 - 1;
+            bool ok = vin && t < 27 && kk >= 0 && kk < a.nz && (a.xper || (ii >= 0 && ii < a.nx)) &&
+                      (a.yper || (jj >= 0 && jj < a.ny));
+            const long long u = ok ? (long long)wrap(ii, a.nx) + (long long)a.nx * (wrap(jj, a.ny) + (long long)a.ny * kk) : 0;
+            const __nv_bfloat16* src = a.in1;
+            if (c < a.c1) src = a.in1 + u * a.ld1 + c;
+            else if (c - a.c1 < a.c2) src = a.in2 + u * a.ld2 + (c - a.c1);
+            else ok = false;
+            cp_async16(dA + mn_off((tid >> 6) + 2 * r, w, 128), ok ? src : a.in1, ok);
+        }
+        unsigned char* dB = stB + st * bBytes;
+        for (int nb = tid >> 6; nb < N / 8; nb += 2) {
+            const bool ok = vin && nb * 8 < a.co;
+            cp_async16(dB + mn_off(nb, w, N), ok ? a.dout + (size_t)v * a.ldd + nb * 8 : a.dout, ok);
+        }
+    };
+
+    uint32_t ph[S];
+    bool pend[S];                    // a commit on bars[s] not yet waited for
+    for (int q = 0; q < S; q++) { ph[q] = 0; pend[q] = false; }
     // failure-detection test: a bounded wait that runs out before any MMA
-    bool ok = a.stall ? mbar_wait_tc(&bars[2], 0, 1u << 10) : true;
-    int issued = 0;                  // K steps whose MMAs were issued
-    for (int st = 0; st < nsteps; st++) {
-        const int s = st & 1;
-        if (pend[s]) {
-            if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
-            ph[s] ^= 1;
-            pend[s] = false;
+    bool ok = a.stall ? mbar_wait_tc(&bars[S], 0, 1u << 10) : true;
+    if (__syncthreads_and(ok)) {
+        for (int q = 0; q < S - 1; q++) {
+            if (q < T) issue(q);
+            cp_async_commit();
         }
-        // after a wait ran out no thread writes a stage and no MMA is issued
-        if (!__syncthreads_and(ok)) {
-            ok = false;
-            break;
-        }
-        // The operands move in 8 x 8 blocks: 8 voxels (rows 8 rg .. 8 rg + 7 of
-        // the step, the same for every block of this thread) by 8 channels,
-        // loaded as 8 rows of 16 bytes, transposed in registers and stored as
-        // 8 rows of 16 bytes of the K-major tile (K = voxel).
-        const int rg = tid & 7;
-        int vA[8], vB[8];            // the voxels for dout, and at the tap's offset for the input (-1: zero)
-        {
-            // the block's 8 voxels are consecutive: with nx a multiple of 8 they
-            // share j and k, so one decomposition serves all of them
-            const int vb = (int)(v0 + (long long)st * KV) + rg * 8;
-            const int nxy = a.nx * a.ny;
-            int i0 = vb % a.nx, j0 = (vb / a.nx) % a.ny, k0 = vb / nxy;
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const int v = vb + u;
-                vA[u] = vB[u] = -1;
-                if (v < V && v - v0 < a.vchunk) {
-                    if (a.nx % 8) { i0 = v % a.nx; j0 = (v / a.nx) % a.ny; k0 = v / nxy; }
-                    const int iu = (a.nx % 8 ? i0 : i0 + u);
-                    vA[u] = v;
-                    const int i = iu + di, j = j0 + dj, k = k0 + dk;
-                    if (k >= 0 && k < a.nz && (a.xper || (i >= 0 && i < a.nx)) && (a.yper || (j >= 0 && j < a.ny)))
-                        vB[u] = wrap(i, a.nx) + a.nx * (wrap(j, a.ny) + a.ny * k);
+        for (int q = 0; q < T; q++) {
+            // refill the stage of step q + S - 1: the MMAs of step q - 1 read it
+            const int qn = q + S - 1;
+            if (qn < T) {
+                const int sn = qn % S;
+                if (pend[sn]) {
+                    if (!mbar_wait_tc(&bars[sn], ph[sn])) ok = false;
+                    ph[sn] ^= 1;
+                    pend[sn] = false;
                 }
             }
-        }
-        const uint4 z4 = make_uint4(0, 0, 0, 0);
-        // A[o][r] = dout[v_r][mo + o] (zero beyond co): one block per thread;
-        // blocks wholly beyond co are zero and written in the first use of
-        // each stage only
-        if (mo + (tid >> 3) * 8 < a.co || st < 2) {
-            const int og = tid >> 3, o0 = mo + og * 8;
-            uint4 rows[8], cols[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-                rows[u] = (vA[u] >= 0 && o0 < a.co)
-                              ? *reinterpret_cast<const uint4*>(a.dout + (size_t)vA[u] * a.ldd + o0) : z4;
-            transpose8x8(rows, cols);
-#pragma unroll
-            for (int c = 0; c < 8; c++)
-                *reinterpret_cast<uint4*>(stA[s] + kmajor_off(og * 8 + c, rg * 8, KV)) = o0 + c < a.co ? cols[c] : z4;
-        }
-        // B[i][r] = in[v_r + off][i]
-        for (int e = tid; e < (Kin / 8) * 8; e += 128) {
-            const int c0 = (e >> 3) * 8;
-            uint4 rows[8], cols[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                rows[u] = z4;
-                if (vB[u] >= 0) {
-                    if (c0 < a.c1) rows[u] = *reinterpret_cast<const uint4*>(a.in1 + (size_t)vB[u] * a.ld1 + c0);
-                    else if (c0 - a.c1 < a.c2)
-                        rows[u] = *reinterpret_cast<const uint4*>(a.in2 + (size_t)vB[u] * a.ld2 + (c0 - a.c1));
+            // after a wait ran out no thread copies into a stage and no MMA is issued
+            if (!__syncthreads_and(ok)) {
+                ok = false;
+                break;
+            }
+            if (qn < T) issue(qn);
+            cp_async_commit();
+            cp_async_wait<S - 1>();                  // step q's copies have landed
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            const int s = q % S;
+            if (tid == 0) {
+                for (int kk = 0; kk < KV / 16; kk++) {
+                    const uint64_t ad = smem_desc(sm_addr(stA + s * aBytes) + kk * 128 * 32, 128, 256);
+                    const uint64_t bd = smem_desc(sm_addr(stB + s * bBytes) + kk * N * 32, 128, 256);
+                    mma_bf16(tbase, ad, bd, id, q > 0 || kk > 0);
                 }
+                mma_commit(&bars[s]);
             }
-            transpose8x8(rows, cols);
-#pragma unroll
-            for (int c = 0; c < 8; c++)
-                *reinterpret_cast<uint4*>(stB[s] + kmajor_off(c0 + c, rg * 8, KV)) = cols[c];
+            pend[s] = true;
         }
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        if (tid == 0) {
-            for (int kk = 0; kk < KV / 16; kk++) {
-                const uint64_t ad = smem_desc(sm_addr(stA[s]) + kk * 256, 128, (uint32_t)KV * 16);
-                const uint64_t bd = smem_desc(sm_addr(stB[s]) + kk * 256, 128, (uint32_t)KV * 16);
-                mma_bf16(tbase, ad, bd, id, st > 0 || kk > 0);
-            }
-            mma_commit(&bars[s]);
-        }
-        pend[s] = true;
-        issued++;
     }
-    // the commits not yet waited for: bounded waits before the accumulator is
-    // read or freed
-    for (int s = 0; s < 2; s++)
-        if (pend[s]) {
-            if (!mbar_wait_tc(&bars[s], ph[s])) ok = false;
-            ph[s] ^= 1;
+    // the copies still in flight, and the commits not yet waited for: bounded
+    // waits before the accumulator is read or freed
+    cp_async_wait_all();
+    for (int q = 0; q < S; q++)
+        if (pend[q]) {
+            if (!mbar_wait_tc(&bars[q], ph[q])) ok = false;
+            ph[q] ^= 1;
         }
     ok = __syncthreads_and(ok);
     tc_fence_after();
-    const int o = mo + 32 * warp + lane;                 // this thread's row: output channel mo + row
-    if (ok && issued > 0) {
-        for (int c0 = 0; c0 < Kin; c0 += 16) {
+    // this thread's row: tap t, input channel ich
+    const int g = m0 + 32 * warp + lane;
+    const int t = g / a.Cp, ich = g - t * a.Cp;
+    const bool mine = t < 27 && ich < a.ci;
+    if (ok && T > 0) {
+        for (int c0 = 0; c0 < N; c0 += 16) {
             float acc[16];
             tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, acc);
-            if (o < a.co) {
+            if (mine) {
 #pragma unroll
                 for (int q = 0; q < 16; q++) {
-                    const int i = c0 + q;
-                    if (i < a.ci) atomicAdd(&a.dW[((size_t)t * a.co + o) * a.ci + i], acc[q]);
+                    const int o = c0 + q;
+                    if (o < a.co) atomicAdd(&a.dW[((size_t)t * a.co + o) * a.ci + ich], acc[q]);
                 }
             }
         }
@@ -791,27 +794,39 @@ int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c
 }
 
 int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1, int c1, const void* in2, int ld2,
-                     int c2, float* dW, int ci, int nx, int ny, int nz, int xper, int yper, int Kin, int vchunk,
-                     int* status, void* stream) {
+                     int c2, float* dW, int ci, int nx, int ny, int nz, int xper, int yper, int vchunk, int* status,
+                     void* stream) {
     if (!dout || !in1 || !dW || !status) return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: null argument");
-    if (Kin % 16 || Kin < 16 || Kin > 256 || c1 + (in2 ? c2 : 0) > Kin || ci > c1 + (in2 ? c2 : 0) || ci < 1 ||
-        co > 256 || co < 1 || vchunk % 64 || vchunk < 64 || c1 % 8 || (long long)nx * ny * nz >= (1ll << 31))
-        return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: channel counts or chunk out of range");
+    const long long V = (long long)nx * ny * nz;
+    if (ci > c1 + (in2 ? c2 : 0) || ci < 1 || co > 256 || co < 1 || vchunk < 0 || vchunk % gmnn::kWgKV || c1 % 8 ||
+        nx < 1 || ny < 1 || nz < 1 || V >= (1ll << 31))
+        return gm::fail(GM_EPARAM, "gm_nn_conv_wgrad: channel counts, grid or chunk out of range");
     int rc;
-    if ((rc = check_view_align(in1, ld1, "gm_nn_conv_wgrad in1")) || (rc = check_view_align(in2, ld2, "gm_nn_conv_wgrad in2")))
+    if ((rc = check_view_align(dout, ldd, "gm_nn_conv_wgrad dout")) ||
+        (rc = check_view_align(in1, ld1, "gm_nn_conv_wgrad in1")) || (rc = check_view_align(in2, ld2, "gm_nn_conv_wgrad in2")))
         return rc;
     WgradArgs a;
     a.dout = (const __nv_bfloat16*)dout; a.ldd = ldd; a.co = co;
     a.in1 = (const __nv_bfloat16*)in1; a.ld1 = ld1; a.c1 = c1;
     a.in2 = (const __nv_bfloat16*)in2; a.ld2 = ld2; a.c2 = in2 ? c2 : 0;
-    a.dW = dW; a.ci = ci; a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper; a.Kin = Kin; a.vchunk = vchunk;
+    a.dW = dW; a.ci = ci; a.Cp = (ci + 7) / 8 * 8; a.N = (co + 15) / 16 * 16;
+    a.nx = nx; a.ny = ny; a.nz = nz; a.xper = xper; a.yper = yper;
     a.status = status;
     a.stall = g_nn_stall;
-    const size_t smem = (size_t)2 * (128 + Kin) * 64 * 2 + 32;
+    const int tiles = (27 * a.Cp + 127) / 128;
+    if (vchunk == 0) {
+        // about four CTAs per SM over the grid, at least 8 steps each: fewer,
+        // longer CTAs cost fewer accumulator flushes (atomics)
+        const long long chunks = (4 * 152 + tiles - 1) / tiles;
+        long long vc = (V + chunks - 1) / chunks;
+        vc = (vc + gmnn::kWgKV - 1) / gmnn::kWgKV * gmnn::kWgKV;
+        vchunk = (int)(vc < 8 * gmnn::kWgKV ? 8 * gmnn::kWgKV : vc);
+    }
+    a.vchunk = vchunk;
+    const size_t smem = (size_t)gmnn::kWgStages * (128 + a.N) * gmnn::kWgKV * 2 + 8 * (gmnn::kWgStages + 1) + 16;
     cudaError_t e = cudaFuncSetAttribute(gmnn::k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return gm::fail(GM_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
-    const long long V = (long long)nx * ny * nz;
-    const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), 27, (unsigned)((co + 127) / 128));
+    const dim3 grid((unsigned)((V + vchunk - 1) / vchunk), (unsigned)tiles);
     gmnn::k_conv_wgrad<<<grid, 128, smem, (cudaStream_t)stream>>>(a);
     e = cudaGetLastError();
     return e == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, std::string("k_conv_wgrad: ") + cudaGetErrorString(e));

@@ -157,8 +157,7 @@ class UNet:
         nx, ny, nz = self.dims[lvl]
         check(self.lib.gm_nn_conv_wgrad(dout[0], dout[1], L.co, src[0], src[1], L.view, None, 0, 0,
                                         C.cast(L.gW.data_ptr(), C.POINTER(C.c_float)), L.ci, nx, ny, nz, self.xper,
-                                        self.yper, L.kin, 2048 if lvl == 0 else 512,
-                                        C.c_void_p(self.status.data_ptr()), C.c_void_p(self.stream)),
+                                        self.yper, 0, C.c_void_p(self.status.data_ptr()), C.c_void_p(self.stream)),
               "gm_nn_conv_wgrad")
         check(self.lib.gm_nn_bias_grad(dout[0], dout[1], L.co, self.V[lvl],
                                        C.cast(L.gb.data_ptr(), C.POINTER(C.c_float)), C.c_void_p(self.stream)),

@@ -426,12 +426,15 @@ int gm_nn_tc_gemm_check(const void* A, const void* B, float* D, int N, int K, in
 int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c2, const void* W, const float* bias,
                void* out, int ldo, int co, const void* mask, int ldm, int relu, int nx, int ny, int nz, int xper,
                int yper, int Kc, int Np, int* status, void* stream);
-/* dW[t][o][i] += sum_v dout[v][o] in[v + off(t)][i] (FP32, i < ci), on the
- * tensor cores over voxel chunks of vchunk (a multiple of 64); Kin >= c1 + c2
- * a multiple of 16 <= 256, co <= 256 (output channels in tiles of 128). */
+/* dW[t][o][i] += sum_v dout[v][o] in[v + off(t)][i] (FP32, i < ci <= c1 +
+ * c2, o < co <= 256), on the tensor cores: one GEMM per chunk of vchunk voxels
+ * (a multiple of 64; 0 lets the library choose) with the 27 taps' input
+ * channels stacked as its rows, in tiles of 128.  dout is read up to co
+ * rounded up to 8 channels, the input views up to ci rounded up to 8; every
+ * view starts on 16 bytes with a channel stride that is a multiple of 8. */
 int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1, int c1, const void* in2, int ld2,
-                     int c2, float* dW, int ci, int nx, int ny, int nz, int xper, int yper, int Kin, int vchunk,
-                     int* status, void* stream);
+                     int c2, float* dW, int ci, int nx, int ny, int nz, int xper, int yper, int vchunk, int* status,
+                     void* stream);
 /* db[o] += sum_v d[v][o]. */
 int gm_nn_bias_grad(const void* d, int ld, int c, long long V, float* db, void* stream);
 /* 2x2x2 mean pooling of the fine grid (nx, ny, nz) and its adjoint
