@@ -1,7 +1,8 @@
 """Benchmark of the relaxation hot path (one JSON line on stdout).
 
 Workload: the six-blob braid on 128x128x256 inner points (periodic x, y;
-line-tied z), FP32 storage with the FP64 error norm and controller.  A step
+line-tied z), FP32 storage with the cancellation-free error norm (errMode 1)
+and the FP64 controller.  A step
 is one attempted adaptive Runge-Kutta step (6 stages + accept/reject) over
 the whole grid; the metric is cell-RK-stages/s = N x 6 x steps / time.
 
@@ -74,7 +75,8 @@ def workload_config(p, extra=None):
         "workload": name,
         "grid": [p.nx, p.ny, p.nz],
         "storage": "fp32" if p.precision == 32 else "fp64",
-        "error_norm": ("errMode 1: |sum (c - c*) k| in fp64, the FP32 default" if p.errMode == 1 else
+        "error_norm": ("errMode 1 (the FP32 default): |sum (c - c*) k| per point in the run precision, "
+                       "its maximum, t, dt and the controller in fp64" if p.errMode == 1 else
                        "errMode 0: |x_new - x*| in the run precision, as the reference"),
         "step": "one attempted adaptive Cash-Karp RK step (6 stages + accept/reject)",
         "l2": f"working set ~{p.nx * p.ny * p.nz * 117 * (p.precision // 8) / 1e9:.1f} GB > 129 MB L2 "

@@ -945,15 +945,16 @@ struct Batch : BatchBase {
         return GM_OK;
     }
 
-    // Work items of depth tzb planes, largest cases first; the cases' TZ and
-    // the device copies follow.
-    int set_work(int tzb) {
+    // Work items of depth tzb planes, largest cases first, of every case or
+    // only of the cases in *only; the cases' TZ and the device copies follow.
+    int set_work(int tzb, const std::vector<int>* only = nullptr) {
         TZB = tzb;
         std::vector<std::pair<long long, int>> order;
         for (int c = 0; c < ncases; c++) {
             hcases[c].a.TZ = TZB;
             const gm_params& p = params[c];
-            order.emplace_back(-(long long)p.nx * p.ny * p.nz, c);
+            if (!only || std::find(only->begin(), only->end(), c) != only->end())
+                order.emplace_back(-(long long)p.nx * p.ny * p.nz, c);
         }
         std::sort(order.begin(), order.end());
         std::vector<int4> work;
@@ -1101,10 +1102,31 @@ struct Batch : BatchBase {
         return GM_OK;
     }
 
+    // Work items of the cases in `cases` at depth tzb.
+    long long count_items(int tzb, const std::vector<int>& cases) const {
+        long long n = 0;
+        for (int c : cases) {
+            const gm_params& p = params[c];
+            n += (long long)((p.nx + gmk::TX - 1) / gmk::TX) * ((p.ny + gmk::STAGE_BATCH_TY - 1) / gmk::STAGE_BATCH_TY) *
+                 ((p.nz + tzb - 1) / tzb);
+        }
+        return n;
+    }
+
     int run(int nCycle, double residual, int pointwise, int checkEvery, gm_batch_case* out) override {
         if (!uploaded_all()) return gm::fail(GM_ENOTREADY, "gm_batch_run before every case is uploaded");
         if (checkEvery < 1 || nCycle < 0) return gm::fail(GM_EPARAM, "gm_batch_run: checkEvery >= 1, nCycle >= 0");
+        int rc = run_pending(nCycle, residual, pointwise, checkEvery, out);
+        // the full work list at the depth the run started with, for later steps
+        const int rc2 = set_work(tuned_tzb);
+        return rc ? rc : rc2;
+    }
+
+    int tuned_tzb = 32;
+
+    int run_pending(int nCycle, double residual, int pointwise, int checkEvery, gm_batch_case* out) {
         int rc;
+        tuned_tzb = TZB;
         for (int c = 0; c < ncases; c++) {
             Impl<T>& im = *cs[c];
             if ((rc = im.read_state())) return rc;
@@ -1148,6 +1170,16 @@ struct Batch : BatchBase {
                 } else {
                     still.push_back(c);
                 }
+            }
+            // As cases finish, the work list keeps only the running ones (no
+            // CTA spends a claim on a stopped case), and where the depth the
+            // run started with would leave fewer than two items per resident
+            // CTA, 16-plane items spread the remaining cases over the SMs.
+            // The depth does not change any result.
+            if (!still.empty() && still.size() < pending.size()) {
+                int tz = tuned_tzb;
+                if (tz > 16 && count_items(tz, still) < 2LL * nblocks) tz = 16;
+                if ((rc = set_work(tz, &still))) return rc;
             }
             pending.swap(still);
         }

@@ -175,14 +175,15 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
             else ok8 = false;
             cp_async16(dA + kmajor_off(tid, c, KCH), ok8 ? src : a.in1, ok8);
         }
-        // B: the slice's Np x kcw weights of the tap
+        // B: the slice's Np x kcw weights of the tap.  A thread copies 8
+        // channels (cc) of rows tid % 16, tid % 16 + 16, ...: the 8 lanes of a
+        // shared-memory store phase write the 8 rows of one core matrix
         const __nv_bfloat16* Wt = a.W + ((size_t)t * a.Np + n0) * Kc + kc0;
         unsigned char* dB = stB + st * bBytes;
-        const int cpr = kcw / 8;                     // 16-byte chunks per row
-        for (int e = tid; e < Np * cpr; e += 128) {
-            const int r = e / cpr, c = (e % cpr) * 8;
-            cp_async16(dB + kmajor_off(r, c, KCH), Wt + (size_t)r * Kc + c, true);
-        }
+        const int cc = (tid >> 4) * 8;               // KCH <= 64: eight 8-channel columns
+        if (cc < kcw)
+            for (int r = tid & 15; r < Np; r += 16)
+                cp_async16(dB + kmajor_off(r, cc, KCH), Wt + (size_t)r * Kc + cc, true);
     };
 
     uint32_t ph[S];
@@ -327,14 +328,33 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
     const int T = (nv + KV - 1) / KV;                 // steps
     const int w = tid & (KV - 1);                     // this thread's voxel within a step
     const int cpb = a.Cp >> 3;                        // 8-channel groups per tap
-    // this thread's 8 row blocks of A (rb = tid / 64 + 2 r): tap and first channel
-    int tr[8], cr[8];
+    // this thread's 8 row blocks of A (rb = tid / 64 + 2 r): the tap's offset
+    // packed as (di + 1) | (dj + 1) << 2 | (dk + 1) << 4 (-1: a row beyond the
+    // 27 taps or the input's channels, zero-filled), and the source view from
+    // the block's first channel, with its channel stride
+    int tapo[8], ldr[8];
+    const __nv_bfloat16* srcr[8];
 #pragma unroll
     for (int r = 0; r < 8; r++) {
         const int g = (m0 >> 3) + (tid >> 6) + 2 * r;
-        tr[r] = g / cpb;
-        cr[r] = (g - tr[r] * cpb) * 8;
+        const int t = g / cpb, c = (g - t * cpb) * 8;
+        tapo[r] = t < 27 ? (t % 3) | (((t / 3) % 3) << 2) | ((t / 9) << 4) : -1;
+        srcr[r] = a.in1;
+        ldr[r] = 0;
+        if (c < a.c1) { srcr[r] = a.in1 + c; ldr[r] = a.ld1; }
+        else if (c - a.c1 < a.c2) { srcr[r] = a.in2 + (c - a.c1); ldr[r] = a.ld2; }
+        else tapo[r] = -1;
     }
+    // the coordinates of this thread's voxel v0 + kWgKV q + w of the next step
+    // to issue, advanced by kWgKV = si + nx (sj + ny sk) voxels per step
+    int vi, vj, vk;
+    {
+        const int v = v0 + w;
+        vi = v % a.nx;
+        vj = (v / a.nx) % a.ny;
+        vk = v / (a.nx * a.ny);
+    }
+    const int si = KV % a.nx, sj = (KV / a.nx) % a.ny, sk = KV / (a.nx * a.ny);
     uint32_t ncols = 32;
     while ((int)ncols < N) ncols <<= 1;
     if (tid == 0)
@@ -347,32 +367,38 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(const WgradArgs a) {
     // A and B both MN-major (transpose bits 15 and 16)
     const uint32_t id = idesc_bf16(128, N) | (1u << 15) | (1u << 16);
 
-    // the copies of step q into stage q % S
+    // the copies of step q into stage q % S (called for q = 0, 1, 2, ... in turn)
     auto issue = [&](int q) {
         const int st = q % S;
         const int vl = q * KV + w;
         const bool vin = vl < nv;
-        const int v = v0 + (vin ? vl : 0);
-        const int i = v % a.nx, j = (v / a.nx) % a.ny, k = v / (a.nx * a.ny);
+        const int v = v0 + vl;
         unsigned char* dA = stA + st * aBytes;
 #pragma unroll
         for (int r = 0; r < 8; r++) {
-            const int t = tr[r], c = cr[r];
-            const int ii = i + t % 3 - 1, jj = j + (t / 3) % 3 - 1, kk = k + t / 9 - 1;
-            bool ok = vin && t < 27 && kk >= 0 && kk < a.nz && (a.xper || (ii >= 0 && ii < a.nx)) &&
-                      (a.yper || (jj >= 0 && jj < a.ny));
-            const long long u = ok ? (long long)wrap(ii, a.nx) + (long long)a.nx * (wrap(jj, a.ny) + (long long)a.ny * kk) : 0;
-            const __nv_bfloat16* src = a.in1;
-            if (c < a.c1) src = a.in1 + u * a.ld1 + c;
-            else if (c - a.c1 < a.c2) src = a.in2 + u * a.ld2 + (c - a.c1);
-            else ok = false;
-            cp_async16(dA + mn_off((tid >> 6) + 2 * r, w, 128), ok ? src : a.in1, ok);
+            const int to = tapo[r];
+            int ii = vi + (to & 3) - 1, jj = vj + ((to >> 2) & 3) - 1;
+            const int kk = vk + (to >> 4) - 1;
+            const bool ok = vin && to >= 0 && kk >= 0 && kk < a.nz && (a.xper || (ii >= 0 && ii < a.nx)) &&
+                            (a.yper || (jj >= 0 && jj < a.ny));
+            ii = wrap(ii, a.nx);
+            jj = wrap(jj, a.ny);
+            const int u = ok ? ii + a.nx * (jj + a.ny * kk) : 0;
+            cp_async16(dA + mn_off((tid >> 6) + 2 * r, w, 128), ok ? srcr[r] + (size_t)u * ldr[r] : a.in1, ok);
         }
         unsigned char* dB = stB + st * bBytes;
         for (int nb = tid >> 6; nb < N / 8; nb += 2) {
             const bool ok = vin && nb * 8 < a.co;
             cp_async16(dB + mn_off(nb, w, N), ok ? a.dout + (size_t)v * a.ldd + nb * 8 : a.dout, ok);
         }
+        // the next step's voxel
+        vi += si;
+        const int cx = vi >= a.nx;
+        vi -= cx ? a.nx : 0;
+        vj += sj + cx;
+        const int cy = vj >= a.ny;
+        vj -= cy ? a.ny : 0;
+        vk += sk + cy;
     };
 
     uint32_t ph[S];

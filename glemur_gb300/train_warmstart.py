@@ -296,10 +296,51 @@ def upsample_displacement(d, f, fine, per=(True, True)):
     return out
 
 
-def evaluate_large(weights, residual, max_attempts, factor=2, log=print):
+LARGE_LEVELS = (0.4, 0.3, 0.25, 0.2, 0.15, 0.1)
+
+
+def residual_history(g, xb, B0, max_attempts, stop_at, check_every=200):
+    """Upload, then relax for at most `max_attempts` attempts or until the
+    weighted residual is at most `stop_at`, reading the residual every
+    `check_every` attempts.  Returns [(seconds, attempts, residual, min
+    Delta)], the first entry at the start, and the final status word (a
+    fold stops the run: GM_ST_DETJAC, GM_ST_DTMIN or GM_ST_NAN)."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.upload(xb, B0)
+    r = g.refresh()
+    hist = [(time.perf_counter() - t0, 0, r["residual"], r["minDetJac"])]
+    status = 0
+    while hist[-1][1] < max_attempts and hist[-1][2] > stop_at:
+        g.steps_async(check_every)
+        s = g.state()
+        r = g.refresh()
+        hist.append((time.perf_counter() - t0, s["nAttempted"], r["residual"], r["minDetJac"]))
+        status = s["status"]
+        if status & 0x17:
+            break
+    return hist, status
+
+
+def first_reach(hist, level, offset=0.0):
+    """(seconds + offset, attempts) of the first entry at or below `level`."""
+    for t, att, res, _ in hist:
+        if res <= level:
+            return t + offset, att
+    return None, None
+
+
+def evaluate_large(weights, residual, max_attempts, factors=(2, 4), log=print):
     """The large case (256x256x512, k = +-1.2, pressure with the p0 profile):
-    the network runs on a factor-x coarsened B0 and its displacement is
-    trilinearly upsampled; plain against warm start to the residual target."""
+    the network runs on B0 averaged over f x f x f blocks and its displacement
+    is trilinearly upsampled to the fine grid.  The plain run and one warm run
+    per factor record the residual every 200 attempts, up to `max_attempts`
+    or `residual`; the report gives, per residual level, the time each run
+    took to reach it (the warm start's own cost included).  A warm grid that
+    folds during the run (the controller stops on Delta <= 0, dt below dtMin
+    or a NaN) is replaced by the identity grid: the levels are then the plain
+    run's, plus the time the warm start and its run took."""
     import torch
     p = configs.braid6_large(256, 256, 512, precision=32)
     B0, xb0 = configs.init_state(p)
@@ -307,42 +348,61 @@ def evaluate_large(weights, residual, max_attempts, factor=2, log=print):
     g.upload(xb0, B0)
     g.steps_async(2)
     g.state()
-    tp, ap, rp0, mdp, okp = time_to_residual(g, p, xb0, B0, residual, max_attempts)
-    cshape = (p.nx // factor, p.ny // factor, p.nz // factor)
-    net = UNet(cshape, seed=0, wb=weights_width(weights))
-    net.load_state_dict(weights)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    Bc = coarse_b0(p, B0, factor)
-    net.set_input_b0(torch.from_numpy(Bc).cuda(), 32)
-    y = net.forward()[:, :3].float().cpu().numpy().reshape(cshape[2], cshape[1], cshape[0], 3)
-    y = smooth_displacement(y.astype(np.float64), 2)
-    # coarse grid units -> physical -> fine inner points
-    sp_c = np.array([p.dx, p.dy, p.dz]) * factor
-    d = upsample_displacement(y * sp_c, factor, (p.nx, p.ny, p.nz))
-    d[0] = 0.0
-    d[-1] = 0.0
-    xw = xb0.astype(np.float64)
-    xw[1:-1, 1:-1, 1:-1] += d
-    nx, ny = p.nx, p.ny
-    xw[:, :, 0] = xw[:, :, nx]; xw[:, :, 0, 0] -= p.Lx + p.dx
-    xw[:, :, nx + 1] = xw[:, :, 1]; xw[:, :, nx + 1, 0] += p.Lx + p.dx
-    xw[:, 0] = xw[:, ny]; xw[:, 0, :, 1] -= p.Ly + p.dy
-    xw[:, ny + 1] = xw[:, 1]; xw[:, ny + 1, :, 1] += p.Ly + p.dy
-    xw = xw.astype(np.float32)
-    g.upload(xw, B0)
-    accepted = g.refresh()["minDetJac"] > 0
-    if not accepted:
-        xw = xb0
-    t_net = time.perf_counter() - t0
-    tw, aw, rw0, mdw, okw = time_to_residual(g, p, xw, B0, residual, max_attempts)
-    tw += t_net
+    plain, _ = residual_history(g, xb0, B0, max_attempts, residual)
+    out = dict(shape=(p.nx, p.ny, p.nz), max_attempts=max_attempts,
+               plain=dict(res0=plain[0][2], res_end=plain[-1][2], attempts=plain[-1][1], s=plain[-1][0],
+                          minDet=min(h[3] for h in plain), history=[(round(h[0], 3), h[1], h[2]) for h in plain[::5]]),
+               warm={})
+    log(f"large plain: {out['plain']}")
+    for f in factors:
+        cshape = (p.nx // f, p.ny // f, p.nz // f)
+        net = UNet(cshape, seed=0, wb=weights_width(weights))
+        net.load_state_dict(weights)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Bc = coarse_b0(p, B0, f)
+        net.set_input_b0(torch.from_numpy(Bc).cuda(), 32)
+        y = net.forward()[:, :3].float().cpu().numpy().reshape(cshape[2], cshape[1], cshape[0], 3)
+        y = smooth_displacement(y.astype(np.float64), 2)
+        # coarse grid units -> physical -> fine inner points
+        sp_c = np.array([p.dx, p.dy, p.dz]) * f
+        d = upsample_displacement(y * sp_c, f, (p.nx, p.ny, p.nz))
+        d[0] = 0.0
+        d[-1] = 0.0
+        xw = xb0.astype(np.float64)
+        xw[1:-1, 1:-1, 1:-1] += d
+        nx, ny = p.nx, p.ny
+        xw[:, :, 0] = xw[:, :, nx]; xw[:, :, 0, 0] -= p.Lx + p.dx
+        xw[:, :, nx + 1] = xw[:, :, 1]; xw[:, :, nx + 1, 0] += p.Lx + p.dx
+        xw[:, 0] = xw[:, ny]; xw[:, 0, :, 1] -= p.Ly + p.dy
+        xw[:, ny + 1] = xw[:, 1]; xw[:, ny + 1, :, 1] += p.Ly + p.dy
+        xw = xw.astype(np.float32)
+        g.upload(xw, B0)
+        accepted = g.refresh()["minDetJac"] > 0
+        if not accepted:
+            xw = xb0
+        t_net = time.perf_counter() - t0
+        del net
+        warm, wstat = residual_history(g, xw, B0, max_attempts, residual)
+        folded = bool(wstat & 0x7) and warm[-1][2] > residual
+        spent = warm[-1][0] + t_net
+        levels = {}
+        for lv in LARGE_LEVELS:
+            tp, ap = first_reach(plain, lv)
+            if folded:
+                tw, aw = first_reach(plain, lv, spent)
+                aw = aw + warm[-1][1] if aw is not None else None
+            else:
+                tw, aw = first_reach(warm, lv, t_net)
+            levels[str(lv)] = dict(plain_s=tp, plain_attempts=ap, warm_s=tw, warm_attempts=aw,
+                                   speedup=(tp / tw) if (tp and tw) else None)
+        out["warm"][str(f)] = dict(coarse_shape=cshape, accepted=bool(accepted), net_s=t_net, res0=warm[0][2],
+                                   res_end=warm[-1][2], attempts=warm[-1][1], s=spent, status=wstat,
+                                   folded_in_run=folded, minDet=min(h[3] for h in warm), levels=levels,
+                                   history=[(round(h[0], 3), h[1], h[2]) for h in warm[::5]])
+        log(f"large warm, factor {f}: {out['warm'][str(f)]}")
     g.close()
-    row = dict(shape=(p.nx, p.ny, p.nz), factor=factor, plain_s=tp, plain_attempts=ap, plain_reached=okp,
-               plain_res0=rp0, plain_minDet=mdp, warm_s=tw, warm_attempts=aw, warm_reached=okw, warm_res0=rw0,
-               warm_minDet=mdw, accepted=bool(accepted), net_s=t_net)
-    log(f"large: {row}")
-    return row
+    return out
 
 
 def evaluate_batched(net, seeds, residual, max_cycles, smooth=2, chunk=64, log=print):
@@ -450,6 +510,7 @@ def main(argv=None):
     ap.add_argument("--large", action="store_true", help="also evaluate the 256x256x512 pressure case")
     ap.add_argument("--large-residual", type=float, default=0.0,
                     help="residual target of the large case (default: --residual)")
+    ap.add_argument("--large-attempts", type=int, default=24000, help="attempts per run of the large case at most")
     ap.add_argument("--smooth", default="2", help="comma-separated box-filter passes to evaluate")
     ap.add_argument("--tta", default="1", help="comma-separated numbers of input translations to average")
     ap.add_argument("--wb", type=int, default=WB, help="bottleneck channels of a network trained here")
@@ -492,7 +553,7 @@ def main(argv=None):
                                              a.residual, a.max_cycles, smooth=best[0], log=log)
         log("batched: " + json.dumps(report["batched"]["summary"]))
     if a.large:
-        report["large"] = evaluate_large(net.state_dict(), a.large_residual or a.residual, 4 * a.max_cycles, log=log)
+        report["large"] = evaluate_large(net.state_dict(), a.large_residual or a.residual, a.large_attempts, log=log)
     log(json.dumps(report.get("summary")))
     if a.report:
         with open(a.report, "w") as f:

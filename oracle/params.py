@@ -76,8 +76,9 @@ def _flit(v: float) -> float:
 
 def defaults(precision: int) -> Params:
     """The namelist variables' initial values, src/readNamelist.f90:91-150,
-    plus this library's extensions (errMode: the FP64 error norm in FP32
-    runs; p0Amp, p0Width: the pressure profile, off)."""
+    plus this library's extensions (errMode: the cancellation-free error
+    norm |sum (c - c*) k| of FP32 runs; p0Amp, p0Width: the pressure
+    profile, off)."""
     p = Params()
     p.precision = precision
     p.nx = p.ny = p.nz = 16

@@ -98,9 +98,9 @@ RUN_TOL = {64: dict(t=1e-6, x=1e-10, B=1e-9, J=1e-8, red=1e-7), 32: dict(t=5e-3,
 def test_run_matches_oracle(name):
     p = cases.make(name)
     if p.precision == 32:
-        # FP64 error norm and a first step whose error is well above float
-        # rounding of the increments, so accept/reject and dt are decided by
-        # the truncation error rather than by rounding noise
+        # cancellation-free error norm, and a first step whose error is well
+        # above float rounding of the increments, so accept/reject and dt are
+        # decided by the truncation error rather than by rounding noise
         p.errMode = 1
         p.dt0 = 0.2
     rt = dict(RUN_TOL[p.precision])

@@ -1,7 +1,8 @@
 """What FP32 storage costs the relaxation at production size: the six-blob
 braid on 128x128x256 inner points (the bench workload), run with FP32 storage
-and the FP64 error norm (errMode 1, the FP32 default) and in FP64 with the
-reference's arithmetic (errMode 0), compared at matched physical time.
+and the cancellation-free error norm (errMode 1, the FP32 default) and in
+FP64 with the reference's arithmetic (errMode 0), compared at matched
+physical time.
 
 The two runs take different dt sequences, so they are compared at the FP32
 run's time t32 after N accepted steps: the FP64 grid is interpolated linearly

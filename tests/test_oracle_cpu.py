@@ -357,8 +357,8 @@ def test_sheared_initial_grid_ghost_planes_follow_the_shear():
 
 def test_fp32_storage_error_against_fp64():
     """What FP32 storage costs the relaxation: the six-blob braid at
-    32x32x64 run 500 accepted steps with FP32 storage (FP64 error norm,
-    errMode = 1) and, to the same physical time, in FP64 (positions
+    32x32x64 run 500 accepted steps with FP32 storage (the cancellation-free
+    error norm, errMode = 1) and, to the same physical time, in FP64 (positions
     interpolated linearly in t between the two FP64 steps around it).  The
     positions then differ by about 3.4e-3 of the largest displacement and the
     force-free residual by about 0.2 %.  (The GPU's FP32 path matches the
