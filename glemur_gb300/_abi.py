@@ -167,11 +167,11 @@ SIGNATURES = {
     "gm_nn_upsample": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, VP]),
     "gm_nn_relu_bwd": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, C.c_longlong, VP]),
     "gm_nn_mse": (C.c_int, [VP, C.c_int, P(C.c_float), VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
-                            P(C.c_float), C.c_int, C.c_int, VP]),
+                            P(C.c_float), C.c_int, C.c_int, C.c_int, VP]),
     "gm_nn_adam": (C.c_int, [P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float),
                              P(C.c_float), P(C.c_float), C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
                              C.c_float, VP, C.c_int, C.c_int, VP, C.c_int, C.c_int, P(C.c_float), VP]),
-    "gm_nn_input": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, VP, C.c_int, C.c_int, C.c_int, VP]),
+    "gm_nn_input": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, VP, C.c_int, C.c_int, C.c_int, C.c_int, VP]),
     "gm_nn_disp_accumulate": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
                                          C.c_int, VP, VP]),
     "gm_nn_warm_grid": (C.c_int, [VP, P(GmParams), C.c_int, VP, VP, VP, VP]),

@@ -87,17 +87,17 @@ struct ConvArgs {
     int nx, ny, nz, xper, yper;
     int Kc, Np;                              // padded input channels (multiple of 16), padded outputs
     int Nt;                                  // output channels per CTA (multiple of 16; blockIdx.y picks the slice)
-    int Kch;                                 // input channels per pipeline step (min(Kc, kConvKc), multiple of 16)
+    int Kch;                                 // input channels per pipeline step (multiple of 16)
     int* status;
     int stall;                               // failure-detection test: wait on an mbarrier nothing arrives on
 };
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// Pipeline of the convolution: a step is one tap and one chunk of up to
-// kConvKc input channels (Kch = min(Kc, kConvKc), so that narrow layers keep
-// small stages and many CTAs per SM); kConvStages steps of operands are in
-// flight.
+// Pipeline of the convolution: a step is one tap and one chunk of the input
+// channels, all of them up to 96 (one step per tap), else chunks of kConvKc
+// (so that the stages stay small enough for two CTAs per SM);
+// kConvStages steps of operands are in flight.
 constexpr int kConvKc = 64;
 constexpr int kConvStages = 4;
 
@@ -568,18 +568,43 @@ __global__ void k_relu_bwd(__nv_bfloat16* __restrict__ d, int ldd, const __nv_bf
 // Masked mean-square error of the 3 output channels against the target
 // (FP32, [V][3]); planes k = 0 and nz-1 are excluded (their displacement is
 // imposed to be zero).  Writes the gradient (BF16) and adds the loss sum.
+// A training sample moved by a symmetry of the periodic cross-section: the
+// value at cell (i, j) is read at the source cell u = (i + sx) mod nx,
+// v = (j + sy) mod ny, then (sym & 4) u <-> v, (sym & 2) v -> ny - 1 - v,
+// (sym & 1) u -> nx - 1 - u; a vector's x, y components are transformed as the
+// positions (x negated for bit 1, y for bit 2, then swapped for bit 4), so
+// the field and the displacement stay a solution pair of the relaxation (the
+// force J x B transforms as a polar vector under reflections).
+__device__ __forceinline__ void sym_source(int i, int j, int nx, int ny, int sx, int sy, int sym, int* is, int* js) {
+    int u = (i + sx) % nx, v = (j + sy) % ny;
+    if (sym & 4) { const int w = u; u = v; v = w; }
+    if (sym & 2) v = ny - 1 - v;
+    if (sym & 1) u = nx - 1 - u;
+    *is = u;
+    *js = v;
+}
+__device__ __forceinline__ void sym_vector(int sym, float* vx, float* vy) {
+    if (sym & 1) *vx = -*vx;
+    if (sym & 2) *vy = -*vy;
+    if (sym & 4) { const float w = *vx; *vx = *vy; *vy = w; }
+}
+
 __global__ void k_mse(const __nv_bfloat16* __restrict__ y, int ldy, const float* __restrict__ tgt,
                       __nv_bfloat16* __restrict__ dy, int lddy, int nx, int ny, int nz, float scale,
-                      float* __restrict__ loss, int sx, int sy) {
+                      float* __restrict__ loss, int sx, int sy, int sym) {
     __shared__ float red[256];
     const long long V = (long long)nx * ny * nz;
     float s = 0.f;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long long)nx * ny));
         const bool in = k > 0 && k < nz - 1;
-        const long long vt = (long long)((i + sx) % nx) + (long long)nx * (((j + sy) % ny) + (long long)ny * k);
+        int is, js;
+        sym_source(i, j, nx, ny, sx, sy, sym, &is, &js);
+        const long long vt = (long long)is + (long long)nx * (js + (long long)ny * k);
+        float t[3] = {tgt[3 * vt], tgt[3 * vt + 1], tgt[3 * vt + 2]};
+        sym_vector(sym, &t[0], &t[1]);
         for (int c = 0; c < 3; c++) {
-            const float e = in ? __bfloat162float(y[v * ldy + c]) - tgt[3 * vt + c] : 0.f;
+            const float e = in ? __bfloat162float(y[v * ldy + c]) - t[c] : 0.f;
             s += e * e;
             dy[v * lddy + c] = __float2bfloat16_rn(2.f * scale * e);
         }
@@ -635,21 +660,21 @@ __global__ void k_adam(float* __restrict__ W, float* __restrict__ mW, float* __r
 
 // Input channels (B0x, B0y, B0z - 1) of the inner points, from the ghosted
 // AoS B0 of the reference layout (REAL T); ld channels, the rest zero.
-// The field is read at (i + sx, j + sy) (periodic): a whole-cell translation
-// of the sample, used to augment training data on the periodic axes.
+// The sample is moved by a symmetry of the periodic cross-section (sym_source,
+// sym_vector): whole-cell translations, mirrors and the x <-> y swap, used to
+// augment training data.
 template <typename T>
 __global__ void k_input(const T* __restrict__ B0, int nx, int ny, int nz, __nv_bfloat16* __restrict__ x, int ld,
-                        int sx, int sy) {
+                        int sx, int sy, int sym) {
     const long long V = (long long)nx * ny * nz;
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(v % nx), j = (int)((v / nx) % ny), k = (int)(v / ((long long)nx * ny));
-        const int is = (i + sx) % nx, js = (j + sy) % ny;
+        int is, js;
+        sym_source(i, j, nx, ny, sx, sy, sym, &is, &js);
         const long long g = (long long)(is + 1) + (long long)(nx + 2) * ((js + 1) + (long long)(ny + 2) * (k + 1));
-        for (int c = 0; c < ld; c++) {
-            float val = 0.f;
-            if (c < 3) val = (float)B0[3 * g + c] - (c == 2 ? 1.f : 0.f);
-            x[v * ld + c] = __float2bfloat16_rn(val);
-        }
+        float b[3] = {(float)B0[3 * g], (float)B0[3 * g + 1], (float)B0[3 * g + 2] - 1.f};
+        sym_vector(sym, &b[0], &b[1]);
+        for (int c = 0; c < ld; c++) x[v * ld + c] = __float2bfloat16_rn(c < 3 ? b[c] : 0.f);
     }
 }
 
@@ -793,7 +818,9 @@ int gm_nn_conv(const void* in1, int ld1, int c1, const void* in2, int ld2, int c
     // output channels per CTA: all of them when the operand stages fit the
     // shared memory, else the widest multiple of 16 that fits (slices in
     // blockIdx.y)
-    const int Kch = Kc < gmnn::kConvKc ? Kc : gmnn::kConvKc;
+    // input channels per pipeline step: all of them up to 96 (one step per
+    // tap), else kConvKc
+    const int Kch = Kc <= 96 ? Kc : gmnn::kConvKc;
     auto conv_smem = [Kch](int nt) { return (size_t)gmnn::kConvStages * (128 + nt) * Kch * 2 + 64; };
     int Nt = Np;
     while (Nt > 16 && conv_smem(Nt) > 200 * 1024) Nt -= 16;
@@ -882,16 +909,18 @@ int gm_nn_upsample(const void* in, int ldi, void* out, int ldo, int c, int nx, i
     return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_upsample");
 }
 
-int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, int sx, int sy,
+int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, int sx, int sy, int sym,
                 void* stream) {
     if (sx < 0 || sx >= nx || sy < 0 || sy >= ny) return gm::fail(GM_EPARAM, "gm_nn_input: shift out of range");
+    if (sym < 0 || sym > 7 || ((sym & 4) && nx != ny))
+        return gm::fail(GM_EPARAM, "gm_nn_input: sym is 0..7, and the x <-> y swap needs nx == ny");
     const long long V = (long long)nx * ny * nz;
     if (precision == 32)
         gmnn::k_input<float><<<gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>((const float*)B0, nx, ny, nz,
-                                                                              (__nv_bfloat16*)x, ld, sx, sy);
+                                                                              (__nv_bfloat16*)x, ld, sx, sy, sym);
     else
         gmnn::k_input<double><<<gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>((const double*)B0, nx, ny, nz,
-                                                                               (__nv_bfloat16*)x, ld, sx, sy);
+                                                                               (__nv_bfloat16*)x, ld, sx, sy, sym);
     return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_input");
 }
 
@@ -941,11 +970,13 @@ int gm_nn_relu_bwd(void* d, int ldd, const void* y, int ldy, int c, long long V,
 }
 
 int gm_nn_mse(const void* y, int ldy, const float* tgt, void* dy, int lddy, int nx, int ny, int nz, float scale,
-              float* loss, int sx, int sy, void* stream) {
+              float* loss, int sx, int sy, int sym, void* stream) {
     if (sx < 0 || sx >= nx || sy < 0 || sy >= ny) return gm::fail(GM_EPARAM, "gm_nn_mse: shift out of range");
+    if (sym < 0 || sym > 7 || ((sym & 4) && nx != ny))
+        return gm::fail(GM_EPARAM, "gm_nn_mse: sym is 0..7, and the x <-> y swap needs nx == ny");
     const long long V = (long long)nx * ny * nz;
     gmnn::k_mse<<<gmnn::nb(V) > 256 ? 256 : gmnn::nb(V), 256, 0, (cudaStream_t)stream>>>(
-        (const __nv_bfloat16*)y, ldy, tgt, (__nv_bfloat16*)dy, lddy, nx, ny, nz, scale, loss, sx, sy);
+        (const __nv_bfloat16*)y, ldy, tgt, (__nv_bfloat16*)dy, lddy, nx, ny, nz, scale, loss, sx, sy, sym);
     return cudaGetLastError() == cudaSuccess ? GM_OK : gm::fail(GM_ECUDA, "k_mse");
 }
 

@@ -72,8 +72,12 @@ def make_data(seeds, residual, max_cycles, log=print):
     return data
 
 
-def train(net, data, minutes, lr=1e-3, batch=4, log=print):
-    """Adam with cosine decay over a wall-clock budget; returns the loss history."""
+def train(net, data, minutes, lr=1e-3, batch=4, log=print, symmetries=True):
+    """Adam with cosine decay over a wall-clock budget; returns the loss
+    history.  Each sample is moved by a random whole-cell translation along
+    the periodic axes and, with `symmetries`, a random mirror / x <-> y swap
+    of the cross-section (gm_nn_input): exact copies of the problem, so a
+    pair stands for 8 nx ny pairs."""
     import torch
     nx, ny, nz = net.shape
     scale = 1.0 / (batch * nx * ny * nz * 3)
@@ -93,11 +97,13 @@ def train(net, data, minutes, lr=1e-3, batch=4, log=print):
             net.zero_grad()
             for k in order[q:q + batch]:
                 B0, tgt = data[k]
-                # whole-cell translations along the periodic axes: exact copies of the problem
+                # whole-cell translations along the periodic axes and the
+                # mirrors / swap of the cross-section: exact copies of the problem
                 sh = (int(rng.integers(nx)), int(rng.integers(ny)))
-                net.set_input_b0(B0, 32, sh)
+                sym = int(rng.integers(8 if nx == ny else 4)) if symmetries else 0
+                net.set_input_b0(B0, 32, sh, sym)
                 net.forward()
-                net.backward(tgt, scale, sh)
+                net.backward(tgt, scale, sh, sym)
             net.refresh_weights(lr=lr_t, step=True)
             step += 1
             if step % 25 == 0:
@@ -506,6 +512,11 @@ def main(argv=None):
     ap.add_argument("--out", default="")
     ap.add_argument("--report", default="")
     ap.add_argument("--weights", default="", help="evaluate these weights instead of training")
+    ap.add_argument("--init", default="", help="start training from these weights (fine-tuning)")
+    ap.add_argument("--train-offset", type=int, default=0,
+                    help="first training seed: TRAIN_SEED0 + this (braids beyond those of an --init network)")
+    ap.add_argument("--no-symmetries", action="store_true",
+                    help="augment with translations only (no mirrors / x <-> y swap)")
     ap.add_argument("--shape", default="64,64,128", help="grid (nx,ny,nz), each divisible by 4")
     ap.add_argument("--large", action="store_true", help="also evaluate the 256x256x512 pressure case")
     ap.add_argument("--large-residual", type=float, default=0.0,
@@ -521,19 +532,25 @@ def main(argv=None):
     SHAPE = tuple(int(v) for v in a.shape.split(","))
     log = lambda m: print(m, flush=True)
     w = load_weights(a.weights) if a.weights else None
-    wb = weights_width(w) if w is not None else a.wb
+    w0 = load_weights(a.init) if a.init else None
+    wb = weights_width(w) if w is not None else (weights_width(w0) if w0 is not None else a.wb)
     net = UNet(SHAPE, seed=7, wb=wb)
     log(f"U-Net: {n_params(wb)} parameters")
     report = dict(shape=SHAPE, residual=a.residual, params=n_params(wb), wb=wb)
     if w is not None:
         net.load_state_dict(w)
     else:
+        if w0 is not None:
+            net.load_state_dict(w0)
+            report.update(init=a.init)
         t0 = time.perf_counter()
-        data = make_data([TRAIN_SEED0 + i for i in range(a.train)], a.residual, a.max_cycles, log)
-        report.update(train_pairs=len(data), data_s=time.perf_counter() - t0,
+        seeds = [TRAIN_SEED0 + a.train_offset + i for i in range(a.train)]
+        data = make_data(seeds, a.residual, a.max_cycles, log)
+        report.update(train_seeds=[seeds[0], seeds[-1]], train_pairs=len(data), data_s=time.perf_counter() - t0,
+                      symmetries=not a.no_symmetries,
                       target_rms=float(np.sqrt(np.mean([float((t.double() ** 2).mean()) for _, t in data]))))
         log(f"target rms {report['target_rms']:.3f} grid spacings")
-        hist = train(net, data, a.minutes, lr=a.lr, log=log)
+        hist = train(net, data, a.minutes, lr=a.lr, log=log, symmetries=not a.no_symmetries)
         report.update(train_steps=hist[-1][0] if hist else 0, loss_first=hist[0][2] if hist else None,
                       loss_last=hist[-1][2] if hist else None)
         if a.out:

@@ -178,12 +178,14 @@ class UNet:
               "gm_nn_relu_bwd")
 
     # -- the network ----------------------------------------------------------
-    def set_input_b0(self, B0_dev, precision, shift=(0, 0)):
+    def set_input_b0(self, B0_dev, precision, shift=(0, 0), sym=0):
         """B0: device array of the reference layout (ghosted AoS, REAL), read
-        translated by `shift` whole cells in x and y (periodic)."""
+        translated by `shift` whole cells in x and y (periodic) and moved by
+        the mirror / swap symmetry `sym` (bits of gm_nn_input)."""
         nx, ny, nz = self.shape
         check(self.lib.gm_nn_input(C.c_void_p(B0_dev.data_ptr()), precision, nx, ny, nz,
-                                   self.v("X0")[0], 8, shift[0], shift[1], C.c_void_p(self.stream)), "gm_nn_input")
+                                   self.v("X0")[0], 8, shift[0], shift[1], sym, C.c_void_p(self.stream)),
+              "gm_nn_input")
 
     def forward(self):
         Ls, v = self.layers, self.v
@@ -211,15 +213,15 @@ class UNet:
                 check(self.lib.gm_nn_zero(C.c_void_p(t.data_ptr()), t.numel() * 4, C.c_void_p(self.stream)), "zero")
         check(self.lib.gm_nn_zero(C.c_void_p(self.loss_acc.data_ptr()), 4, C.c_void_p(self.stream)), "zero")
 
-    def backward(self, target, scale, shift=(0, 0)):
+    def backward(self, target, scale, shift=(0, 0), sym=0):
         """Loss scale * sum (y - target)^2 (planes 1..nz-2, 3 channels) and the
         accumulation of every weight gradient; target: float32 [V][3] on the
-        device, read translated by `shift` as the input was."""
+        device, moved by `shift` and `sym` as the input was."""
         Ls, v = self.layers, self.v
         nx, ny, nz = self.shape
         check(self.lib.gm_nn_mse(v("Y")[0], 8, C.cast(target.data_ptr(), C.POINTER(C.c_float)), v("dY")[0], 8,
                                  nx, ny, nz, C.c_float(scale), C.cast(self.loss_acc.data_ptr(), C.POINTER(C.c_float)),
-                                 shift[0], shift[1], C.c_void_p(self.stream)), "gm_nn_mse")
+                                 shift[0], shift[1], sym, C.c_void_p(self.stream)), "gm_nn_mse")
         L = Ls["head"]
         self._wgrad(L, v("dY"), v("D0b"), 0)
         self._conv(L, v("dY"), v("dD0b"), 24, 0, False, mask=v("D0b"), backward=True, src_c=8)

@@ -448,9 +448,10 @@ int gm_nn_upsample(const void* in, int ldi, void* out, int ldo, int c, int nx, i
 int gm_nn_relu_bwd(void* d, int ldd, const void* y, int ldy, int c, long long V, void* stream);
 /* loss += scale sum (y - tgt)^2 over channels 0..2 and planes 1..nz-2;
  * dy = 2 scale (y - tgt) there and 0 on the first and last planes; tgt FP32
- * [V][3], read at (i + sx, j + sy) (periodic), as gm_nn_input's input. */
+ * [V][3], moved by the translation (sx, sy) and symmetry `sym` as
+ * gm_nn_input's input. */
 int gm_nn_mse(const void* y, int ldy, const float* tgt, void* dy, int lddy, int nx, int ny, int nz, float scale,
-              float* loss, int sx, int sy, void* stream);
+              float* loss, int sx, int sy, int sym, void* stream);
 /* Adam step t (t = 0: no update) of FP32 W[27][co][ci], b[co] with their
  * moments and gradients, then the BF16 operand layouts Wf[27][Npo][Kci]
  * (forward) and Wb[27][Npi][Kco] (input gradient: taps flipped, transposed)
@@ -460,9 +461,13 @@ int gm_nn_adam(float* W, float* mW, float* vW, const float* gW, float* b, float*
                int Kco, float* bpad, void* stream);
 /* Network input from B0 on the device (reference layout, REAL of
  * `precision`): channels (B0x, B0y, B0z - 1) of the inner points, ld
- * channels, the field read at (i + sx, j + sy) (periodic; 0 <= sx < nx,
- * 0 <= sy < ny): a whole-cell translation for data augmentation. */
-int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, int sx, int sy,
+ * channels, the sample moved by a symmetry of the periodic cross-section for
+ * data augmentation: cell (i, j) reads the source cell u = (i + sx) mod nx,
+ * v = (j + sy) mod ny (0 <= sx < nx, 0 <= sy < ny), then, by the bits of
+ * `sym` (0..7), 4: u <-> v (nx == ny only), 2: v -> ny - 1 - v, 1: u -> nx -
+ * 1 - u; the vector's x, y components follow as polar vectors (x negated for
+ * bit 1, y for bit 2, then swapped for bit 4). */
+int gm_nn_input(const void* B0, int precision, int nx, int ny, int nz, void* x, int ld, int sx, int sy, int sym,
                 void* stream);
 /* Test-time translation averaging of the warm-start network: the displacement
  * channels 0..2 of an output y (BF16 [V][ldy], in grid spacings) computed on

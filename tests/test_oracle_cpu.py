@@ -499,3 +499,53 @@ def test_grid_fields_known_answers():
     o = Oracle(p, B0, xs)
     assert np.allclose(o.grid_fields()["cellVol"], v, rtol=1e-10)
     o.close()
+
+
+def _sym_field(a, sym):
+    """Ghosted array [nz + 2][ny + 2][nx + 2][3] moved by the mirror / swap
+    symmetry `sym` (the bits of gm_nn_input, no translation): cell (I, J)
+    reads (U, V) with 4: U <-> V, 2: V -> ny + 1 - V, 1: U -> nx + 1 - U, and
+    the x, y components follow as polar vectors."""
+    nzg, nyg, nxg = a.shape[:3]
+    I = np.arange(nxg)[None, :].repeat(nyg, 0)
+    J = np.arange(nyg)[:, None].repeat(nxg, 1)
+    U, V = (J, I) if sym & 4 else (I, J)
+    if sym & 2:
+        V = nyg - 1 - V
+    if sym & 1:
+        U = nxg - 1 - U
+    out = a[:, V, U].copy()
+    if sym & 1:
+        out[..., 0] *= -1
+    if sym & 2:
+        out[..., 1] *= -1
+    if sym & 4:
+        out[..., [0, 1]] = out[..., [1, 0]]
+    return out
+
+
+@pytest.mark.parametrize("sym", [1, 2, 4, 7])
+def test_mirror_and_swap_are_symmetries_of_the_relaxation(sym):
+    """The warm-start network's training pairs are augmented with the mirrors
+    and the x <-> y swap of the periodic cross-section (gm_nn_input,
+    gm_nn_mse), the field and the displacement moved as polar vectors.  That
+    is exact for the relaxation: the oracle run from the moved field gives the
+    moved displacement (FP64, a random braid, 6 accepted steps) with the same
+    steps, up to rounding (the x mirror evaluates the same sums in another
+    order: 3e-12 in t and in the displacement)."""
+    from glemur_gb300 import configs
+    p = configs.random_braid(4242, shape=(12, 12, 16), precision=64)
+    B0, xb = Oracle.init_state(p)
+    o = Oracle(p, B0, xb)
+    o.run(6)
+    s = o.scalars()
+    d = o.get()["xb"] - xb
+    o.close()
+    o2 = Oracle(p, _sym_field(B0, sym), xb)
+    o2.run(6)
+    s2 = o2.scalars()
+    d2 = o2.get()["xb"] - xb
+    o2.close()
+    assert s2["nAttempted"] == s["nAttempted"] and s2["t"] == pytest.approx(s["t"], rel=1e-10)
+    want = _sym_field(d, sym)[1:-1, 1:-1, 1:-1]
+    assert np.abs(d2[1:-1, 1:-1, 1:-1] - want).max() <= 1e-10 * np.abs(want).max()

@@ -260,3 +260,68 @@ def test_gpu_warm_grid_matches_host_build(smooth):
     # line-tied z ghost planes and the held first / last inner planes stay at
     # the identity (away from the periodic images, which are recomputed)
     np.testing.assert_array_equal(dev[[0, 1, -2, -1], 1:-1, 1:-1], xb0[[0, 1, -2, -1], 1:-1, 1:-1])
+
+
+def _sym_ref(a, sx, sy, sym):
+    """numpy restatement of gm_nn_input's sample move on an inner array
+    [nz][ny][nx][3]: cell (i, j) reads u = (i + sx) % nx, v = (j + sy) % ny,
+    then 4: u <-> v, 2: v -> ny - 1 - v, 1: u -> nx - 1 - u; the x, y
+    components negated (1, 2) and swapped (4)."""
+    nz, ny, nx = a.shape[:3]
+    i = np.arange(nx)[None, :].repeat(ny, 0)
+    j = np.arange(ny)[:, None].repeat(nx, 1)
+    u, v = (i + sx) % nx, (j + sy) % ny
+    if sym & 4:
+        u, v = v, u
+    if sym & 2:
+        v = ny - 1 - v
+    if sym & 1:
+        u = nx - 1 - u
+    out = a[:, v, u].astype(np.float64)
+    if sym & 1:
+        out[..., 0] *= -1
+    if sym & 2:
+        out[..., 1] *= -1
+    if sym & 4:
+        out[..., [0, 1]] = out[..., [1, 0]]
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sym", range(8))
+def test_gpu_input_and_loss_symmetries(sym):
+    """The mirror / swap augmentation of gm_nn_input and gm_nn_mse against
+    numpy, with a translation: the input channels and the loss's target."""
+    import torch
+    from glemur_gb300.warmstart import UNet
+    nx, ny, nz = 8, 8, 16
+    net = UNet((nx, ny, nz), seed=0)
+    rng = np.random.default_rng(10 + sym)
+    B0 = rng.normal(size=(nz + 2, ny + 2, nx + 2, 3)).astype(np.float32)
+    sh = (3, 5)
+    net.set_input_b0(torch.from_numpy(B0).cuda(), 32, sh, sym)
+    x = net.A["X0"][:, :3].float().cpu().numpy().reshape(nz, ny, nx, 3)
+    ref = _sym_ref(B0[1:-1, 1:-1, 1:-1], sh[0], sh[1], sym)
+    ref[..., 2] -= 1.0
+    assert np.abs(x - ref).max() < 1e-2 * np.abs(ref).max()
+    tgt = rng.normal(size=(nz, ny, nx, 3)).astype(np.float32)
+    net.zero_grad()
+    net.forward()
+    net.backward(torch.from_numpy(tgt.reshape(-1, 3)).cuda(), 1.0, sh, sym)
+    torch.cuda.synchronize()
+    y = net.A["Y"][:, :3].float().cpu().numpy().reshape(nz, ny, nx, 3).astype(np.float64)
+    e = y - _sym_ref(tgt, sh[0], sh[1], sym)
+    e[0] = 0
+    e[-1] = 0
+    assert float(net.loss_acc.item()) == pytest.approx(float((e * e).sum()), rel=1e-3)
+
+
+@pytest.mark.gpu
+def test_gpu_input_refuses_swap_on_a_rectangle():
+    import torch
+    from glemur_gb300 import GlemurError
+    from glemur_gb300.warmstart import UNet
+    net = UNet((8, 12, 16), seed=0)
+    B0 = torch.zeros((18, 14, 10, 3), dtype=torch.float32, device="cuda")
+    with pytest.raises(GlemurError):
+        net.set_input_b0(B0, 32, (0, 0), 4)
