@@ -175,13 +175,13 @@ __global__ void __launch_bounds__(128) k_conv(const ConvArgs a) {
             else ok8 = false;
             cp_async16(dA + kmajor_off(tid, c, KCH), ok8 ? src : a.in1, ok8);
         }
-        // B: the slice's Np x kcw weights of the tap.  A thread copies 8
-        // channels (cc) of rows tid % 16, tid % 16 + 16, ...: the 8 lanes of a
-        // shared-memory store phase write the 8 rows of one core matrix
+        // B: the slice's Np x kcw weights of the tap.  A thread copies the 8
+        // channels cc, cc + 64, ... (cc = 8 (tid / 16)) of rows tid % 16,
+        // tid % 16 + 16, ...: the 8 lanes of a shared-memory store phase write
+        // the 8 rows of one core matrix
         const __nv_bfloat16* Wt = a.W + ((size_t)t * a.Np + n0) * Kc + kc0;
         unsigned char* dB = stB + st * bBytes;
-        const int cc = (tid >> 4) * 8;               // KCH <= 64: eight 8-channel columns
-        if (cc < kcw)
+        for (int cc = (tid >> 4) * 8; cc < kcw; cc += 64)
             for (int r = tid & 15; r < Np; r += 16)
                 cp_async16(dB + kmajor_off(r, cc, KCH), Wt + (size_t)r * Kc + cc, true);
     };
@@ -870,7 +870,10 @@ int gm_nn_conv_wgrad(const void* dout, int ldd, int co, const void* in1, int ld1
     if (vchunk == 0) {
         // about four CTAs per SM over the grid, at least 8 steps each: fewer,
         // longer CTAs cost fewer accumulator flushes (atomics)
-        const long long chunks = (4 * 152 + tiles - 1) / tiles;
+        int dev = 0, nsm = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const long long chunks = (4LL * nsm + tiles - 1) / tiles;
         long long vc = (V + chunks - 1) / chunks;
         vc = (vc + gmnn::kWgKV - 1) / gmnn::kWgKV * gmnn::kWgKV;
         vchunk = (int)(vc < 8 * gmnn::kWgKV ? 8 * gmnn::kWgKV : vc);
