@@ -761,7 +761,28 @@ struct Impl : ImplBase {
         launches += 3 + kp.xPeri + kp.yPeri + kp.zPeri;
         CUDA_TRY(cudaMemcpyAsync(h_red, red, (gmk::R_COUNT + 1) * sizeof(double), cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
-        if (r) {
+        reduction_from_host(r);
+        return GM_OK;
+    }
+
+    // The batched run's convergence check of this case, enqueued on `stream`
+    // without waiting: the diagnostic pass and its reductions, then the
+    // reductions and the controller state copied to the pinned host buffers.
+    // After the stream has synchronised, h_st holds the state and
+    // reduction_from_host the reductions (no exported ghosts or epsilon*).
+    int enqueue_check() {
+        StageArgs<T> a = args(0);
+        CUDA_TRY(gmk::launch_stage<T>(a, gmk::MODE_DIAG, gp.pressure, grid, block, smem_diag, stream));
+        CUDA_TRY(gmk::launch_finalize<T>(part, nparts, red, stream));
+        launches += 2;
+        CUDA_TRY(cudaMemcpyAsync(h_red, red, (gmk::R_COUNT + 1) * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaMemcpyAsync(h_st, st, sizeof(DevState), cudaMemcpyDeviceToHost, stream));
+        return GM_OK;
+    }
+
+    void reduction_from_host(gm_reduction* r) const {
+        if (!r) return;
+        {
             const double* v = h_red;
             r->B2 = v[gmk::R_SUM_B2W] * gp.dx * gp.dy * gp.dz;
             r->residual = v[gmk::R_SUM_JB] > 0 ? v[gmk::R_SUM_CROSS] / v[gmk::R_SUM_JB] : 0.0;
@@ -778,7 +799,6 @@ struct Impl : ImplBase {
             r->U2 = v[gmk::R_SUM_U2] * gp.dx * gp.dy * gp.dz;
             r->UMax = v[gmk::R_MAX_U];
         }
-        return GM_OK;
     }
 
     int download(void* xb, void* B, void* J, void* D) override {
@@ -1152,20 +1172,24 @@ struct Batch : BatchBase {
         };
         while (!pending.empty()) {
             if ((rc = steps_async(checkEvery))) return rc;
+            // every running case's check on the batch stream, one wait for all
+            for (int c : pending)
+                if ((rc = cs[c]->enqueue_check())) return rc;
             CUDA_TRY(cudaStreamSynchronize(stream));
             const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             std::vector<int> still;
             for (int c : pending) {
                 Impl<T>& im = *cs[c];
-                if ((rc = im.read_state())) return rc;
                 const bool done = im.h_st->done != 0;
                 gm_reduction r;
-                if ((rc = im.refresh(&r))) return rc;
+                im.reduction_from_host(&r);
                 const double res = pointwise ? r.residualPw : r.residual;
                 const bool conv = res <= residual;
                 if (conv && !done && (rc = stop(c))) return rc;
                 if (conv || done) {
-                    if ((rc = im.read_state())) return rc;
+                    // a finished case's state and exported fields (with their
+                    // ghosts), as gm_batch_refresh leaves them
+                    if ((rc = im.refresh(nullptr))) return rc;
                     record(c, res, conv, sec);
                 } else {
                     still.push_back(c);
