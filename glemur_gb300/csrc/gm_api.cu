@@ -914,6 +914,7 @@ struct Batch : BatchBase {
     cudaStream_t stream = nullptr;
     StageArgsTMA<T>* d_cases = nullptr;
     int4* d_work = nullptr;
+    size_t work_cap = 0;                    // int4 entries d_work holds
     int* d_counters = nullptr;
     int nwork = 0, nblocks = 0, pressure = 0;
     cudaGraph_t graph = nullptr;
@@ -987,10 +988,16 @@ struct Batch : BatchBase {
                     for (int bx = 0; bx < nbx; bx++) work.push_back(make_int4(o.second, bx, by, bz));
         }
         CUDA_TRY(cudaStreamSynchronize(stream));
-        if (d_work) CUDA_TRY(cudaFree(d_work));
-        d_work = nullptr;
         nwork = (int)work.size();
-        CUDA_TRY(cudaMalloc((void**)&d_work, work.size() * sizeof(int4)));
+        if (work.size() > work_cap) {
+            // reallocated only when the list outgrows it (during a run the
+            // list shrinks as cases finish)
+            if (d_work) CUDA_TRY(cudaFree(d_work));
+            d_work = nullptr;
+            work_cap = 0;
+            CUDA_TRY(cudaMalloc((void**)&d_work, work.size() * sizeof(int4)));
+            work_cap = work.size();
+        }
         CUDA_TRY(cudaMemcpyAsync(d_cases, hcases.data(), ncases * sizeof(StageArgsTMA<T>), cudaMemcpyHostToDevice,
                                  stream));
         CUDA_TRY(cudaMemcpyAsync(d_work, work.data(), work.size() * sizeof(int4), cudaMemcpyHostToDevice, stream));

@@ -11,10 +11,11 @@ down (24, 48 and wb channels, 2x2x2 mean pooling between levels), nearest
 upsampling and concatenation with the skip on the way up (48, 24 channels),
 and a 3x3x3 head to 3 channels: the displacement in grid spacings.  The
 bottleneck width wb is 192 for networks trained here (1.79 M parameters; 96
-gives 0.80 M); a weights file records it in the shapes of its arrays.  Padding
-is periodic in x, y and zero in z.  The displacement of the first and last
-z-planes is imposed to be zero, and a predicted grid whose cells are not all
-positive (min Delta <= 0) is rejected in favour of the identity grid.
+gives 0.80 M parameters); a weights file records it in the shapes of its
+arrays.  Padding is periodic in x, y and zero in z.  The displacement of the
+first and last z-planes is imposed to be zero, and a predicted grid whose
+cells are not all positive (min Delta <= 0) is rejected in favour of the
+identity grid.
 """
 from __future__ import annotations
 
