@@ -219,6 +219,12 @@ class NvmlClocks:
         if self.thread is not None:
             self.stop = True
             self.thread.join(timeout=2)
+        if self.lib is not None:
+            try:
+                self.lib.nvmlShutdown()
+            except Exception:
+                pass
+            self.lib = None
 
     def summary(self):
         if not self.samples:

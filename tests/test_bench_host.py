@@ -25,6 +25,28 @@ def test_clock_summary_median_and_reasons():
     assert s["reasons"] == ["hw_slowdown", "sw_power_cap"] and s["samples"] == 6
 
 
+def test_nvml_sampler_summary_and_fallback():
+    """The NVML sampler's summary (median SM clock, clock-event reason bits
+    decoded), and its behaviour without NVML: no thread, no summary, so the
+    bench line falls back to the nvidia-smi record."""
+    c = bench.NvmlClocks.__new__(bench.NvmlClocks)
+    c.lib, c.max_mhz = None, 2070.0
+    c.samples = [(2070.0, 0), (2055.0, 0x4), (2070.0, 0)]
+    s = c.summary()
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 3
+    assert s["reasons"] == ["sw_power_cap"] and s["sampler"].startswith("nvml")
+    c.samples.append((1500.0, 0x8 | 0x40))
+    assert c.summary()["reasons"] == ["hw_slowdown", "hw_thermal_slowdown", "sw_power_cap"]
+    c.samples = []
+    assert c.summary() is None
+    # a library that is not there: the context manager starts nothing
+    n = bench.NvmlClocks.__new__(bench.NvmlClocks)
+    n.lib, n.samples = None, []
+    with n as ck:
+        pass
+    assert ck.thread is None and ck.summary() is None
+
+
 def test_clock_summary_without_samples():
     assert _clocks("", sampled=False).summary()["reasons"] == ["unsampled"]
     assert _clocks("garbage\n[N/A]\n").summary()["reasons"] == ["unsampled"]
