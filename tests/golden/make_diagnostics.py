@@ -14,7 +14,7 @@ from the reference's kernels dirCellVol, gridConvexity, gridWedgeMin
 epsilonStar + findDevMax, src/diagnostics.cu:32-47), errB_1ez and
 errXb_XbAn (src/diagnostics.cu:51-71).
 
-Needs a GPU; run on the GPU machine after the build:
+Needs a GPU; run it on a GB300 after the build:
   python tests/golden/make_diagnostics.py [OUT_DIR]
 """
 from __future__ import annotations

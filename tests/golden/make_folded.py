@@ -15,7 +15,7 @@ at that grid, as after an accepted step (src/main.cu:343-353).  Stored:
   J_<method>  J of each method (inner points); StokesTri is NaN where a
               plane takes a triangle
 
-Needs a GPU; run on the GPU machine after the build:
+Needs a GPU; run it on a GB300 after the build:
   python tests/golden/make_folded.py [OUT_DIR]
 """
 from __future__ import annotations

@@ -15,7 +15,7 @@ their outputs as tests/golden/<case>.npz:
   u1, unew1, uN     with inertia: the velocity after stage 0, u_new of the
                     first step and the velocity after N_ACCEPTED steps
 
-Needs a GPU; run on the GPU machine after the build:
+Needs a GPU; run it on a GB300 after the build:
   python tests/golden/make_golden.py [OUT_DIR [CASE ...]]
 """
 from __future__ import annotations
