@@ -337,6 +337,26 @@ def first_reach(hist, level, offset=0.0):
     return None, None
 
 
+def level_times(plain, warm, t_net, folded, levels=LARGE_LEVELS):
+    """Per residual level: the plain run's and the warm-started run's time and
+    attempts to reach it (residual_history entries), the warm start's own
+    cost t_net included.  A warm grid that folded during its run is replaced
+    by the identity grid: its levels are then the plain run's, plus the time
+    and attempts the folded run took."""
+    out = {}
+    spent, spent_att = warm[-1][0] + t_net, warm[-1][1]
+    for lv in levels:
+        tp, ap = first_reach(plain, lv)
+        if folded:
+            tw, aw = first_reach(plain, lv, spent)
+            aw = aw + spent_att if aw is not None else None
+        else:
+            tw, aw = first_reach(warm, lv, t_net)
+        out[str(lv)] = dict(plain_s=tp, plain_attempts=ap, warm_s=tw, warm_attempts=aw,
+                            speedup=(tp / tw) if (tp and tw) else None)
+    return out
+
+
 def evaluate_large(weights, residual, max_attempts, factors=(2, 4), log=print):
     """The large case (256x256x512, k = +-1.2, pressure with the p0 profile):
     the network runs on B0 averaged over f x f x f blocks and its displacement
@@ -391,19 +411,9 @@ def evaluate_large(weights, residual, max_attempts, factors=(2, 4), log=print):
         del net
         warm, wstat = residual_history(g, xw, B0, max_attempts, residual)
         folded = bool(wstat & 0x7) and warm[-1][2] > residual
-        spent = warm[-1][0] + t_net
-        levels = {}
-        for lv in LARGE_LEVELS:
-            tp, ap = first_reach(plain, lv)
-            if folded:
-                tw, aw = first_reach(plain, lv, spent)
-                aw = aw + warm[-1][1] if aw is not None else None
-            else:
-                tw, aw = first_reach(warm, lv, t_net)
-            levels[str(lv)] = dict(plain_s=tp, plain_attempts=ap, warm_s=tw, warm_attempts=aw,
-                                   speedup=(tp / tw) if (tp and tw) else None)
+        levels = level_times(plain, warm, t_net, folded)
         out["warm"][str(f)] = dict(coarse_shape=cshape, accepted=bool(accepted), net_s=t_net, res0=warm[0][2],
-                                   res_end=warm[-1][2], attempts=warm[-1][1], s=spent, status=wstat,
+                                   res_end=warm[-1][2], attempts=warm[-1][1], s=warm[-1][0] + t_net, status=wstat,
                                    folded_in_run=folded, minDet=min(h[3] for h in warm), levels=levels,
                                    history=[(round(h[0], 3), h[1], h[2]) for h in warm[::5]])
         log(f"large warm, factor {f}: {out['warm'][str(f)]}")
